@@ -1,0 +1,379 @@
+"""Benchmark of the probe-particle AFM hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload slab_molecule]
+                    [--impl ours|reference] [--cpu-budget S] [--no-cpu-baseline]
+
+One step = one full pass of the reference CPU pipeline's work on the workload: the
+Lennard-Jones + point-charge force field with the Fmax clamps and FF = FFLJ + Q*FFel
+(one fused kernel), the relaxed scan with FIRE at every pixel and height, and Fz -> Δf
+(fused into the relaxation kernel).  Default workload: the 2000-atom slab + 60-atom
+molecule, 800x800x500 grid, 512x512x40 scan (the large single system).
+
+Printed (rank 0, one JSON line): value = relaxed pixel-heights per second of the whole
+step with the atoms already in device memory; e2e = the same metric through the public
+host API (ppafm_gb300.HighLevel.Pipeline with host atoms in and host fzs/positions/Δf
+out, copies inside the timed region); roofline of the dominant kernel (force field,
+float32-FMA bound) against an FFMA peak measured in the same process; the CPU baseline
+(the reference pipeline on this host's cores, bounded sample, extrapolated).
+
+Multi-GPU (torchrun, N > 1): every rank relaxes its own independent system (weak scaling,
+no collective on the data path); value = all ranks' pixel-heights / max rank time.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "relaxed pixel-z points/s & FF grid-pt·atoms/s; FIRE iters/pixel at 1e-4 eV/Å"
+UNIT = "pixel-z/s"
+FLOPS_LJ_PAIR = 26  # float32 flops per atom-point pair, FMA = 2 (LJ only)
+FLOPS_LJC_PAIR = 30  # LJ + Coulomb sharing r^2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(name, seed, scale):
+    from ppafm_gb300 import workloads
+
+    return getattr(workloads, name)(seed=seed, scale=scale)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": float(max(smax)) if smax else None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_profile_traffic(workload):
+    """DRAM bytes per force-field launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"ff_kernel_{workload}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def ffma_peak_tflops(torch, lib, check, tptr, stream_handle):
+    """FP32 FMA peak of this GPU measured now: dependent FFMA chains on every SM."""
+    import ctypes
+
+    scratch = torch.zeros(1024, device="cuda")
+    cnt = ctypes.c_longlong(0)
+    iters = 20000
+    for _ in range(2):
+        check(lib.ppgpu_ffma_peak(tptr(scratch), iters, ctypes.byref(cnt), stream_handle()))
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        check(lib.ppgpu_ffma_peak(tptr(scratch), iters, ctypes.byref(cnt), stream_handle()))
+        b.record()
+        b.synchronize()
+        t = a.elapsed_time(b) * 1e-3
+        best = max(best, 2.0 * cnt.value / t / 1e12)
+    return best
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = make_workload(args.workload, args.seed + rank, args.scale)
+    relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    pl = HL.Pipeline(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w["gridN"], w, relax=relax, want_iters=False)
+    nx, ny, nz = pl.scan_shape
+    units = nx * ny * nz
+    npts = int(np.prod(pl.gridN))
+    natoms = pl.natoms
+    nch = pl.ncharged
+    st = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---------------- device-resident steps
+    for _ in range(args.warmup):
+        pl.run()
+    torch.cuda.synchronize()
+    pl.counter.zero_()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for e0, e1, e2 in ev:
+        e0.record(st)
+        pl.build_ff()
+        e1.record(st)
+        pl.relax()
+        e2.record(st)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    t_ff = [a.elapsed_time(b) * 1e-3 for a, b, _ in ev]
+    t_rx = [b.elapsed_time(c) * 1e-3 for _, b, c in ev]
+    t_step = sum(a.elapsed_time(c) * 1e-3 for a, _, c in ev)
+    iters_total = int(pl.counter.item())
+    _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
+
+    # ---------------- end to end through the host API
+    import ctypes  # noqa: F401
+
+    host_in = {k: np.asarray(w[k]).copy() for k in ("Zs", "Rs", "Qs")}
+    pin_out = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in pl.out.items()}
+    rec_pinned = torch.empty(pl.atoms.shape, dtype=pl.atoms.dtype, pin_memory=True)
+
+    def e2e_step():
+        # host prep (PBC images, LJ mixing, packing) + H2D of the atom records
+        Rs0, cLJs, kqq = HL.prepare_atoms(host_in["Zs"], host_in["Rs"], host_in["Qs"], pl.lvec, w)
+        from ppafm_gb300.device import pack_atoms
+
+        rec, _, _ = pack_atoms(Rs0, cLJs, kqq if pl.Q != 0.0 else None, device="cpu")
+        rec_pinned.copy_(rec)
+        pl.atoms.copy_(rec_pinned, non_blocking=True)
+        pl.run()
+        for k, v in pl.out.items():
+            pin_out[k].copy_(v, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(args.steps):
+        e2e_step()
+    b.record(st)
+    b.synchronize()
+    barrier()
+    t_e2e = a.elapsed_time(b) * 1e-3
+    h2d = int(rec_pinned.numel() * rec_pinned.element_size())
+    d2h = int(sum(v.numel() * v.element_size() for v in pin_out.values()))
+
+    # ---------------- max over ranks
+    t_step_max, t_e2e_max = t_step, t_e2e
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step_max, t_e2e_max = float(tt[0]), float(tt[1])
+    K = args.steps
+    value = units * world * K / t_step_max
+    e2e_value = units * world * K / t_e2e_max
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return None
+
+    # ---------------- roofline (force-field kernel, float32 FMA bound)
+    peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
+    t_ff_avg = float(np.mean(t_ff))
+    if pl.Q != 0.0:
+        flops = npts * ((natoms - nch) * FLOPS_LJ_PAIR + nch * FLOPS_LJC_PAIR)
+    else:
+        flops = npts * natoms * FLOPS_LJ_PAIR
+    achieved = flops / t_ff_avg / 1e12
+    traffic = read_profile_traffic(args.workload)
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            from oracle import cpu_baseline
+
+            s = cpu_baseline.sample_pipeline(w, budget_s=args.cpu_budget)
+            cpu = {"value": s["pixel_z_per_s"], "unit": UNIT, "cores": s["cores"], "kind": s["kind"], "sample": s["sample"], "ff_grid_pt_atoms_per_s": s["ff_pairs_per_s"], "seconds_full_job": s["seconds_full_job"]}
+        except Exception as e:  # the baseline is reported, never fatal
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_step_max / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {
+            "workload": args.workload,
+            "atoms": len(w["Zs"]),
+            "atoms_with_images": natoms,
+            "charged_atoms_with_images": nch,
+            "grid": list(pl.gridN),
+            "scan": [nx, ny, nz],
+            "fire": relax,
+            "probe": {"klat": w["klat"], "krad": w["krad"], "r0": list(w["r0Probe"]), "Q": w["charge"]},
+            "df": {"f0": w["f0Cantilever"], "k": w["kCantilever"], "A": w["Amplitude"]},
+            "l2": "inputs larger than L2 (force field %.2f GB)" % (npts * 16 / 1e9),
+            "parallelism": f"replicas x{world}",
+        },
+        "ff_grid_pt_atoms_per_s": npts * natoms / t_ff_avg,
+        "fire_iters_per_pixel_z": iters_total / (units * K),
+        "stage_ms": {"force_field": 1e3 * t_ff_avg, "relax_and_df": 1e3 * float(np.mean(t_rx))},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * K,
+        "roofline": {
+            "bound": "fp32",
+            "kernel": "ff_kernel<LJC> (force field)",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None,
+            "peak_source": "FFMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP32 figure)",
+            "flops_per_launch": flops,
+            "traffic": traffic,
+        },
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return line
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from oracle import cpu_baseline
+
+    w = make_workload(args.workload, args.seed, args.scale)
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        s = cpu_baseline.sample_pipeline(w, budget_s=args.cpu_budget / 2, seed=i)
+        if i >= args.warmup:
+            vals.append(s["pixel_z_per_s"])
+            info = s
+    v = float(np.median(vals))
+    from ppafm_gb300 import common as C
+
+    xT, yT, zT, _ = C.prepareScanGrids(w["scanMin"], w["scanMax"], w["scanStep"], w["r0Probe"])
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * len(xT) * len(yT) * len(zT) / v,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "grid": list(w["gridN"]), "scan": [len(xT), len(yT), len(zT)], "parallelism": "host cores"},
+        "ff_grid_pt_atoms_per_s": info["ff_pairs_per_s"],
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": info["sample"], "seconds_full_job": info["seconds_full_job"]},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,188 @@
+/*
+ * ppgpu.h -- C ABI of libppgpu.so, the GB300 (sm_103a) probe-particle AFM hot path.
+ *
+ * Two layers share one library:
+ *
+ *  1. Drop-in symbols.  The exact names and signatures that the reference's ctypes
+ *     layer (ppafm/core.py) binds from ProbeParticle_lib.so, for the in-scope subset.
+ *     They keep the reference's process-global state and host (numpy) float64 buffers;
+ *     each call mirrors what it needs to the GPU and writes results back into the
+ *     caller's arrays.  A ctypes binding written for the reference binds these unchanged.
+ *
+ *  2. Device API (ppgpu_*).  Plain device pointers, sizes and a CUDA stream (void*,
+ *     NULL = legacy default stream).  Every function returns a status code; no function
+ *     takes ownership of caller memory.  Force grids are interleaved float4
+ *     (Fx, Fy, Fz, E) in C order [n0][n1][n2] (the reference's i3D order, Grid.h:16).
+ *
+ * Errors: every ppgpu_* call returns PPGPU_OK or an error code, with a message in
+ * ppgpu_last_error().  The drop-in symbols return void like the reference; they set the
+ * same last-error state (read it with ppgpu_last_error()/ppgpu_last_status()).
+ * Device-side waits are bounded: a kernel that gives up sets a device error word that
+ * ppgpu_device_status() reads (PPGPU_ERR_DEVICE_TIMEOUT) instead of hanging.
+ */
+#ifndef PPGPU_H
+#define PPGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define PPGPU_OK 0
+#define PPGPU_ERR_ARG 1            /* invalid argument (sizes, null pointers, modes) */
+#define PPGPU_ERR_CUDA 2           /* a CUDA runtime / cuFFT call failed */
+#define PPGPU_ERR_STATE 3          /* drop-in call before the state it needs was set */
+#define PPGPU_ERR_DEVICE_TIMEOUT 4 /* a bounded device-side wait gave up */
+#define PPGPU_ERR_NO_DEVICE 5      /* no CUDA device / wrong architecture */
+
+const char *ppgpu_last_error(void);
+int ppgpu_last_status(void);
+/* Synchronises `stream`, returns PPGPU_OK or the device error recorded by a kernel
+ * (and clears it). */
+int ppgpu_device_status(void *stream);
+/* Library/device description: writes "sm_XY <name>" into buf. */
+int ppgpu_device_info(char *buf, int len);
+
+/* =============================================================== 1. drop-in symbols */
+
+/* ProbeParticle.cpp:358  (ppafm/core.py:38) */
+void setGridN(int *n);
+/* ProbeParticle.cpp:365  (core.py:48) -- cell: 3x3 row vectors a,b,c */
+void setGridCell(double *cell);
+/* ProbeParticle.cpp:338  (core.py:59) -- borrows the caller's [n0,n1,n2,3] float64 grid */
+void setFF_Fpointer(double *gridF);
+/* ProbeParticle.cpp:343  (core.py:69) -- borrows the caller's [n0,n1,n2] float64 grid */
+void setFF_Epointer(double *gridE);
+/* ProbeParticle.cpp:348  (core.py:79) */
+void deleteFF_Fpointer(void);
+/* ProbeParticle.cpp:353  (core.py:88) */
+void deleteFF_Epointer(void);
+/* ProbeParticle.cpp:322  (core.py:97; the reference wrapper is broken, the symbol is not) */
+void setRelax(int maxIters, double convF2, double dt, double damping);
+/* ProbeParticle.cpp:331  (core.py:106) */
+void setFIRE(double finc, double fdec, double falpha);
+/* ProbeParticle.cpp:371  (core.py:115) -- rPP0 is made consistent with lRad when kRad != 0 */
+void setTip(double lRad, double kRad, double *rPP0, double *kSpring);
+/* ProbeParticle.cpp:508  (core.py:193) -- gridF (+gridE if set) += LJ field of the atoms */
+void getLennardJonesFF(int natoms, double *Ratoms, double *cLJs);
+/* ProbeParticle.cpp:540  (core.py:270) -- kind 0 = s, 1 = pz, 2 = dz2 tip */
+void getCoulombFF(int natoms, double *Ratoms, double *kQQs, int kind);
+/* ProbeParticle.cpp:633  (core.py:312) -- returns the stroke's iteration sum.
+ * splineParams must be NULL: the radial tip spline is not part of this library. */
+int relaxTipStroke(int probeStart, int relaxAlg, int nstep, double *rTips, double *rs, double *fs,
+                   void *splineParams);
+/* ProbeParticle.cpp:682  (core.py:322) -- returns 0 like the reference; the total
+ * iteration count of the call is available from ppgpu_last_iterations(). */
+int relaxTipStrokes_omp(int nx, int ny, int probeStart, int relaxAlg, int nstep, double *rTips, double *rs,
+                        double *fs, void *splineParams);
+/* Total FIRE iterations of the last relaxTipStroke(s) call (no reference counterpart:
+ * the reference discards them, ProbeParticle.cpp:682-701). */
+long long ppgpu_last_iterations(void);
+
+/* ================================================================== 2. device API */
+
+/* ---------------------------------------------------------------- atom records
+ * Force-field kernels read atoms as packed 48-byte records (12 floats):
+ *   [x_hi, y_hi, z_hi, kqq] [x_lo, y_lo, z_lo, 0] [c6, c12, 6*c6, 12*c12]
+ * where x = x_hi + x_lo splits the float64 coordinate (relative to the grid origin)
+ * into two floats, kqq = k_e*Q_atom*(charge weight) and (c6, c12) are the
+ * Lennard-Jones coefficients.  The first `ncharged` records are the atoms with
+ * kqq != 0.  ppgpu_pack_atoms builds this layout on the host. */
+#define PPGPU_ATOM_FLOATS 12
+int ppgpu_pack_atoms(int natoms, const double *R, const double *cLJ, const double *kqq, float *out,
+                     int *ncharged_out);
+
+/* ---------------------------------------------------------------- FF generation
+ * mode:
+ *   PPGPU_FF_LJ        F += sum_i LJ(p - R_i)                     (getLennardJonesFF)
+ *   PPGPU_FF_COULOMB   F += sum_i Coulomb_kind(p - R_i)            (getCoulombFF, coul_kind 0/1/2)
+ *   PPGPU_FF_LJC       F  = clamp(F_LJ) + Q * clamp(F_el)          (perform_relaxation's
+ *                      FF = FFLJ + Q*FFel after computeLJ / computeELFF_pointCharge clamps,
+ *                      HighLevel.py:143-145, 294-296, 374-376; clamp skipped when Fmax <= 0)
+ *   PPGPU_FF_QZS       F  = LJ + sum_k Qs[k]*k_e*Coulomb(p + QZs[k] z) (AFMulator point-charge,
+ *                      FF.cl:366-423), R2SAFE 1e-6
+ * flags: PPGPU_FF_WITH_E (also E in .w; otherwise .w = 0), PPGPU_FF_ACCUMULATE (add into FE),
+ *        PPGPU_FF_F64 (float64 sums; result still stored as float4).
+ * Grid point (ia,ib,ic) sits at origin + ia*a/n0 + ib*b/n1 + ic*c/n2; atom coordinates
+ * in the records are relative to `origin`.  cell: rows a, b, c (float64, host). */
+#define PPGPU_FF_LJ 0
+#define PPGPU_FF_COULOMB 1
+#define PPGPU_FF_LJC 2
+#define PPGPU_FF_QZS 3
+#define PPGPU_FF_WITH_E 1
+#define PPGPU_FF_ACCUMULATE 2
+#define PPGPU_FF_F64 4 /* evaluate the sums in float64 (the GPU error oracle); always on for
+                          the pz/dz2 Coulomb tips, whose finite differences need it */
+int ppgpu_ff_grid(float *FE, const int *n, const double *cell, const float *atoms, int natoms, int ncharged,
+                  int mode, int coul_kind, double Q, double Fmax, const double *Qs, const double *QZs, int flags,
+                  void *stream);
+
+/* Sub-box variant: fills FE[ns0][ns1][ns2] with the points [i0, i0+ns) of the full grid n. */
+int ppgpu_ff_subgrid(float *FE, const int *n, const double *cell, const int *i0, const int *ns,
+                     const float *atoms, int natoms, int ncharged, int mode, int coul_kind, double Q,
+                     double Fmax, const double *Qs, const double *QZs, int flags, void *stream);
+
+/* ------------------------------------------------------------------- relaxation
+ * Tip/relaxation parameters shared by the relax entry points (float64, host):
+ *   prm[0]  maxIters        prm[1] convF2    prm[2] dt (= dtmax)  prm[3] damping (= acoef0)
+ *   prm[4]  finc            prm[5] fdec      prm[6] falpha
+ *   prm[7]  lRadial         prm[8] kRadial   prm[9..11] rPP0 (consistent)  prm[12..14] kSpring
+ * (ProbeParticle.cpp:51-114; set by setRelax/setFIRE/setTip.) */
+#define PPGPU_RELAX_NPARAM 15
+
+/* relaxTipStrokes_omp semantics on device buffers: stroke s uses rTips[s*nstep .. +nstep)
+ * (float64 xyz, relative to the grid origin); writes rs, fs (float64 xyz) and, when
+ * non-NULL, iters[s*nstep+i] (int32) and itrsum[s] (int32).  iter_total (nullable, device
+ * u64) accumulates all iterations.  probeStart -1/0/1, relaxAlg 0 (damped MD) / 1 (FIRE). */
+int ppgpu_relax_strokes(const float *FE, const int *n, const double *cell, const double *prm, int probeStart,
+                        int relaxAlg, int nstroke, int nstep, const double *rTips, double *rs, double *fs,
+                        int *iters, int *itrsum, unsigned long long *iter_total, void *stream);
+
+/* relaxedScan3D_omp + Fz2df semantics on a regular scan (HighLevel.py:104-124,
+ * common.py:421-430): tips at (xs[ix], ys[iy], zs[iz]) with zs descending (the approach
+ * order) and coordinates relative to the grid origin; pixel p = ix*ny + iy.
+ * Outputs (ascending z, like the reference's reversed arrays; each nullable):
+ *   fzs   [nx][ny][nz]   float32   grid Fz at the relaxed position
+ *   ppos  [nx][ny][nz][3] float32  relaxed position + pos_offset[3]
+ *   iters [nx][ny][nz]   int32
+ *   df    [nx][ny][nz-nw+1] float32 = sum_i fzs[j+i]*W[nw-1-i]  (np.convolve 'valid'),
+ *         W = df_weights (already scaled by units*f0/k0), nw <= 64; df NULL skips it. */
+int ppgpu_relax_scan(const float *FE, const int *n, const double *cell, const double *prm, int nx, int ny, int nz,
+                     const double *xs, const double *ys, const double *zs, const double *pos_offset, float *fzs,
+                     float *ppos, int *iters, int nw, const double *df_weights, float *df,
+                     unsigned long long *iter_total, void *stream);
+
+/* AFMulator relaxation (relaxStrokesTilted, relax.cl:391-464, + convolveZ, relax.cl:571-608):
+ * prm_afm[0..3] relax_params (dt, damp, -, -), [4..7] stiffness (kx,ky,kz,kr) already divided
+ * by -eVA_Nm, [8..11] dpos0 (x,y,z,l0), [12..23] tip rows A,B,C (4 each, C[3] = -zstep),
+ * [24..27] surfFF.  inv_cell: rows of transpose(inv(cell)) (fractional coordinates).
+ * points: [npix][4] float32 tip start positions relative to the FF origin.
+ * Outputs (nullable): FEs/paths [npix][nz][4] float32 (scan order), iters [npix][nz] int32,
+ * X [npix][nz-nw+1] float32 = sum_j FEs[o+j].z * W[j] (no flip). */
+#define PPGPU_AFM_NPARAM 28
+int ppgpu_relax_afm(const float *FE, const int *n, const double *inv_cell, const double *prm_afm, int npix,
+                    const float *points, int nz, float *FEs, float *paths, int *iters, int nw,
+                    const double *weights, float *X, unsigned long long *iter_total, void *stream);
+
+/* -------------------------------------------------------------- grid utilities */
+/* Fz -> df along the last axis: out[c][j] = scale * sum_i F[c][j+i] * W[nw-1-i]. */
+int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const double *W, double scale, float *out,
+                void *stream);
+/* |F| <= Fmax clamp of a float4 grid, direction preserved (io.py:766-778). */
+int ppgpu_clamp_grid(float *FE, long long npts, double Fmax, void *stream);
+/* FE_out = a*FE_a + b*FE_b (float4 grids; E included). */
+int ppgpu_axpby_grid(float *FE_out, const float *FE_a, double a, const float *FE_b, double b, long long npts,
+                     void *stream);
+/* float64 [npts,3] (+ optional [npts] energy) <-> float4 conversions. */
+int ppgpu_grid_from_f64(float *FE, const double *F3, const double *E, long long npts, void *stream);
+int ppgpu_grid_to_f64(double *F3, double *E, const float *FE, long long npts, int accumulate, void *stream);
+
+/* ------------------------------------------------------------ measurement helper */
+/* Runs a dependent-FFMA kernel for `iters` iterations on all SMs and returns the number
+ * of FP32 FMAs executed (the caller times it) -- the FP32 roofline denominator. */
+int ppgpu_ffma_peak(float *scratch, int iters, long long *fma_count, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PPGPU_H */

@@ -1,0 +1,183 @@
+"""Bounded CPU timing sample of the reference pipeline -- TEST/BENCH INFRASTRUCTURE ONLY.
+
+Times the reference's CPU hot path for a workload on the host cores and extrapolates to
+the full job.  The pipeline is the reference's own composition (HighLevel.computeLJ +
+computeELFF_pointCharge with the Fmax clamp, perform_relaxation's FF = FFLJ + Q*FFel,
+relaxTipStrokes_omp, common.Fz2df), run either by the reference core compiled from its
+sources (oracle/_ref, kind "reference") or by the C restatement (libpporacle, kind "port").
+
+Sample, chosen so one call takes roughly ``budget_s`` seconds:
+  * force field: a slab of whole z-planes of the full grid (cost is exactly linear in
+    grid points x atoms), LJ and Coulomb passes over all atoms like the reference;
+  * clamp and FF composition (numpy): timed on the same slab;
+  * relaxation: blocks of adjacent pixel columns (one over the molecule, one at a seeded
+    random place); the force field is filled on a box around each block (not timed) and
+    the strokes are relaxed with the reference's FIRE;
+  * Fz -> Δf: numpy convolution on the sampled columns.
+Each stage's time per unit (grid point, pixel-height) is scaled to the full workload.
+"""
+
+import ctypes
+import os
+import time
+
+import numpy as np
+
+from . import oracle as O
+
+
+def _ref_lib():
+    return O.Reference() if O.reference_available() else None
+
+
+def _prep(w):
+    """Atoms after in-plane PBC, LJ coefficients, kqq, shifted to the grid origin."""
+    from ppafm_gb300 import common as C
+
+    FFp = C.loadSpecies()
+    lv = np.asarray(w["lvec"], dtype=np.float64)
+    iZ, R, Q = O.PBCAtoms(np.asarray(w["Zs"]), np.asarray(w["Rs"], np.float64), np.asarray(w["Qs"], np.float64), lv[1], lv[2], w["nPBC"][0], w["nPBC"][1])
+    FFarr = np.array([(r[0], r[1], r[2]) for r in FFp])
+    cLJ = O.getAtomsLJ(int(w["probeType"]), iZ, FFarr)
+    return np.ascontiguousarray(R - lv[0]), np.ascontiguousarray(cLJ), np.ascontiguousarray(Q * O.CoulombConst)
+
+
+def _ff_slab(ref, n, cell, R, coefs, kind, iz0, nzs, nthreads):
+    """One force-field pass over the z-planes [iz0, iz0+nzs) of the full grid."""
+    if ref is None:
+        F, _ = O.ff_subgrid(n, cell, (0, 0, iz0), (n[0], n[1], nzs), R, coefs, kind, nthreads=nthreads)
+        return F
+    dC = np.asarray(cell[2]) / n[2]
+    sub_cell = np.array(cell, dtype=np.float64).copy()
+    sub_cell[2] = dC * nzs
+    ref.set_grid(np.array([n[0], n[1], nzs], np.int32), sub_cell)
+    F = np.zeros((n[0], n[1], nzs, 3))
+    ref.L.setFF_Fpointer(F)
+    Rs = np.ascontiguousarray(R - iz0 * dC)
+    if kind < 0:
+        ref.L.getLennardJonesFF(len(Rs), Rs, np.ascontiguousarray(coefs).reshape(-1, 2))
+    else:
+        ref.L.getCoulombFF(len(Rs), Rs, np.ascontiguousarray(coefs), kind)
+    return F
+
+
+def sample_pipeline(w, budget_s=20.0, nthreads=0, use_reference=True, seed=0):
+    """Returns a dict with per-stage seconds for the full job, pixel-z/s, pair rate,
+    cores, kind and a description of the sample."""
+    ref = _ref_lib() if use_reference else None
+    kind = "reference" if ref is not None else "port"
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(nthreads)
+    n = np.array(w["gridN"], np.int32)
+    lv = np.asarray(w["lvec"], np.float64)
+    cell = lv[1:4]
+    R, cLJ, kqq = _prep(w)
+    na = len(R)
+    npts = int(np.prod(n.astype(np.int64)))
+    from ppafm_gb300 import common as C
+
+    xT, yT, zT, _ = C.prepareScanGrids(w["scanMin"], w["scanMax"], w["scanStep"], w["r0Probe"])
+    P = len(xT) * len(yT)
+    Z = len(zT)
+
+    # ---- force field: calibrate on a few rows, then one timed slab
+    t0 = time.perf_counter()
+    _ = O.ff_subgrid(n, cell, (0, 0, 0), (1, min(16, n[1]), min(8, n[2])), R, cLJ, -1, nthreads=nthreads)
+    t_cal = max(time.perf_counter() - t0, 1e-4)
+    rate = (min(16, n[1]) * min(8, n[2])) / t_cal  # points/s of one pass, roughly
+    plane = int(n[0]) * int(n[1])
+    nzs = int(max(1, min(n[2], (0.3 * budget_s * rate) / plane)))
+    iz0 = int(n[2] // 2)
+    if iz0 + nzs > n[2]:
+        iz0 = int(n[2]) - nzs
+    t0 = time.perf_counter()
+    Fl = _ff_slab(ref, n, cell, R, cLJ, -1, iz0, nzs, nthreads)
+    t_lj = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Fe = _ff_slab(ref, n, cell, R, kqq, 0, iz0, nzs, nthreads)
+    t_el = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.limit_vec_field(Fl, 10.0)
+    O.limit_vec_field(Fe, 10.0)
+    FFs = Fl.copy()
+    FFs += Fe * w["charge"]
+    t_np = time.perf_counter() - t0
+    scale_ff = npts / float(plane * nzs)
+
+    # ---- relaxation on pixel blocks
+    rng = np.random.default_rng(seed)
+    nb = 4
+    blocks = [(len(xT) // 2 - nb // 2, len(yT) // 2 - nb // 2), (int(rng.integers(0, len(xT) - nb)), int(rng.integers(0, len(yT) - nb)))]
+    ds = np.linalg.norm(cell, axis=1) / n
+    r0 = w["r0Probe"]
+    stiff = [w["klat"], w["klat"], w["krad"]]
+    tip = O.tip_params(r0[2], stiff[2] / -O.eVA_Nm, [r0[0], r0[1], 0.0], np.array([stiff[0], stiff[1], 0.0]) / -O.eVA_Nm)
+    prm = O.relax_param_vector(tip, maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    t_relax = 0.0
+    nrel = 0
+    fz_cols = []
+    patch_ok = True
+    FFbox = np.zeros(tuple(n) + (3,))  # lazily committed: only the boxes are touched
+    for bx, by in blocks:
+        xs = xT[bx : bx + nb] - lv[0, 0]
+        ys = yT[by : by + nb] - lv[0, 1]
+        lo = np.array([xs.min() - 1.5, ys.min() - 1.5, zT.min() - lv[0, 2] - r0[2] - 1.5])
+        hi = np.array([xs.max() + 1.5, ys.max() + 1.5, zT.max() - lv[0, 2] - r0[2] + 1.5])
+        i_lo = np.floor(lo / ds).astype(int)
+        i_hi = np.ceil(hi / ds).astype(int) + 1
+        ns = i_hi - i_lo
+        for k in range(3):
+            if i_lo[k] < 0 or i_hi[k] > n[k]:
+                ns[k] = min(ns[k], n[k])
+                i_lo[k] = max(0, min(i_lo[k], n[k] - ns[k]))
+        Fb, _ = O.ff_subgrid(n, cell, i_lo, ns, R, cLJ, -1, nthreads=nthreads)
+        Fq, _ = O.ff_subgrid(n, cell, i_lo, ns, R, kqq, 0, nthreads=nthreads)
+        O.limit_vec_field(Fb, 10.0)
+        O.limit_vec_field(Fq, 10.0)
+        FFbox[i_lo[0] : i_lo[0] + ns[0], i_lo[1] : i_lo[1] + ns[1], i_lo[2] : i_lo[2] + ns[2]] = Fb + Fq * w["charge"]
+        rT = np.zeros((nb, nb, Z, 3))
+        rT[..., 0] = xs[:, None, None]
+        rT[..., 1] = ys[None, :, None]
+        rT[..., 2] = (zT[::-1] - lv[0, 2])[None, None, :]
+        t0 = time.perf_counter()
+        if ref is not None:
+            L = ref.L
+            ref.set_grid(n, cell)
+            L.setFF_Fpointer(FFbox)
+            L.setRelax(int(w["maxIters"]), float(w["convF2"]), float(w["dt"]), float(w["damping"]))
+            L.setFIRE(1.1, 0.5, 0.99)
+            L.setTip(float(r0[2]), stiff[2] / -O.eVA_Nm, np.array([r0[0], r0[1], 0.0]), np.array([stiff[0], stiff[1], 0.0]) / -O.eVA_Nm)
+            rs = np.zeros_like(rT)
+            fs = np.zeros_like(rT)
+            L.relaxTipStrokes_omp(nb, nb, 1, 1, Z, rT, rs, fs, None)
+        else:
+            rs, fs, _, _ = O.relax_strokes(n, cell, FFbox, prm, rT, nthreads=nthreads)
+        t_relax += time.perf_counter() - t0
+        nrel += nb * nb * Z
+        gpos = rs / ds
+        if (gpos < i_lo + 1).any() or (gpos > i_lo + ns - 2).any():
+            patch_ok = False
+        fz_cols.append(fs[:, :, ::-1, 2].reshape(-1, Z))
+    del FFbox
+    fz = np.concatenate(fz_cols)
+    t0 = time.perf_counter()
+    O.Fz2df_numpy(fz[:, None, :], w["scanStep"][2], w["kCantilever"], w["f0Cantilever"], w["Amplitude"])
+    t_df = time.perf_counter() - t0
+    full = dict(
+        ff_lj=t_lj * scale_ff,
+        ff_el=t_el * scale_ff,
+        clamp_and_sum=t_np * scale_ff,
+        relax=t_relax * (P * Z) / nrel,
+        df=t_df * P / len(fz),
+    )
+    total = sum(full.values())
+    return dict(
+        kind=kind,
+        cores=nthreads,
+        seconds_full_job=full,
+        total_s=total,
+        pixel_z_per_s=P * Z / total,
+        ff_pairs_per_s=npts * na / (full["ff_lj"] + full["ff_el"]),
+        sample=f"FF: {nzs} of {n[2]} z-planes ({plane * nzs} points x {na} atoms, LJ + Coulomb passes); relax: {len(blocks)} blocks of {nb}x{nb} pixels x {Z} heights; patch_ok={patch_ok}; extrapolated linearly per grid point / pixel-height",
+    )

@@ -1,0 +1,265 @@
+"""High-level hot-path drivers, mirroring ppafm/HighLevel.py on the GPU.
+
+* ``setFF``, ``relaxedScan3D_omp``, ``perform_relaxation``: the reference's functions with
+  the same arguments and return values (host numpy in/out), run through the device path.
+* ``computeLJ_atoms`` / ``computeELFF_pointCharge_atoms``: ``computeLJ`` /
+  ``computeELFF_pointCharge`` (HighLevel.py:260-387) from in-memory atoms instead of
+  geometry files (file I/O is outside this library).
+* ``relaxed_scan_pipeline``: the whole CPU pipeline of the reference -- LJ grid, point-charge
+  grid, clamps, FF = FFLJ + Q*FFel, relaxed scan, Fz -> Δf -- as one device-resident pass
+  with no host copy of the force field.
+"""
+
+import numpy as np
+import torch
+
+from . import common as PPU
+from . import core
+from .device import DeviceFF, iter_counter, pack_atoms, relax_params, relax_scan
+from ._lib import FF_COULOMB, FF_LJ, FF_LJC
+
+Fmax_DEFAULT = 10.0  # HighLevel.py:17
+Vmax_DEFAULT = 10.0
+TIP_KINDS = {"s": 0, "pz": 1, "dz2": 2}
+
+
+def _get(p, name, default=None):
+    if p is None:
+        return default
+    if isinstance(p, dict):
+        return p.get(name, default)
+    return getattr(p, name, default)
+
+
+# ------------------------------------------------------------ reference mirrors
+
+
+def setFF(FF=None, computeVpot=False, n=None, lvec=None, parameters=None):
+    """HighLevel.py:190-257: registers (or allocates) the host force field with the core."""
+    if FF is not None:
+        gridN = np.array(np.shape(FF)[0:3], dtype=np.int32)
+    else:
+        if n is not None:
+            gridN = np.array(n, dtype=np.int32)
+        elif parameters is not None:
+            gridN = np.array(_get(parameters, "gridN"), dtype=np.int32)
+        else:
+            raise ValueError("FF dimensions not set !!")
+        FF = np.zeros((gridN[0], gridN[1], gridN[2], 3))
+    core.setGridN(gridN)
+    if FF.ndim == 4 and FF.shape[-1] == 3:
+        core.setFF_Fpointer(FF)
+    elif FF.ndim == 3 or FF.shape[-1] == 1:
+        core.setFF_Epointer(FF)
+        computeVpot = False
+    else:
+        raise ValueError("setFF: Array dimensions wrong for both vector and array field !!")
+    V = None
+    if computeVpot:
+        V = np.zeros((gridN[0], gridN[1], gridN[2]))
+        core.setFF_Epointer(V)
+    if lvec is None and parameters is not None:
+        lvec = np.array([_get(parameters, "gridA"), _get(parameters, "gridB"), _get(parameters, "gridC")], dtype=np.float64)
+    lvec = np.array(lvec, dtype=np.float64)
+    if lvec.shape == (4, 3):
+        lvec = lvec[1:, :].copy()
+    elif lvec.shape != (3, 3):
+        raise ValueError("lvec matrix has a wrong format !!")
+    core.setGridCell(lvec)
+    return FF, V
+
+
+def relaxedScan3D_omp(xTips, yTips, zTips, trj=None, bF3d=False, tip_spline=None):
+    """HighLevel.py:104-124 through the drop-in core (FF registered with setFF)."""
+    if trj is not None:
+        raise NotImplementedError("tilted trajectories are not supported")
+    nx, ny, nz = len(xTips), len(yTips), len(zTips)
+    rTips = np.zeros((nx, ny, nz, 3))
+    rTips[:, :, :, 0] = xTips[:, None, None]
+    rTips[:, :, :, 1] = yTips[None, :, None]
+    rTips[:, :, :, 2] = zTips[::-1][None, None, :]
+    rs = np.zeros((nx, ny, nz, 3))
+    fs = np.zeros((nx, ny, nz, 3))
+    core.relaxTipStrokes_omp(rTips, rs, fs, tip_spline=tip_spline)
+    rs = rs[:, :, ::-1, :].copy()
+    fzs = fs[:, :, ::-1, :].copy() if bF3d else fs[:, :, ::-1, 2].copy()
+    return fzs, rs
+
+
+def tip_vector(parameters, relax=None):
+    """setTip/setRelax state of perform_relaxation (HighLevel.py:157-160) as the
+    parameter vector of the device relax kernels."""
+    stiff = np.array(_get(parameters, "stiffness", [-1.0, -1.0, -1.0]), dtype=np.float64)
+    if (stiff < 0.0).any():
+        stiff = np.array([_get(parameters, "klat"), _get(parameters, "klat"), _get(parameters, "krad")], dtype=np.float64)
+    r0 = _get(parameters, "r0Probe")
+    relax = relax or {}
+    return relax_params(
+        maxIters=relax.get("maxIters", _get(parameters, "maxIters", 1000)),
+        convF2=relax.get("convF2", _get(parameters, "convF2", 1e-8)),
+        dt=relax.get("dt", _get(parameters, "dt", 0.1)),
+        damping=relax.get("damping", _get(parameters, "damping", 0.1)),
+        lRadial=r0[2],
+        kRadial=stiff[2] / -PPU.eVA_Nm,
+        rPP0=(r0[0], r0[1], 0.0),
+        kSpring=np.array((stiff[0], stiff[1], 0.0)) / -PPU.eVA_Nm,
+    )
+
+
+def perform_relaxation(lvec, FFLJ, FFel=None, FFpauli=None, FFboltz=None, FFkpfm_t0sV=None, FFkpfm_tVs0=None, tip_spline=None, bPPdisp=False, bFFtotDebug=False, parameters=None, relax=None):
+    """HighLevel.py:127-184 on the GPU: FF = FFLJ + Q*FFel (+ Pauli, Boltzmann, KPFM
+    terms) composed on the host like the reference, then one device relaxed scan.
+    ``relax`` optionally overrides maxIters/convF2/dt/damping (the reference reads the
+    core's global setRelax state)."""
+    if tip_spline is not None:
+        raise NotImplementedError("tip_spline is not supported")
+    if _get(parameters, "tiltedScan", False):
+        raise NotImplementedError("tilted scans are not supported")
+    lvec = np.asarray(lvec, dtype=np.float64)
+    xTips, yTips, zTips, lvecScan = PPU.prepareScanGrids(_get(parameters, "scanMin"), _get(parameters, "scanMax"), _get(parameters, "scanStep"), _get(parameters, "r0Probe"))
+    FF = FFLJ.copy()
+    if FFel is not None:
+        FF += FFel * _get(parameters, "charge")
+    if FFkpfm_t0sV is not None and FFkpfm_tVs0 is not None:
+        FF += (_get(parameters, "charge") * FFkpfm_t0sV - FFkpfm_tVs0) * _get(parameters, "Vbias", 0.0)
+    if FFpauli is not None:
+        FF += FFpauli * _get(parameters, "Apauli")
+    if FFboltz is not None:
+        FF += FFboltz
+    ff = DeviceFF(FF.shape[:3], lvec).from_host_f64(FF.reshape(-1, 3))
+    prm = tip_vector(parameters, relax)
+    out = relax_scan(ff, prm, xTips - lvec[0, 0], yTips - lvec[0, 1], zTips[::-1] - lvec[0, 2], pos_offset=lvec[0])
+    fzs = out["fzs"].cpu().numpy().astype(np.float64)
+    PPpos = out["ppos"].cpu().numpy().astype(np.float64)
+    PPdisp = None
+    if bPPdisp:
+        r0 = _get(parameters, "r0Probe")
+        init_pos = np.array(np.meshgrid(xTips, yTips, zTips)).transpose(3, 1, 2, 0) + np.array([r0[0], r0[1], -r0[2]])
+        PPdisp = PPpos - init_pos
+    return fzs, PPpos, PPdisp, lvecScan
+
+
+# ----------------------------------------------------------------- atom input
+
+
+def prepare_atoms(Zs, Rs, Qs, lvec, parameters, FFparams=None):
+    """parseAtoms + getAtomsLJ + origin shift (common.py:828-868, HighLevel.py:269-277):
+    returns (Rs0 relative to the grid origin, cLJs, kQQs) after in-plane PBC replication."""
+    lvec = np.asarray(lvec, dtype=np.float64)
+    FFparams = PPU.loadSpecies() if FFparams is None else FFparams
+    elem_dict = PPU.getFFdict(FFparams)
+    iZs = np.asarray(Zs, dtype=np.int32)
+    Rs = np.asarray(Rs, dtype=np.float64)
+    Qs = np.asarray(Qs, dtype=np.float64)
+    if _get(parameters, "PBC", True):
+        nP = _get(parameters, "nPBC", (1, 1, 1))
+        iZs, Rs, Qs = PPU.PBCAtoms(iZs, Rs, Qs, lvec[1], lvec[2], na=nP[0], nb=nP[1])
+    iPP = PPU.atom2iZ(_get(parameters, "probeType", "O"), elem_dict)
+    cLJs = PPU.getAtomsLJ(iPP, iZs, FFparams)
+    return Rs - lvec[0], cLJs, Qs * PPU.CoulombConst
+
+
+def computeLJ_atoms(Zs, Rs, lvec, gridN, parameters, Fmax=Fmax_DEFAULT, computeVpot=False, FFparams=None, device=False):
+    """computeLJ (HighLevel.py:260-307) from in-memory atoms; returns (FF, V) float64 host
+    arrays (or the DeviceFF when device=True)."""
+    Rs0, cLJs, _ = prepare_atoms(Zs, Rs, np.zeros(len(Zs)), lvec, parameters, FFparams)
+    atoms, na, _ = pack_atoms(Rs0, cLJs, None)
+    ff = DeviceFF(gridN, lvec).compute(atoms, na, 0, FF_LJ, with_E=computeVpot)
+    if Fmax is not None:
+        ff.clamp(Fmax)
+    if device:
+        return ff
+    F, E = ff.to_host()
+    V = None
+    if computeVpot:
+        V = E
+        if Vmax_DEFAULT is not None:
+            V[V > Vmax_DEFAULT] = Vmax_DEFAULT
+    return F, V
+
+
+def computeELFF_pointCharge_atoms(Zs, Rs, Qs, lvec, gridN, parameters, tip="s", Fmax=Fmax_DEFAULT, computeVpot=False, device=False):
+    """computeELFF_pointCharge (HighLevel.py:353-387) from in-memory atoms."""
+    Rs0, _, kqq = prepare_atoms(Zs, Rs, Qs, lvec, parameters)
+    atoms, na, nch = pack_atoms(Rs0, None, kqq)
+    ff = DeviceFF(gridN, lvec).compute(atoms, na, nch, FF_COULOMB, kind=TIP_KINDS[tip], with_E=computeVpot)
+    if Fmax is not None:
+        ff.clamp(Fmax)
+    if device:
+        return ff
+    F, E = ff.to_host()
+    return F, (E if computeVpot else None)
+
+
+# ------------------------------------------------------------------- pipeline
+
+
+class Pipeline:
+    """The reference CPU pipeline (computeLJ + computeELFF_pointCharge with the default
+    clamp, perform_relaxation, Fz2df) as device-resident stages.  Build once per system,
+    then ``run()``; all buffers stay in HBM between runs."""
+
+    def __init__(self, Zs, Rs, Qs, lvec, gridN, parameters, relax=None, with_df=True, want_ppos=True, want_iters=False, FFparams=None):
+        self.p = parameters
+        self.lvec = np.asarray(lvec, dtype=np.float64)
+        self.gridN = tuple(int(x) for x in gridN)
+        self.Rs0, self.cLJs, self.kqq = prepare_atoms(Zs, Rs, Qs, self.lvec, parameters, FFparams)
+        self.natoms = len(self.Rs0)
+        self.Q = float(_get(parameters, "charge", 0.0))
+        self.tip = _get(parameters, "tip", "s")
+        self.ff = DeviceFF(self.gridN, self.lvec)
+        self.ff_el = None
+        self.prm = tip_vector(parameters, relax)
+        xT, yT, zT, self.lvecScan = PPU.prepareScanGrids(_get(parameters, "scanMin"), _get(parameters, "scanMax"), _get(parameters, "scanStep"), _get(parameters, "r0Probe"))
+        self.xs = xT - self.lvec[0, 0]
+        self.ys = yT - self.lvec[0, 1]
+        self.zs = zT[::-1] - self.lvec[0, 2]
+        self.scan_shape = (len(xT), len(yT), len(zT))
+        self.W = None
+        if with_df:
+            units = 16.0217656
+            W = PPU.get_df_weight(_get(parameters, "Amplitude", 1.0), dz=_get(parameters, "scanStep")[2])
+            self.W = W * units * _get(parameters, "f0Cantilever") / _get(parameters, "kCantilever")
+        self.want_ppos = want_ppos
+        self.want_iters = want_iters
+        self.counter = iter_counter()
+        self.out = None
+        self.upload_atoms()
+
+    def upload_atoms(self, stream=None):
+        """Host -> device copy of the atom records (the inputs of one run)."""
+        self.atoms, _, self.ncharged = pack_atoms(self.Rs0, self.cLJs, self.kqq if self.Q != 0.0 else None)
+        if self.tip != "s" and self.Q != 0.0:
+            self.atoms_el, _, self.nch_el = pack_atoms(self.Rs0, None, self.kqq)
+
+    def build_ff(self, stream=None):
+        if self.Q == 0.0:
+            self.ff.compute(self.atoms, self.natoms, 0, FF_LJ, stream=stream).clamp(Fmax_DEFAULT, stream=stream)
+        elif self.tip == "s":
+            self.ff.compute(self.atoms, self.natoms, self.ncharged, FF_LJC, Q=self.Q, Fmax=Fmax_DEFAULT, stream=stream)
+        else:
+            self.ff.compute(self.atoms, self.natoms, 0, FF_LJ, stream=stream).clamp(Fmax_DEFAULT, stream=stream)
+            if self.ff_el is None:
+                self.ff_el = DeviceFF(self.gridN, self.lvec)
+            self.ff_el.compute(self.atoms_el, self.natoms, self.nch_el, FF_COULOMB, kind=TIP_KINDS[self.tip], stream=stream).clamp(Fmax_DEFAULT, stream=stream)
+            self.ff.axpby(1.0, self.ff_el, self.Q, stream=stream)
+        return self.ff
+
+    def relax(self, stream=None):
+        self.out = relax_scan(self.ff, self.prm, self.xs, self.ys, self.zs, pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
+        return self.out
+
+    def run(self, stream=None):
+        self.build_ff(stream)
+        return self.relax(stream)
+
+    def iterations(self):
+        return int(self.counter.item())
+
+
+def relaxed_scan_pipeline(Zs, Rs, Qs, lvec, gridN, parameters, relax=None, with_df=True):
+    """One call: host atoms in, host (fzs, PPpos, df, lvecScan) out (float64)."""
+    pl = Pipeline(Zs, Rs, Qs, lvec, gridN, parameters, relax=relax, with_df=with_df)
+    out = pl.run()
+    res = {k: v.cpu().numpy().astype(np.float64) for k, v in out.items()}
+    return res.get("fzs"), res.get("ppos"), res.get("df"), pl.lvecScan

@@ -1,0 +1,169 @@
+"""Host-side helpers of the hot path, mirroring ppafm/common.py.
+
+Pure host arithmetic (Δf kernels, periodic images, LJ mixing, scan grids) lives here as
+numpy; the per-column Fz -> Δf convolution runs on the GPU (``Fz2df``).
+"""
+
+import numpy as np
+
+from . import species as _species
+from ._lib import check, dptr, lib, stream_handle, tptr
+
+# ppafm/common.py:20-21
+eVA_Nm = 16.0217662
+CoulombConst = 14.399645
+
+loadSpecies = _species.loadSpecies
+getFFdict = _species.getFFdict
+atom2iZ = _species.atom2iZ
+atoms2iZs = _species.atoms2iZs
+
+
+# ------------------------------------------------------------------ Δf weights
+
+
+def get_df_weight(Amp, dz=0.1):
+    """Discretised Giessibl convolution kernel for peak-to-peak amplitude Amp and step dz
+    (common.py:333-392): linear interpolation of F between samples, integrated against
+    t/sqrt(1-t^2); returned already reversed for np.convolve."""
+    n = int(np.ceil(Amp / dz))
+    t = np.linspace(-1 + 2 * n * dz / Amp, -1, n + 1)
+    f = np.zeros(n + 1)
+    f2 = np.zeros(n + 1)
+    if n > 1:
+        ti = t[1:-1]
+        f[1:-1] = np.sqrt(1 - ti * ti)
+        f2[1:-1] = (np.arccos(-ti) - ti * f[1:-1]) / 2.0
+    f2[0] = np.pi / 2  # t >= 1 behaves like t = 1
+    df = f[:-1] - f[1:]
+    df2 = f2[:-1] - f2[1:]
+    w = np.zeros(n + 1)
+    w[1:] = t[:-1] * df + df2
+    w[:-1] -= t[1:] * df + df2
+    return w / (np.pi * dz)
+
+
+def get_simple_df_weight(n=10, dz=0.1):
+    """The simpler kernel the AFMulator uses (common.py:395-418)."""
+    n = max(int(n), 2)
+    t = np.linspace(-1 + 0.5 / n, 1 - 0.5 / n, n - 1)
+    f = np.sqrt(1 - t * t)
+    w = np.zeros(n)
+    w[:-1] = f
+    w[1:] -= f
+    w0 = np.sum(np.linspace(-1, 1, n) * w)
+    return w / (w0 * n * dz)
+
+
+def Fz2df(F, dz, k0, f0, amplitude=1.0, units=16.0217656, out=None, stream=None):
+    """Frequency shift from Fz along the last axis (common.py:421-430) on the GPU.
+
+    F: numpy array (any float dtype; the result is float64 like the reference) or a CUDA
+    float32 torch tensor (result stays on the device).  Same 'valid'-mode convolution with
+    get_df_weight(amplitude, dz), scaled by units*f0/k0."""
+    import torch
+
+    W = get_df_weight(amplitude, dz=dz)
+    scale = units * f0 / k0
+    host = not (isinstance(F, torch.Tensor) and F.is_cuda)
+    Ft = torch.as_tensor(np.ascontiguousarray(F, dtype=np.float32)).cuda() if host else F.contiguous().float()
+    nz = Ft.shape[-1]
+    nw = len(W)
+    if nw > nz:
+        raise ValueError(f"amplitude/dz needs {nw} z samples, F has {nz}")
+    nout = nz - nw + 1
+    ncol = Ft.numel() // nz
+    o = torch.empty(Ft.shape[:-1] + (nout,), dtype=torch.float32, device=Ft.device)
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    check(lib().ppgpu_fz2df(tptr(Ft), ncol, nz, nw, dptr(W), scale, tptr(o), stream_handle(stream)))
+    if host:
+        res = o.cpu().numpy().astype(np.float64)
+        if out is not None:
+            out[...] = res
+            return out
+        return res
+    return o
+
+
+# ------------------------------------------------------------- atoms and LJ
+
+
+def PBCAtoms(Zs, Rs, Qs, avec, bvec, na=1, nb=1):
+    """In-plane periodic images (common.py:608-628): images ordered i (along a) outer,
+    j (along b) inner, atoms innermost; z unchanged."""
+    Rs = np.asarray(Rs, dtype=np.float64)
+    shifts = [(i, j) for i in range(-na, na + 1) for j in range(-nb, nb + 1)]
+    Rs_ = np.concatenate([np.column_stack([Rs[:, 0] + i * avec[0] + j * bvec[0], Rs[:, 1] + i * avec[1] + j * bvec[1], Rs[:, 2]]) for i, j in shifts])
+    return np.tile(np.asarray(Zs), len(shifts)), Rs_, np.tile(np.asarray(Qs, dtype=np.float64), len(shifts))
+
+
+def PBCAtoms3D_np(Zs, Rs, Qs, cLJs, REAs, lvec, npbc=(1, 1, 1)):
+    """3-D periodic images with the home cell first, float32 (common.py:728-776)."""
+    lvec = np.asarray(lvec, dtype=np.float64)
+    shifts = [(0, 0, 0)] + [(a, b, c) for a in range(-npbc[0], npbc[0] + 1) for b in range(-npbc[1], npbc[1] + 1) for c in range(-npbc[2], npbc[2] + 1) if (a, b, c) != (0, 0, 0)]
+    Rs = np.asarray(Rs)
+    xyz = np.concatenate([Rs + (a * lvec[0] + b * lvec[1] + c * lvec[2])[None, :] for a, b, c in shifts]).astype(np.float32)
+    m = len(shifts)
+    Zs_ = np.tile(np.asarray(Zs, dtype=np.int32), m)
+    qs_ = np.tile(np.asarray(Qs), m).astype(np.float32)
+    cLJs_ = None if cLJs is None else np.tile(np.asarray(cLJs), (m, 1)).astype(np.float32)
+    REAs_ = None if REAs is None else np.tile(np.asarray(REAs), (m, 1)).astype(np.float32)
+    return Zs_, xyz, qs_, cLJs_, REAs_
+
+
+def get_C612(i, j, FFparams):
+    """c6 = 2 eps R^6, c12 = eps R^12 with R = r_i + r_j, eps = sqrt(e_i e_j) (common.py:851-857)."""
+    Rij = FFparams[i][0] + FFparams[j][0]
+    Eij = np.sqrt(FFparams[i][1] * FFparams[j][1])
+    return 2 * Eij * (Rij**6), Eij * (Rij**12)
+
+
+def getAtomsLJ(iZprobe, iZs, FFparams):
+    """(c6, c12) of every atom against the probe (common.py:860-868)."""
+    cLJs = np.zeros((len(iZs), 2))
+    for i, z in enumerate(iZs):
+        cLJs[i] = get_C612(iZprobe - 1, z - 1, FFparams)
+    return cLJs
+
+
+def getAtomsREA(iZprobe, iZs, FFparams, alphaFac=-1.0):
+    """(R, E, alpha) pair parameters (common.py:880-892)."""
+    REAs = np.zeros((len(iZs), 4))
+    i = iZprobe - 1
+    for ii, z in enumerate(iZs):
+        j = z - 1
+        REAs[ii, 0] = FFparams[i][0] + FFparams[j][0]
+        REAs[ii, 1] = np.sqrt(FFparams[i][1] * FFparams[j][1])
+        REAs[ii, 2] = FFparams[j][2] * alphaFac
+    return REAs
+
+
+def REA2LJ(cREAs, cLJs=None):
+    """common.py:871-877."""
+    if cLJs is None:
+        cLJs = np.zeros((len(cREAs), 2))
+    R6 = cREAs[:, 0] ** 6
+    cLJs[:, 0] = 2 * cREAs[:, 1] * R6
+    cLJs[:, 1] = cREAs[:, 1] * (R6**2)
+    return cLJs
+
+
+def prepareScanGrids(scanMin, scanMax, scanStep, r0Probe):
+    """Tip positions and the scan-output lattice (common.py:922-946)."""
+    xTips = np.arange(scanMin[0], scanMax[0] + 0.5 * scanStep[0], scanStep[0])
+    yTips = np.arange(scanMin[1], scanMax[1] + 0.5 * scanStep[1], scanStep[1])
+    zTips = np.arange(scanMin[2], scanMax[2] + 0.5 * scanStep[2], scanStep[2])
+    lvecScan = np.array(
+        [
+            [scanMin[0] + r0Probe[0], scanMin[1] + r0Probe[1], scanMin[2] - r0Probe[2]],
+            [scanMax[0] - scanMin[0], 0.0, 0.0],
+            [0.0, scanMax[1] - scanMin[1], 0.0],
+            [0.0, 0.0, scanMax[2] - scanMin[2]],
+        ]
+    )
+    return xTips, yTips, zTips, lvecScan
+
+
+def genFFSampling(lvec, pixPerAngstrome=10):
+    """Grid size for a lattice at a given density (common.py:967-977)."""
+    return np.array([int(round(pixPerAngstrome * np.sqrt(np.dot(lvec[k], lvec[k])))) for k in (1, 2, 3)], np.int32)

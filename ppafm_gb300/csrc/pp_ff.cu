@@ -1,0 +1,756 @@
+// pp_ff.cu -- force-field grid generation on sm_103a.
+//
+// Computes, for every grid point p, sums over atoms of the Lennard-Jones and
+// point-charge Coulomb interactions of the reference core:
+//   addAtomLJ      (ppafm/cpp/Forces.h:120-132)
+//   addAtomCoulomb (Forces.h:237-244) and the pz / dz2 finite-difference tips
+//                  (ppafm/cpp/ProbeParticle.cpp:192-209)
+//   evalLJC_QZs_noPos (ppafm/ocl/cl/FF.cl:366-423) for the AFMulator grid
+// on the grid of GridShape (ppafm/cpp/Grid.h:29-36, 142-170).
+//
+// Design (GB300):
+//  * Atom records (48 B: hi/lo split coordinates, charge, LJ coefficients) are streamed
+//    through shared memory in tiles of FF_TILE atoms by 1-D TMA bulk copies
+//    (cp.async.bulk + mbarrier, two stages), so the tile for step t+1 lands while
+//    step t is computed.
+//  * Each thread owns P consecutive points of one grid column (x,y fixed, z varying),
+//    so the in-plane displacement and its square are computed once per atom and
+//    shared by the P points.
+//  * dR = p - R is formed from float hi/lo pairs of the float64 coordinates, which
+//    keeps the displacement accurate to float rounding of |dR| itself instead of the
+//    rounding of |p| (that matters for the r^-13 repulsive wall).
+//  * Partial sums per atom tile are folded into running totals (two-level summation)
+//    to bound the FP32 accumulation error over thousands of atoms.
+//  * Points whose float32 result overflows (a grid point within ~5e-3 A of an atom
+//    centre) are recomputed by a slow path that floors r^2 at 1e-4 A^2.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "pp_common.cuh"
+
+namespace ppgpu {
+
+constexpr int FF_THREADS = 256;
+constexpr int FF_TILE = 256;       // atoms per shared-memory stage
+constexpr int FF_REC = 3;          // float4 per atom record
+constexpr float R2CAP = 1e-4f;     // slow-path floor of r^2 (A^2)
+
+enum { M_LJ = 0, M_COUL = 1, M_LJC = 2, M_QZS = 3 };
+
+struct FFParams {
+    float4 *FE;
+    const float4 *atoms;
+    int natoms, ncharged;
+    int i0[3], ns[3];
+    double dA[3], dB[3], dC[3];
+    float eps;
+    double eps64;
+    float Q, Fmax;
+    float Qs[4], QZs[4];
+    int nq;
+    int accumulate;
+    long long nchunks;
+    int nzc;
+    int *err;
+};
+
+// ------------------------------------------------------------------ TMA helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait (about 2 s of wall time) on an mbarrier phase.
+__device__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 0; i < (1u << 26); i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 255u) == 255u && global_ns() - t0 > 2000000000ull) break;
+    }
+    return false;
+}
+
+// ------------------------------------------------------------- pair interactions
+
+// Lennard-Jones term (Forces.h:120-132) given r^2 (eps included) and dR.
+template <bool WITH_E>
+__device__ __forceinline__ void lj_term(float r2, float dx, float dy, float dz, const float4 &C, float &fx,
+                                        float &fy, float &fz, float &e) {
+    const float ir2 = rcp_approx(r2);
+    const float ir6 = ir2 * ir2 * ir2;
+    const float b = fmaf(C.w, ir6, -C.z);  // 12 c12 ir6 - 6 c6
+    const float fr = b * (ir6 * ir2);
+    fx = fmaf(fr, dx, fx);
+    fy = fmaf(fr, dy, fy);
+    fz = fmaf(fr, dz, fz);
+    if (WITH_E) e = fmaf(fmaf(C.y, ir6, -C.x), ir6, e);
+}
+
+// Coulomb term (Forces.h:237-244): kqq/r and kqq dR/r^3.
+template <bool WITH_E>
+__device__ __forceinline__ void coul_term(float r2, float dx, float dy, float dz, float kqq, float &fx, float &fy,
+                                          float &fz, float &e) {
+    const float ir = rsqrt_approx(r2);
+    const float eq = kqq * ir;
+    const float fq = eq * (ir * ir);
+    fx = fmaf(fq, dx, fx);
+    fy = fmaf(fq, dy, fy);
+    fz = fmaf(fq, dz, fz);
+    if (WITH_E) e += eq;
+}
+
+// Number of accumulators per point for each mode.
+template <int MODE>
+struct NAcc {
+    static constexpr int v = (MODE == M_LJC) ? 8 : 4;
+};
+
+// One atom against one point.  acc: [0..2] F (LJ or total), [3] E, [4..6] F_el, [7] E_el.
+template <int MODE, int KIND, bool WITH_E, bool CHARGED, bool CAP>
+__device__ __forceinline__ void atom_point(float dx, float dy, float dz, float dxy2, const float4 &A,
+                                           const float4 &C, const FFParams &prm, float *acc) {
+    (void)prm;
+    if (MODE == M_LJ) {
+        float r2 = fmaf(dz, dz, dxy2);
+        if (CAP) r2 = fmaxf(r2, R2CAP);
+        lj_term<WITH_E>(r2, dx, dy, dz, C, acc[0], acc[1], acc[2], acc[3]);
+    } else if (MODE == M_COUL) {
+        if (KIND == 0) {
+            float r2 = fmaf(dz, dz, dxy2);
+            if (CAP) r2 = fmaxf(r2, R2CAP);
+            coul_term<WITH_E>(r2, dx, dy, dz, A.w, acc[0], acc[1], acc[2], acc[3]);
+        } else if (KIND == 1) {  // pz: C(dz-0.1, -kqq) + C(dz+0.1, +kqq)  (x10 at the end)
+            float dm = dz - 0.1f, dp = dz + 0.1f;
+            float r2m = fmaf(dm, dm, dxy2), r2p = fmaf(dp, dp, dxy2);
+            if (CAP) {
+                r2m = fmaxf(r2m, R2CAP);
+                r2p = fmaxf(r2p, R2CAP);
+            }
+            coul_term<WITH_E>(r2m, dx, dy, dm, -A.w, acc[0], acc[1], acc[2], acc[3]);
+            coul_term<WITH_E>(r2p, dx, dy, dp, A.w, acc[0], acc[1], acc[2], acc[3]);
+        } else {  // dz2: C(dz,-2kqq) + C(dz-0.1,kqq) + C(dz+0.1,kqq)  (x100 at the end)
+            float dm = dz - 0.1f, dp = dz + 0.1f;
+            float r20 = fmaf(dz, dz, dxy2), r2m = fmaf(dm, dm, dxy2), r2p = fmaf(dp, dp, dxy2);
+            if (CAP) {
+                r20 = fmaxf(r20, R2CAP);
+                r2m = fmaxf(r2m, R2CAP);
+                r2p = fmaxf(r2p, R2CAP);
+            }
+            coul_term<WITH_E>(r20, dx, dy, dz, -2.f * A.w, acc[0], acc[1], acc[2], acc[3]);
+            coul_term<WITH_E>(r2m, dx, dy, dm, A.w, acc[0], acc[1], acc[2], acc[3]);
+            coul_term<WITH_E>(r2p, dx, dy, dp, A.w, acc[0], acc[1], acc[2], acc[3]);
+        }
+    } else if (MODE == M_LJC) {
+        float r2 = fmaf(dz, dz, dxy2);
+        if (CAP) r2 = fmaxf(r2, R2CAP);
+        if (CHARGED) {
+            const float ir = rsqrt_approx(r2);
+            const float ir2 = ir * ir;
+            const float ir6 = ir2 * ir2 * ir2;
+            const float b = fmaf(C.w, ir6, -C.z);
+            const float fr = b * (ir6 * ir2);
+            acc[0] = fmaf(fr, dx, acc[0]);
+            acc[1] = fmaf(fr, dy, acc[1]);
+            acc[2] = fmaf(fr, dz, acc[2]);
+            if (WITH_E) acc[3] = fmaf(fmaf(C.y, ir6, -C.x), ir6, acc[3]);
+            const float eq = A.w * ir;
+            const float fq = eq * ir2;
+            acc[4] = fmaf(fq, dx, acc[4]);
+            acc[5] = fmaf(fq, dy, acc[5]);
+            acc[6] = fmaf(fq, dz, acc[6]);
+            if (WITH_E) acc[7] += eq;
+        } else {
+            lj_term<WITH_E>(r2, dx, dy, dz, C, acc[0], acc[1], acc[2], acc[3]);
+        }
+    } else {  // M_QZS: LJ + sum_q Qs[q] * Coulomb(dz + QZs[q])
+        float r2 = fmaf(dz, dz, dxy2);
+        if (CAP) r2 = fmaxf(r2, R2CAP);
+        lj_term<WITH_E>(r2, dx, dy, dz, C, acc[0], acc[1], acc[2], acc[3]);
+        if (CHARGED) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (q < prm.nq) {
+                    const float dq = dz + prm.QZs[q];
+                    float rq = fmaf(dq, dq, dxy2);
+                    if (CAP) rq = fmaxf(rq, R2CAP);
+                    const float ir = rsqrt_approx(rq);
+                    const float eq = A.w * ir * prm.Qs[q];
+                    const float fq = eq * (ir * ir);
+                    acc[0] = fmaf(fq, dx, acc[0]);
+                    acc[1] = fmaf(fq, dy, acc[1]);
+                    acc[2] = fmaf(fq, dq, acc[2]);
+                    if (WITH_E) acc[3] += eq;
+                }
+            }
+        }
+    }
+}
+
+// Overflow-safe |F| <= Fmax clamp preserving direction (io.py:766-778).
+__device__ __forceinline__ void clamp_vec(float &x, float &y, float &z, float Fmax) {
+    const float m = fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z)));
+    if (!(m > 0.f)) return;
+    const float s = 1.f / m;
+    const float sx = x * s, sy = y * s, sz = z * s;
+    const float fr = m * sqrtf(sx * sx + sy * sy + sz * sz);
+    if (fr > Fmax) {
+        const float k = Fmax / fr;
+        x *= k;
+        y *= k;
+        z *= k;
+    }
+}
+
+// Combines the accumulators of one point into (Fx,Fy,Fz,E).
+template <int MODE, int KIND, bool WITH_E>
+__device__ __forceinline__ float4 finalize(const float *t, const FFParams &prm) {
+    float4 o;
+    if (MODE == M_LJC) {
+        float ax = t[0], ay = t[1], az = t[2], bx = t[4], by = t[5], bz = t[6];
+        if (prm.Fmax > 0.f) {
+            clamp_vec(ax, ay, az, prm.Fmax);
+            clamp_vec(bx, by, bz, prm.Fmax);
+        }
+        o.x = fmaf(prm.Q, bx, ax);
+        o.y = fmaf(prm.Q, by, ay);
+        o.z = fmaf(prm.Q, bz, az);
+        o.w = WITH_E ? fmaf(prm.Q, t[7], t[3]) : 0.f;
+    } else {
+        const float s = (MODE == M_COUL && KIND == 1) ? 10.f : ((MODE == M_COUL && KIND == 2) ? 100.f : 1.f);
+        o.x = t[0] * s;
+        o.y = t[1] * s;
+        o.z = t[2] * s;
+        o.w = WITH_E ? t[3] * s : 0.f;
+    }
+    return o;
+}
+
+__device__ __forceinline__ bool finite4(const float4 &v) {
+    return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w);
+}
+
+// Slow path for one point: all atoms from global memory, r^2 floored at R2CAP.
+template <int MODE, int KIND, bool WITH_E>
+__device__ float4 point_slow(const FFParams &prm, const float3 ph, const float3 pl) {
+    constexpr int NA = NAcc<MODE>::v;
+    float acc[NA];
+#pragma unroll
+    for (int c = 0; c < NA; c++) acc[c] = 0.f;
+    const int nat = (MODE == M_COUL) ? prm.ncharged : prm.natoms;
+    for (int j = 0; j < nat; j++) {
+        const float4 A = prm.atoms[3 * j], B = prm.atoms[3 * j + 1], C = prm.atoms[3 * j + 2];
+        const float dx = (ph.x - A.x) + (pl.x - B.x);
+        const float dy = (ph.y - A.y) + (pl.y - B.y);
+        const float dz = (ph.z - A.z) + (pl.z - B.z);
+        const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
+        if (j < prm.ncharged)
+            atom_point<MODE, KIND, WITH_E, true, true>(dx, dy, dz, dxy2, A, C, prm, acc);
+        else
+            atom_point<MODE, KIND, WITH_E, false, true>(dx, dy, dz, dxy2, A, C, prm, acc);
+    }
+    return finalize<MODE, KIND, WITH_E>(acc, prm);
+}
+
+template <int MODE, int KIND, bool WITH_E, bool ORTHO, int P>
+__global__ void __launch_bounds__(FF_THREADS) ff_kernel(const FFParams prm) {
+    constexpr int NA = NAcc<MODE>::v;
+    __shared__ __align__(128) float4 s_at[2][FF_TILE * FF_REC];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x;
+    const long long chunk = (long long)blockIdx.x * FF_THREADS + tid;
+    const bool valid = chunk < prm.nchunks;
+
+    // ---- this thread's points: column (ga, gb), z points gc0 .. gc0+P-1
+    int la = 0, lb = 0, lz0 = 0;
+    if (valid) {
+        const long long col = chunk / prm.nzc;
+        lz0 = (int)(chunk - col * prm.nzc) * P;
+        la = (int)(col / prm.ns[1]);
+        lb = (int)(col - (long long)la * prm.ns[1]);
+    }
+    const double ga = prm.i0[0] + la, gb = prm.i0[1] + lb, gc = prm.i0[2] + lz0;
+    double p[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) p[k] = ((prm.dA[k] * ga) + prm.dB[k] * gb) + prm.dC[k] * gc;
+    float3 ph, pl;
+    ph.x = __double2float_rn(p[0]);
+    ph.y = __double2float_rn(p[1]);
+    ph.z = __double2float_rn(p[2]);
+    pl.x = __double2float_rn(p[0] - (double)ph.x);
+    pl.y = __double2float_rn(p[1] - (double)ph.y);
+    pl.z = __double2float_rn(p[2] - (double)ph.z);
+    float off[3][P];
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+        off[0][k] = __double2float_rn(prm.dC[0] * k);
+        off[1][k] = __double2float_rn(prm.dC[1] * k);
+        off[2][k] = __double2float_rn(prm.dC[2] * k);
+    }
+
+    float acc[P][NA], tot[P][NA];
+#pragma unroll
+    for (int k = 0; k < P; k++)
+#pragma unroll
+        for (int c = 0; c < NA; c++) {
+            acc[k][c] = 0.f;
+            tot[k][c] = 0.f;
+        }
+
+    const int nat = (MODE == M_COUL) ? prm.ncharged : prm.natoms;
+    const int ntiles = (nat + FF_TILE - 1) / FF_TILE;
+
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        s_abort = 0;
+        for (int t = 0; t < 2 && t < ntiles; t++) {
+            const int nj = min(FF_TILE, nat - t * FF_TILE);
+            const uint32_t bytes = (uint32_t)nj * FF_REC * 16u;
+            mbar_expect_tx(&s_bar[t], bytes);
+            bulk_g2s(&s_at[t][0], prm.atoms + (size_t)t * FF_TILE * FF_REC, bytes, &s_bar[t]);
+        }
+    }
+    __syncthreads();
+
+    for (int t = 0; t < ntiles; t++) {
+        const int s = t & 1;
+        if (tid == 0) {
+            if (!mbar_wait_bounded(&s_bar[s], (uint32_t)((t >> 1) & 1))) s_abort = 1;
+        }
+        __syncthreads();
+        if (s_abort) {
+            // Drain: give any copy still in flight a bounded chance to land before exit.
+            if (tid == 0) {
+                raise_device_error(prm.err, PPGPU_ERR_DEVICE_TIMEOUT);
+                for (int u = t; u < t + 2 && u < ntiles; u++) mbar_wait_bounded(&s_bar[u & 1], (uint32_t)((u >> 1) & 1));
+            }
+            return;
+        }
+        const int base = t * FF_TILE;
+        const int nj = min(FF_TILE, nat - base);
+        const int jc = max(0, min(nj, prm.ncharged - base));  // charged atoms of this tile
+        const float4 *S = &s_at[s][0];
+
+        auto run_atoms = [&](int j0, int j1, auto charged_tag) {
+            constexpr bool CH = decltype(charged_tag)::value;
+            for (int j = j0; j < j1; j++) {
+                const float4 A = S[3 * j], B = S[3 * j + 1], C = S[3 * j + 2];
+                if (ORTHO) {
+                    const float dx = (ph.x - A.x) + (pl.x - B.x);
+                    const float dy = (ph.y - A.y) + (pl.y - B.y);
+                    const float dz0 = (ph.z - A.z) + (pl.z - B.z);
+                    const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
+#pragma unroll
+                    for (int k = 0; k < P; k++)
+                        atom_point<MODE, KIND, WITH_E, CH, false>(dx, dy, dz0 + off[2][k], dxy2, A, C, prm, acc[k]);
+                } else {
+                    const float dx0 = (ph.x - A.x) + (pl.x - B.x);
+                    const float dy0 = (ph.y - A.y) + (pl.y - B.y);
+                    const float dz0 = (ph.z - A.z) + (pl.z - B.z);
+#pragma unroll
+                    for (int k = 0; k < P; k++) {
+                        const float dx = dx0 + off[0][k], dy = dy0 + off[1][k];
+                        const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
+                        atom_point<MODE, KIND, WITH_E, CH, false>(dx, dy, dz0 + off[2][k], dxy2, A, C, prm, acc[k]);
+                    }
+                }
+            }
+        };
+        if (MODE == M_LJ) {
+            run_atoms(0, nj, std::false_type{});
+        } else if (MODE == M_COUL) {
+            run_atoms(0, nj, std::true_type{});
+        } else {
+            run_atoms(0, jc, std::true_type{});
+            run_atoms(jc, nj, std::false_type{});
+        }
+#pragma unroll
+        for (int k = 0; k < P; k++)
+#pragma unroll
+            for (int c = 0; c < NA; c++) {
+                tot[k][c] += acc[k][c];
+                acc[k][c] = 0.f;
+            }
+        __syncthreads();  // every thread is done with stage s
+        if (tid == 0 && t + 2 < ntiles) {
+            const int nj2 = min(FF_TILE, nat - (t + 2) * FF_TILE);
+            const uint32_t bytes = (uint32_t)nj2 * FF_REC * 16u;
+            mbar_expect_tx(&s_bar[s], bytes);
+            bulk_g2s(&s_at[s][0], prm.atoms + (size_t)(t + 2) * FF_TILE * FF_REC, bytes, &s_bar[s]);
+        }
+    }
+
+    if (!valid) return;
+    const long long colbase = ((long long)la * prm.ns[1] + lb) * prm.ns[2];
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+        const int lz = lz0 + k;
+        if (lz >= prm.ns[2]) break;
+        float4 o = finalize<MODE, KIND, WITH_E>(tot[k], prm);
+        if (!finite4(o)) {
+            float3 pk_h, pk_l;
+            double q[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) q[c] = ((prm.dA[c] * ga) + prm.dB[c] * gb) + prm.dC[c] * (gc + k);
+            pk_h = make_float3(__double2float_rn(q[0]), __double2float_rn(q[1]), __double2float_rn(q[2]));
+            pk_l = make_float3(__double2float_rn(q[0] - (double)pk_h.x), __double2float_rn(q[1] - (double)pk_h.y),
+                               __double2float_rn(q[2] - (double)pk_h.z));
+            o = point_slow<MODE, KIND, WITH_E>(prm, pk_h, pk_l);
+        }
+        float4 *dst = prm.FE + colbase + lz;
+        if (prm.accumulate) {
+            const float4 old = *dst;
+            o.x += old.x;
+            o.y += old.y;
+            o.z += old.z;
+            o.w += old.w;
+        }
+        *dst = o;
+    }
+}
+
+// ------------------------------------------------------------- float64 kernel
+//
+// The same sums in float64, one grid point per thread, following the reference's
+// arithmetic (Forces.h:120-132, 237-244; ProbeParticle.cpp:192-209).  Used for the pz and
+// dz2 tips, whose finite differences (step 0.1 A) cancel ~r^2/h^2 of the float32
+// significand, and as the GPU float64 error oracle of the float32 kernels
+// (PPGPU_FF_F64).  Atom coordinates are hi + lo (exact to ~1e-13 A); coefficients are
+// the float32 values of the records.
+
+__device__ __forceinline__ double coul64(double dx, double dy, double dz, double kqq, double &fx, double &fy,
+                                         double &fz) {
+    const double ir2 = 1.0 / (((dx * dx + dy * dy) + dz * dz) + 1.0e-8);
+    const double ir = sqrt(ir2);
+    const double e = ir * kqq;
+    const double fr = e * ir2;
+    fx += dx * fr;
+    fy += dy * fr;
+    fz += dz * fr;
+    return e;
+}
+
+template <int MODE, int KIND>
+__global__ void __launch_bounds__(FF_THREADS) ff_f64_kernel(const FFParams prm) {
+    __shared__ __align__(16) float4 s_at[FF_TILE * FF_REC];
+    const int tid = threadIdx.x;
+    const long long pidx = (long long)blockIdx.x * FF_THREADS + tid;
+    const long long ntot = (long long)prm.ns[0] * prm.ns[1] * prm.ns[2];
+    const bool valid = pidx < ntot;
+    const long long q = valid ? pidx : 0;
+    const int lz = (int)(q % prm.ns[2]);
+    const int lb = (int)((q / prm.ns[2]) % prm.ns[1]);
+    const int la = (int)(q / ((long long)prm.ns[1] * prm.ns[2]));
+    const double ga = prm.i0[0] + la, gb = prm.i0[1] + lb, gc = prm.i0[2] + lz;
+    double p[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) p[k] = ((prm.dA[k] * ga) + prm.dB[k] * gb) + prm.dC[k] * gc;
+    double F[3] = {0, 0, 0}, E = 0, G[3] = {0, 0, 0}, Ge = 0;
+    const int nat = (MODE == M_COUL) ? prm.ncharged : prm.natoms;
+    for (int base = 0; base < nat; base += FF_TILE) {
+        const int nj = min(FF_TILE, nat - base);
+        __syncthreads();
+        for (int i = tid; i < nj * FF_REC; i += FF_THREADS) s_at[i] = prm.atoms[(size_t)base * FF_REC + i];
+        __syncthreads();
+        for (int j = 0; j < nj; j++) {
+            const float4 A = s_at[3 * j], B = s_at[3 * j + 1], C = s_at[3 * j + 2];
+            const double dx = p[0] - ((double)A.x + (double)B.x);
+            const double dy = p[1] - ((double)A.y + (double)B.y);
+            double dz = p[2] - ((double)A.z + (double)B.z);
+            const bool charged = (base + j) < prm.ncharged;
+            if (MODE == M_LJ || MODE == M_LJC || MODE == M_QZS) {
+                const double ir2 = 1.0 / (((dx * dx + dy * dy) + dz * dz) + prm.eps64);
+                const double ir6 = ir2 * ir2 * ir2;
+                const double e6 = (double)C.x * ir6;
+                const double e12 = (double)C.y * ir6 * ir6;
+                const double fr = (12 * e12 - 6 * e6) * ir2;
+                F[0] += dx * fr;
+                F[1] += dy * fr;
+                F[2] += dz * fr;
+                E += e12 - e6;
+            }
+            if (MODE == M_LJC && charged) Ge += coul64(dx, dy, dz, (double)A.w, G[0], G[1], G[2]);
+            if (MODE == M_QZS && charged) {
+                for (int k = 0; k < prm.nq; k++) {
+                    const double dq = dz + (double)prm.QZs[k];
+                    const double ir2 = 1.0 / (((dx * dx + dy * dy) + dq * dq) + prm.eps64);
+                    const double eq = (double)A.w * sqrt(ir2) * (double)prm.Qs[k];
+                    const double fq = eq * ir2;
+                    F[0] += dx * fq;
+                    F[1] += dy * fq;
+                    F[2] += dq * fq;
+                    E += eq;
+                }
+            }
+            if (MODE == M_COUL) {
+                const double kqq = (double)A.w;
+                if (KIND == 0) {
+                    E += coul64(dx, dy, dz, kqq, F[0], F[1], F[2]);
+                } else if (KIND == 1) {
+                    double g0 = 0, g1 = 0, g2 = 0, e = 0;
+                    dz -= 0.1;
+                    e += coul64(dx, dy, dz, -kqq, g0, g1, g2);
+                    dz += 2 * 0.1;
+                    e += coul64(dx, dy, dz, kqq, g0, g1, g2);
+                    F[0] += g0 * 10.0;
+                    F[1] += g1 * 10.0;
+                    F[2] += g2 * 10.0;
+                    E += e * 10.0;
+                } else {
+                    double g0 = 0, g1 = 0, g2 = 0, e = 0;
+                    e += coul64(dx, dy, dz, -2 * kqq, g0, g1, g2);
+                    dz -= 0.1;
+                    e += coul64(dx, dy, dz, kqq, g0, g1, g2);
+                    dz += 2 * 0.1;
+                    e += coul64(dx, dy, dz, kqq, g0, g1, g2);
+                    F[0] += g0 * 100.0;
+                    F[1] += g1 * 100.0;
+                    F[2] += g2 * 100.0;
+                    E += e * 100.0;
+                }
+            }
+        }
+    }
+    if (!valid) return;
+    if (MODE == M_LJC) {
+        auto clamp64 = [&](double *v) {
+            const double fr = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            if (prm.Fmax > 0.f && fr > (double)prm.Fmax) {
+                const double k = (double)prm.Fmax / fr;
+                v[0] *= k;
+                v[1] *= k;
+                v[2] *= k;
+            }
+        };
+        clamp64(F);
+        clamp64(G);
+        for (int k = 0; k < 3; k++) F[k] += (double)prm.Q * G[k];
+        E += (double)prm.Q * Ge;
+    }
+    float4 o = make_float4((float)F[0], (float)F[1], (float)F[2], (float)E);
+    float4 *dst = prm.FE + q;
+    if (prm.accumulate) {
+        const float4 old = *dst;
+        o.x += old.x;
+        o.y += old.y;
+        o.z += old.z;
+        o.w += old.w;
+    }
+    *dst = o;
+}
+
+template <int MODE, int KIND>
+static int launch_ff64(const FFParams &prm, cudaStream_t st) {
+    const long long ntot = (long long)prm.ns[0] * prm.ns[1] * prm.ns[2];
+    const long long nblk = (ntot + FF_THREADS - 1) / FF_THREADS;
+    if (nblk <= 0) return set_ok();
+    if (nblk > 0x7fffffffLL) return set_error(PPGPU_ERR_ARG, "ff grid too large (%lld blocks)", nblk);
+    ff_f64_kernel<MODE, KIND><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+    PPGPU_CHECK_LAUNCH("ff_f64_kernel launch");
+    return set_ok();
+}
+
+static int ff64_dispatch(const FFParams &prm, int mode, int kind, cudaStream_t st) {
+    switch (mode) {
+        case PPGPU_FF_LJ:
+            return launch_ff64<M_LJ, 0>(prm, st);
+        case PPGPU_FF_COULOMB:
+            if (kind == 0) return launch_ff64<M_COUL, 0>(prm, st);
+            if (kind == 1) return launch_ff64<M_COUL, 1>(prm, st);
+            return launch_ff64<M_COUL, 2>(prm, st);
+        case PPGPU_FF_LJC:
+            return launch_ff64<M_LJC, 0>(prm, st);
+        default:
+            return launch_ff64<M_QZS, 0>(prm, st);
+    }
+}
+
+// ------------------------------------------------------------------------ host
+
+template <int MODE, int KIND, bool WITH_E, int P>
+static int launch_ff(const FFParams &prm, bool ortho, cudaStream_t st) {
+    const long long nblk = (prm.nchunks + FF_THREADS - 1) / FF_THREADS;
+    if (nblk <= 0) return set_ok();
+    if (nblk > 0x7fffffffLL) return set_error(PPGPU_ERR_ARG, "ff grid too large (%lld blocks)", nblk);
+    if (ortho)
+        ff_kernel<MODE, KIND, WITH_E, true, P><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+    else
+        ff_kernel<MODE, KIND, WITH_E, false, P><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+    PPGPU_CHECK_LAUNCH("ff_kernel launch");
+    return set_ok();
+}
+
+template <int MODE, int KIND, int P>
+static int launch_ff_e(const FFParams &prm, bool with_e, bool ortho, cudaStream_t st) {
+    return with_e ? launch_ff<MODE, KIND, true, P>(prm, ortho, st) : launch_ff<MODE, KIND, false, P>(prm, ortho, st);
+}
+
+static int ff_dispatch(FFParams &prm, int mode, int kind, bool with_e, bool ortho, cudaStream_t st) {
+    constexpr int P8 = 8, P4 = 4;
+    switch (mode) {
+        case PPGPU_FF_LJ:
+            prm.nzc = (prm.ns[2] + P8 - 1) / P8;
+            prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
+            return launch_ff_e<M_LJ, 0, P8>(prm, with_e, ortho, st);
+        case PPGPU_FF_COULOMB:
+            if (kind == 0) {
+                prm.nzc = (prm.ns[2] + P8 - 1) / P8;
+                prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
+                return launch_ff_e<M_COUL, 0, P8>(prm, with_e, ortho, st);
+            }
+            if (kind == 1 || kind == 2) return ff64_dispatch(prm, mode, kind, st);
+            return set_error(PPGPU_ERR_ARG, "coulomb kind %d not in {0,1,2}", kind);
+        case PPGPU_FF_LJC:
+            prm.nzc = (prm.ns[2] + P4 - 1) / P4;
+            prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
+            return launch_ff_e<M_LJC, 0, P4>(prm, with_e, ortho, st);
+        case PPGPU_FF_QZS:
+            prm.nzc = (prm.ns[2] + P8 - 1) / P8;
+            prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
+            return launch_ff_e<M_QZS, 0, P8>(prm, with_e, ortho, st);
+        default:
+            return set_error(PPGPU_ERR_ARG, "unknown force-field mode %d", mode);
+    }
+}
+
+}  // namespace ppgpu
+
+using namespace ppgpu;
+
+extern "C" int ppgpu_pack_atoms(int natoms, const double *R, const double *cLJ, const double *kqq, float *out,
+                                int *ncharged_out) {
+    if (natoms < 0 || (natoms > 0 && (!R || !out))) return set_error(PPGPU_ERR_ARG, "pack_atoms: bad arguments");
+    std::vector<int> order;
+    order.reserve(natoms);
+    for (int i = 0; i < natoms; i++)
+        if (kqq && kqq[i] != 0.0) order.push_back(i);
+    const int nch = (int)order.size();
+    for (int i = 0; i < natoms; i++)
+        if (!(kqq && kqq[i] != 0.0)) order.push_back(i);
+    for (int r = 0; r < natoms; r++) {
+        const int i = order[r];
+        float *o = out + (size_t)r * PPGPU_ATOM_FLOATS;
+        for (int k = 0; k < 3; k++) {
+            const double x = R[3 * i + k];
+            const float hi = (float)x;
+            o[k] = hi;
+            o[4 + k] = (float)(x - (double)hi);
+        }
+        o[3] = kqq ? (float)kqq[i] : 0.f;
+        o[7] = 0.f;
+        const double c6 = cLJ ? cLJ[2 * i] : 0.0, c12 = cLJ ? cLJ[2 * i + 1] : 0.0;
+        o[8] = (float)c6;
+        o[9] = (float)c12;
+        o[10] = (float)(6.0 * c6);
+        o[11] = (float)(12.0 * c12);
+    }
+    if (ncharged_out) *ncharged_out = nch;
+    return set_ok();
+}
+
+extern "C" int ppgpu_ff_subgrid(float *FE, const int *n, const double *cell, const int *i0, const int *ns,
+                                const float *atoms, int natoms, int ncharged, int mode, int coul_kind, double Q,
+                                double Fmax, const double *Qs, const double *QZs, int flags, void *stream) {
+    if (!FE || !n || !cell || !i0 || !ns) return set_error(PPGPU_ERR_ARG, "ff_grid: null argument");
+    if (natoms < 0 || ncharged < 0 || ncharged > natoms) return set_error(PPGPU_ERR_ARG, "ff_grid: bad atom counts");
+    if (natoms > 0 && !atoms) return set_error(PPGPU_ERR_ARG, "ff_grid: null atoms");
+    if (((uintptr_t)atoms & 15u) != 0 || ((uintptr_t)FE & 15u) != 0)
+        return set_error(PPGPU_ERR_ARG, "ff_grid: atoms and FE must be 16-byte aligned");
+    for (int k = 0; k < 3; k++) {
+        if (n[k] <= 0 || ns[k] < 0 || i0[k] < 0 || i0[k] + ns[k] > n[k])
+            return set_error(PPGPU_ERR_ARG, "ff_grid: bad grid/sub-box on axis %d", k);
+    }
+    if (mode < PPGPU_FF_LJ || mode > PPGPU_FF_QZS) return set_error(PPGPU_ERR_ARG, "unknown force-field mode %d", mode);
+    if (mode == PPGPU_FF_COULOMB && (coul_kind < 0 || coul_kind > 2))
+        return set_error(PPGPU_ERR_ARG, "coulomb kind %d not in {0,1,2}", coul_kind);
+    if (mode == PPGPU_FF_QZS && (!Qs || !QZs)) return set_error(PPGPU_ERR_ARG, "ff_grid: QZS mode needs Qs, QZs");
+    GridGeom g;
+    int st = make_geom(n, cell, &g);
+    if (st) return st;
+    FFParams prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.FE = reinterpret_cast<float4 *>(FE);
+    prm.atoms = reinterpret_cast<const float4 *>(atoms);
+    prm.natoms = natoms;
+    prm.ncharged = ncharged;
+    for (int k = 0; k < 3; k++) {
+        prm.i0[k] = i0[k];
+        prm.ns[k] = ns[k];
+        prm.dA[k] = g.dcell[k];
+        prm.dB[k] = g.dcell[3 + k];
+        prm.dC[k] = g.dcell[6 + k];
+    }
+    // Forces.h:12 (R2SAFE = 1e-8 for the CPU core) and FF.cl:1 (1e-6 for the OpenCL grid).
+    prm.eps = (mode == PPGPU_FF_QZS) ? 1e-6f : 1.0e-8f;
+    prm.eps64 = (mode == PPGPU_FF_QZS) ? (double)1e-6f : (double)1.0e-8f;
+    prm.Q = (float)Q;
+    prm.Fmax = (float)Fmax;
+    prm.nq = 0;
+    if (mode == PPGPU_FF_QZS) {
+        // Coulomb constant of FF.cl:2, folded into the tip charges; zero charges dropped.
+        for (int q = 0; q < 4; q++) {
+            if (Qs[q] != 0.0) {
+                prm.Qs[prm.nq] = (float)Qs[q] * 14.399644f;
+                prm.QZs[prm.nq] = (float)QZs[q];
+                prm.nq++;
+            }
+        }
+    }
+    prm.accumulate = (flags & PPGPU_FF_ACCUMULATE) ? 1 : 0;
+    prm.err = device_error_word();
+    const bool with_e = (flags & PPGPU_FF_WITH_E) != 0;
+    const bool ortho = (g.dcell[6] == 0.0 && g.dcell[7] == 0.0);
+    if ((long long)ns[0] * ns[1] * ns[2] == 0) return set_ok();
+    if (mode == PPGPU_FF_COULOMB && ncharged == 0 && !prm.accumulate) {
+        // Nothing charged: the grid is exactly zero (plus nothing to add when accumulating).
+        PPGPU_CUDA(cudaMemsetAsync(FE, 0, (size_t)ns[0] * ns[1] * ns[2] * 16, (cudaStream_t)stream), "memset FE");
+        return set_ok();
+    }
+    if (flags & PPGPU_FF_F64) return ff64_dispatch(prm, mode, coul_kind, (cudaStream_t)stream);
+    return ff_dispatch(prm, mode, coul_kind, with_e, ortho, (cudaStream_t)stream);
+}
+
+extern "C" int ppgpu_ff_grid(float *FE, const int *n, const double *cell, const float *atoms, int natoms,
+                             int ncharged, int mode, int coul_kind, double Q, double Fmax, const double *Qs,
+                             const double *QZs, int flags, void *stream) {
+    const int zero[3] = {0, 0, 0};
+    if (!n) return set_error(PPGPU_ERR_ARG, "ff_grid: null n");
+    return ppgpu_ff_subgrid(FE, n, cell, zero, n, atoms, natoms, ncharged, mode, coul_kind, Q, Fmax, Qs, QZs, flags,
+                            stream);
+}

@@ -1,0 +1,570 @@
+// pp_relax.cu -- probe-particle relaxation on sm_103a.
+//
+// CPU-core semantics (ppafm/cpp/ProbeParticle.cpp):
+//   relaxTipStrokes_omp 682-701, relaxTipStroke 633-676, relaxProbe 297-313,
+//   getPPforce 282-294, FIREstate::move 142-174, RELAX::move 84-88,
+//   interpolate3DvecWrap + SET_GRID_IND (ppafm/cpp/Grid.h:66-69, 93-111),
+//   forceRSpring (ppafm/cpp/Forces.h:85-89);
+//   Fz2df (ppafm/common.py:421-430) fused as a per-pixel epilogue.
+// AFMulator semantics (ppafm/ocl/cl/relax.cl):
+//   relaxStrokesTilted 391-464, update_FIRE 105-126, tipForce 37-41, convolveZ 571-608.
+//
+// Design (GB300):
+//  * One lane per stroke (pixel column).  A lane's whole z-walk is a single flattened
+//    loop in which every trip does exactly one trilinear gather (8 x 16-byte __ldg of
+//    the interleaved float4 grid), so lanes that converge early at one height move on
+//    to their next height instead of idling; the warp leaves the loop on a
+//    __any_sync vote once all of its lanes have finished their strokes.
+//  * Mixed precision, chosen by measurement against the float64 reference: the grid
+//    values, the trilinear weights and the FIRE mixing coefficient are float32; the FIRE
+//    state (d = r - r_tip, v, dt, acoef), the grid coordinate, the force sum and the
+//    radial-spring factor k (l - l0)/l are float64.  With a float32 state, rounding moves
+//    the stopping point of ~1.5 % of pixel heights by more than 1e-3 A inside the
+//    |F| < 1e-4 eV/A ball (the soft lateral spring leaves it ~6e-3 A wide); with this
+//    split every pixel height stays within 2e-4 A of the reference.
+//  * Trilinear weights are explicit float32 (no texture filtering).
+#include <cmath>
+#include <cstring>
+
+#include "pp_common.cuh"
+
+namespace ppgpu {
+
+constexpr int RELAX_THREADS = 128;
+constexpr int MAX_DF_TAPS = 64;
+constexpr unsigned FULL = 0xffffffffu;
+
+struct RelaxPrm {
+    const float4 *FE;
+    int n0, n1, n2;
+    double dicd[9];  // grid coordinate rows: g_k = r . dicd[3k..3k+2]
+    int maxIters;
+    double convF2, dtmax, acoef0, finc, fdec, falpha;
+    double lRad, kRad;
+    double rPP0[3], kSpring[3];
+    int relaxAlg, probeStart;
+    unsigned long long *iter_total;
+    int *err;
+};
+
+struct StrokeIO {  // relaxTipStrokes semantics (float64 in/out)
+    int nstroke, nstep;
+    const double *rTips;
+    double *rs, *fs;
+    int *iters, *itrsum;
+};
+
+struct ScanIO {  // regular scan semantics
+    int nx, ny, nz;
+    const double *xs, *ys, *zs;
+    double off[3];
+    float *fzs, *ppos, *df;
+    int *iters;
+    int nw;
+    float W[MAX_DF_TAPS];
+};
+
+// ----------------------------------------------------------- interpolation
+
+// Periodic trilinear interpolation of the force (Grid.h:93-111) at the float64 grid
+// coordinate g: integer corner and float32 fractional weights.
+__device__ __forceinline__ float3 interp_force(const float4 *__restrict__ FE, int n0, int n1, int n2, double3 g) {
+    const double fx = floor(g.x), fy = floor(g.y), fz = floor(g.z);
+    const float tx = (float)(g.x - fx), ty = (float)(g.y - fy), tz = (float)(g.z - fz);
+    const float mx = 1.f - tx, my = 1.f - ty, mz = 1.f - tz;
+    const int ix0 = wrap_index((int)fx, n0), iy0 = wrap_index((int)fy, n1), iz0 = wrap_index((int)fz, n2);
+    const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
+    const int iy1 = (iy0 + 1 == n1) ? 0 : iy0 + 1;
+    const int iz1 = (iz0 + 1 == n2) ? 0 : iz0 + 1;
+    const long long r00 = ((long long)ix0 * n1 + iy0) * n2, r01 = ((long long)ix0 * n1 + iy1) * n2;
+    const long long r10 = ((long long)ix1 * n1 + iy0) * n2, r11 = ((long long)ix1 * n1 + iy1) * n2;
+    const float4 c000 = ldg4(FE + r00 + iz0), c001 = ldg4(FE + r00 + iz1);
+    const float4 c010 = ldg4(FE + r01 + iz0), c011 = ldg4(FE + r01 + iz1);
+    const float4 c110 = ldg4(FE + r11 + iz0), c111 = ldg4(FE + r11 + iz1);
+    const float4 c100 = ldg4(FE + r10 + iz0), c101 = ldg4(FE + r10 + iz1);
+    const float mxmy = mx * my, mxty = mx * ty, txmy = tx * my, txty = tx * ty;
+    const float w0 = mxmy * mz, w1 = mxmy * tz, w2 = mxty * mz, w3 = mxty * tz;
+    const float w4 = txty * mz, w5 = txty * tz, w6 = txmy * mz, w7 = txmy * tz;
+    float3 o;
+    o.x = c000.x * w0;
+    o.y = c000.y * w0;
+    o.z = c000.z * w0;
+    o.x = fmaf(c001.x, w1, o.x); o.y = fmaf(c001.y, w1, o.y); o.z = fmaf(c001.z, w1, o.z);
+    o.x = fmaf(c010.x, w2, o.x); o.y = fmaf(c010.y, w2, o.y); o.z = fmaf(c010.z, w2, o.z);
+    o.x = fmaf(c011.x, w3, o.x); o.y = fmaf(c011.y, w3, o.y); o.z = fmaf(c011.z, w3, o.z);
+    o.x = fmaf(c110.x, w4, o.x); o.y = fmaf(c110.y, w4, o.y); o.z = fmaf(c110.z, w4, o.z);
+    o.x = fmaf(c111.x, w5, o.x); o.y = fmaf(c111.y, w5, o.y); o.z = fmaf(c111.z, w5, o.z);
+    o.x = fmaf(c100.x, w6, o.x); o.y = fmaf(c100.y, w6, o.y); o.z = fmaf(c100.z, w6, o.z);
+    o.x = fmaf(c101.x, w7, o.x); o.y = fmaf(c101.y, w7, o.y); o.z = fmaf(c101.z, w7, o.z);
+    return o;
+}
+
+// Same, all four channels, at a float grid coordinate (AFMulator path).
+__device__ __forceinline__ float4 interp_fe4(const float4 *__restrict__ FE, int n0, int n1, int n2, float3 g) {
+    const float fx = floorf(g.x), fy = floorf(g.y), fz = floorf(g.z);
+    const float tx = g.x - fx, ty = g.y - fy, tz = g.z - fz;
+    const float mx = 1.f - tx, my = 1.f - ty, mz = 1.f - tz;
+    const int ix0 = wrap_index((int)fx, n0), iy0 = wrap_index((int)fy, n1), iz0 = wrap_index((int)fz, n2);
+    const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
+    const int iy1 = (iy0 + 1 == n1) ? 0 : iy0 + 1;
+    const int iz1 = (iz0 + 1 == n2) ? 0 : iz0 + 1;
+    const long long r00 = ((long long)ix0 * n1 + iy0) * n2, r01 = ((long long)ix0 * n1 + iy1) * n2;
+    const long long r10 = ((long long)ix1 * n1 + iy0) * n2, r11 = ((long long)ix1 * n1 + iy1) * n2;
+    const float4 c000 = ldg4(FE + r00 + iz0), c001 = ldg4(FE + r00 + iz1);
+    const float4 c010 = ldg4(FE + r01 + iz0), c011 = ldg4(FE + r01 + iz1);
+    const float4 c100 = ldg4(FE + r10 + iz0), c101 = ldg4(FE + r10 + iz1);
+    const float4 c110 = ldg4(FE + r11 + iz0), c111 = ldg4(FE + r11 + iz1);
+    float4 o;
+#define PP_LERP3(c)                                                                                \
+    {                                                                                              \
+        const float v00 = fmaf(c100.c, tx, c000.c * mx), v10 = fmaf(c110.c, tx, c010.c * mx);     \
+        const float v01 = fmaf(c101.c, tx, c001.c * mx), v11 = fmaf(c111.c, tx, c011.c * mx);     \
+        const float v0 = fmaf(v10, ty, v00 * my), v1 = fmaf(v11, ty, v01 * my);                   \
+        o.c = fmaf(v1, tz, v0 * mz);                                                               \
+    }
+    PP_LERP3(x) PP_LERP3(y) PP_LERP3(z) PP_LERP3(w)
+#undef PP_LERP3
+    return o;
+}
+
+// Grid coordinate g_k = r . dicell_row_k of a float64 position (Grid.h:46-50).
+__device__ __forceinline__ double3 to_grid(const RelaxPrm &P, double x, double y, double z) {
+    return make_double3(fma(z, P.dicd[2], fma(y, P.dicd[1], x * P.dicd[0])),
+                        fma(z, P.dicd[5], fma(y, P.dicd[4], x * P.dicd[3])),
+                        fma(z, P.dicd[8], fma(y, P.dicd[7], x * P.dicd[6])));
+}
+
+// Probe-particle force = grid force + radial spring + lateral spring (getPPforce,
+// ProbeParticle.cpp:282-294; forceRSpring, Forces.h:85-89), in float64: the radial spring
+// is stiff, so l - l0 is a small difference of ~4 A lengths.
+__device__ __forceinline__ double3 pp_force(const RelaxPrm &P, float3 F, double3 d) {
+    const double l = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+    const double s = P.kRad * (l - P.lRad) / l;
+    double3 f;
+    f.x = fma(d.x - P.rPP0[0], P.kSpring[0], fma(d.x, s, (double)F.x));
+    f.y = fma(d.y - P.rPP0[1], P.kSpring[1], fma(d.y, s, (double)F.y));
+    f.z = fma(d.z - P.rPP0[2], P.kSpring[2], fma(d.z, s, (double)F.z));
+    return f;
+}
+
+// One FIRE move (FIREstate::move, ProbeParticle.cpp:153-172; relaxAlg 1) or damped
+// leap-frog (RELAX::move, ProbeParticle.cpp:84-88; relaxAlg 0).  The state is float64;
+// the FIRE mixing coefficient acoef*sqrt(vv/ff) is formed in float32.  Returns |f|^2.
+__device__ __forceinline__ double relax_move(const RelaxPrm &P, double3 f, double3 &d, double3 &v, double &dt,
+                                             double &acoef) {
+    const double ff = f.x * f.x + f.y * f.y + f.z * f.z;
+    double h;
+    if (P.relaxAlg == 1) {
+        const double vv = v.x * v.x + v.y * v.y + v.z * v.z;
+        const double vf = f.x * v.x + f.y * v.y + f.z * v.z;
+        if (vf < 0.0) {
+            v = make_double3(0.0, 0.0, 0.0);
+            dt = dt * P.fdec;
+            acoef = P.acoef0;
+        } else {
+            // ff == 0 gives cf = 0 (the reference would divide by zero)
+            const double cf = (ff > 0.0) ? (double)((float)acoef * sqrtf((float)vv / (float)ff)) : 0.0;
+            const double cv = 1.0 - acoef;
+            v.x = fma(f.x, cf, v.x * cv);
+            v.y = fma(f.y, cf, v.y * cv);
+            v.z = fma(f.z, cf, v.z * cv);
+            dt = fmin(dt * P.finc, P.dtmax);
+            acoef = acoef * P.falpha;
+        }
+        h = dt;
+    } else {
+        const double c = 1.0 - P.acoef0;
+        v.x *= c;
+        v.y *= c;
+        v.z *= c;
+        h = P.dtmax;
+    }
+    v.x = fma(f.x, h, v.x);
+    v.y = fma(f.y, h, v.y);
+    v.z = fma(f.z, h, v.z);
+    d.x = fma(v.x, h, d.x);
+    d.y = fma(v.y, h, d.y);
+    d.z = fma(v.z, h, d.z);
+    return ff;
+}
+
+__device__ __forceinline__ void add_iterations(unsigned long long *total, unsigned long long mine) {
+    if (!total) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(FULL, mine, o);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(total, mine);
+}
+
+// --------------------------------------------------------- CPU-core semantics
+
+template <bool SCAN>
+__global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, const StrokeIO S, const ScanIO C) {
+    const int s = blockIdx.x * RELAX_THREADS + threadIdx.x;
+    const int nstroke = SCAN ? C.nx * C.ny : S.nstroke;
+    const int nstep = SCAN ? C.nz : S.nstep;
+    bool active = s < nstroke && nstep > 0;
+
+    int ix = 0, iy = 0;
+    if (SCAN && active) {
+        ix = s / C.ny;
+        iy = s - ix * C.ny;
+    }
+    auto tip_at = [&](int iz) {
+        if (SCAN) return make_double3(C.xs[ix], C.ys[iy], C.zs[iz]);
+        const double *t = S.rTips + ((long long)s * nstep + iz) * 3;
+        return make_double3(t[0], t[1], t[2]);
+    };
+
+    double3 tip = make_double3(0.0, 0.0, 0.0), gt = tip;
+    double3 d = make_double3(P.rPP0[0], P.rPP0[1], P.rPP0[2]);  // first start: r = tip + rPP0
+    double3 v = make_double3(0.0, 0.0, 0.0);
+    double dt = P.dtmax, acoef = P.acoef0;
+    int iz = 0, it = 0, itcount = 0;
+    bool fin = P.maxIters <= 0;
+    int itsum = 0;
+    unsigned long long mine = 0;
+    if (active) {
+        tip = tip_at(0);
+        gt = to_grid(P, tip.x, tip.y, tip.z);
+    }
+
+    while (__any_sync(FULL, active)) {
+        if (!active) continue;
+        const double3 gd = to_grid(P, d.x, d.y, d.z);
+        const float3 F = interp_force(P.FE, P.n0, P.n1, P.n2, make_double3(gt.x + gd.x, gt.y + gd.y, gt.z + gd.z));
+        if (fin) {
+            // outputs of height iz: position after the last move, grid force there
+            if (SCAN) {
+                const long long o = (long long)s * nstep + (nstep - 1 - iz);
+                if (C.fzs) C.fzs[o] = F.z;
+                if (C.ppos) {
+                    C.ppos[3 * o + 0] = (float)((tip.x + d.x) + C.off[0]);
+                    C.ppos[3 * o + 1] = (float)((tip.y + d.y) + C.off[1]);
+                    C.ppos[3 * o + 2] = (float)((tip.z + d.z) + C.off[2]);
+                }
+                if (C.iters) C.iters[o] = itcount;
+            } else {
+                const long long o = (long long)s * nstep + iz;
+                S.rs[3 * o + 0] = tip.x + d.x;
+                S.rs[3 * o + 1] = tip.y + d.y;
+                S.rs[3 * o + 2] = tip.z + d.z;
+                S.fs[3 * o + 0] = F.x;
+                S.fs[3 * o + 1] = F.y;
+                S.fs[3 * o + 2] = F.z;
+                if (S.iters) S.iters[o] = itcount;
+            }
+            itsum += itcount;
+            iz++;
+            if (iz == nstep) {
+                active = false;
+                if (!SCAN && S.itrsum) S.itrsum[s] = itsum;
+                if (SCAN && C.df && C.fzs && C.nw > 0) {
+                    // np.convolve(fzs, W, 'valid') along ascending z (Fz2df, common.py:421-430)
+                    const float *f = C.fzs + (long long)s * nstep;
+                    const int nout = nstep - C.nw + 1;
+                    float *out = C.df + (long long)s * nout;
+                    for (int j = 0; j < nout; j++) {
+                        float acc = 0.f;
+                        for (int i = 0; i < C.nw; i++) acc = fmaf(f[j + i], C.W[C.nw - 1 - i], acc);
+                        out[j] = acc;
+                    }
+                }
+                continue;
+            }
+            // next height: warm start (relaxTipStroke, ProbeParticle.cpp:643-655)
+            const double3 nt = tip_at(iz);
+            if (P.probeStart == 0) {
+                d = make_double3(P.rPP0[0], P.rPP0[1], P.rPP0[2]);
+            } else if (P.probeStart == -1) {  // the probe stays where it was
+                d = make_double3((tip.x + d.x) - nt.x, (tip.y + d.y) - nt.y, (tip.z + d.z) - nt.z);
+            }  // probeStart == 1: d = r - r_tip carries over unchanged
+            tip = nt;
+            gt = to_grid(P, tip.x, tip.y, tip.z);
+            v = make_double3(0.0, 0.0, 0.0);
+            dt = P.dtmax;
+            acoef = P.acoef0;
+            it = 0;
+            fin = P.maxIters <= 0;
+            itcount = 0;
+            continue;
+        }
+        const double3 f = pp_force(P, F, d);
+        const double ff = relax_move(P, f, d, v, dt, acoef);
+        mine++;
+        if (ff < P.convF2) {
+            itcount = it;
+            fin = true;
+        } else if (++it >= P.maxIters) {
+            itcount = P.maxIters;
+            fin = true;
+        }
+    }
+    add_iterations(P.iter_total, mine);
+}
+
+// ------------------------------------------------------------- AFMulator semantics
+
+struct AfmPrm {
+    const float4 *FE;
+    int n0, n1, n2;
+    float dic[9];  // rows: transpose(inv(cell)) row k times n_k
+    float dtmax, damp0;
+    float stiff[4], dpos0[4];
+    float tA[3], tB[3], tC[3], zstep_w;
+    float surf;
+    int npix, nz;
+    const float4 *points;
+    float4 *FEs, *paths;
+    int *iters;
+    float *X;
+    int nw;
+    float W[MAX_DF_TAPS];
+    unsigned long long *iter_total;
+};
+
+__device__ __forceinline__ float dot3(float3 a, const float *b) { return a.x * b[0] + a.y * b[1] + a.z * b[2]; }
+
+__global__ void __launch_bounds__(RELAX_THREADS) relax_afm_kernel(const AfmPrm P) {
+    const int p = blockIdx.x * RELAX_THREADS + threadIdx.x;
+    bool active = p < P.npix && P.nz > 0;
+    const float3 dTip = make_float3(P.tC[0] * P.zstep_w, P.tC[1] * P.zstep_w, P.tC[2] * P.zstep_w);
+    // dpos0 rotated to the lab frame (rotMatT)
+    const float3 d0 = make_float3(P.tA[0] * P.dpos0[0] + P.tB[0] * P.dpos0[1] + P.tC[0] * P.dpos0[2],
+                                  P.tA[1] * P.dpos0[0] + P.tB[1] * P.dpos0[1] + P.tC[1] * P.dpos0[2],
+                                  P.tA[2] * P.dpos0[0] + P.tB[2] * P.dpos0[1] + P.tC[2] * P.dpos0[2]);
+    float3 tip = make_float3(0.f, 0.f, 0.f), pos = tip;
+    if (active) {
+        const float4 q = P.points[p];
+        tip = make_float3(q.x, q.y, q.z);
+        pos = make_float3(tip.x + d0.x, tip.y + d0.y, tip.z + d0.z);
+    }
+    float dt = P.dtmax, damp = P.damp0;
+    const float dtmin = P.dtmax * 0.1f;
+    float3 v = make_float3(0.f, 0.f, 0.f);
+    int iz = 0, it = 0;
+    unsigned long long mine = 0;
+    constexpr int NMAX = 128;  // N_RELAX_STEP_MAX (relax.cl:90)
+
+    while (__any_sync(FULL, active)) {
+        if (!active) continue;
+        float3 g;
+        g.x = dot3(pos, P.dic);
+        g.y = dot3(pos, P.dic + 3);
+        g.z = dot3(pos, P.dic + 6);
+        const float4 fe = interp_fe4(P.FE, P.n0, P.n1, P.n2, g);
+        float3 f = make_float3(fe.x, fe.y, fe.z);
+        const float3 dp = make_float3(pos.x - tip.x, pos.y - tip.y, pos.z - tip.z);
+        const float3 dq = make_float3(dot3(dp, P.tA), dot3(dp, P.tB), dot3(dp, P.tC));
+        const float r = sqrtf(dq.x * dq.x + dq.y * dq.y + dq.z * dq.z);
+        const float rad = P.stiff[3] * (r - P.dpos0[3]) / r;
+        const float3 ft = make_float3((dq.x - P.dpos0[0]) * P.stiff[0] + dq.x * rad,
+                                      (dq.y - P.dpos0[1]) * P.stiff[1] + dq.y * rad,
+                                      (dq.z - P.dpos0[2]) * P.stiff[2] + dq.z * rad);
+        f.x += P.tA[0] * ft.x + P.tB[0] * ft.y + P.tC[0] * ft.z + P.tC[0] * P.surf;
+        f.y += P.tA[1] * ft.x + P.tB[1] * ft.y + P.tC[1] * ft.z + P.tC[1] * P.surf;
+        f.z += P.tA[2] * ft.x + P.tB[2] * ft.y + P.tC[2] * ft.z + P.tC[2] * P.surf;
+        // update_FIRE (relax.cl:105-126)
+        const float ff = f.x * f.x + f.y * f.y + f.z * f.z;
+        const float vv = v.x * v.x + v.y * v.y + v.z * v.z;
+        const float vf = v.x * f.x + v.y * f.y + v.z * f.z;
+        if (vf < 0.f) {
+            v = make_float3(0.f, 0.f, 0.f);
+            dt = fmaxf(dtmin, dt * 0.5f);
+            damp = P.damp0;
+        } else {
+            const float cf = damp * sqrtf(vv / (ff + 1e-8f));
+            const float cv = 1.f - damp;
+            v.x = fmaf(f.x, cf, v.x * cv);
+            v.y = fmaf(f.y, cf, v.y * cv);
+            v.z = fmaf(f.z, cf, v.z * cv);
+            dt = fminf(P.dtmax, dt * 1.1f);
+            damp *= 0.99f;
+        }
+        v.x = fmaf(f.x, dt, v.x);
+        v.y = fmaf(f.y, dt, v.y);
+        v.z = fmaf(f.z, dt, v.z);
+        pos.x = fmaf(v.x, dt, pos.x);
+        pos.y = fmaf(v.y, dt, pos.y);
+        pos.z = fmaf(v.z, dt, pos.z);
+        mine++;
+        it++;
+        if (ff < 1e-8f || it >= NMAX) {
+            const long long o = (long long)p * P.nz + iz;
+            if (P.FEs) {
+                float4 r4;
+                r4.x = fe.x * P.tA[0] + fe.y * P.tA[1] + fe.z * P.tA[2];
+                r4.y = fe.x * P.tB[0] + fe.y * P.tB[1] + fe.z * P.tB[2];
+                r4.z = fe.x * P.tC[0] + fe.y * P.tC[1] + fe.z * P.tC[2];
+                r4.w = fe.w;
+                P.FEs[o] = r4;
+            }
+            if (P.paths) P.paths[o] = make_float4(pos.x, pos.y, pos.z, 0.f);
+            if (P.iters) P.iters[o] = (ff < 1e-8f) ? it - 1 : NMAX;
+            tip.x += dTip.x;
+            tip.y += dTip.y;
+            tip.z += dTip.z;
+            pos.x += dTip.x;
+            pos.y += dTip.y;
+            pos.z += dTip.z;
+            v = make_float3(0.f, 0.f, 0.f);
+            it = 0;
+            iz++;
+            if (iz == P.nz) {
+                active = false;
+                if (P.X && P.FEs && P.nw > 0) {
+                    // convolveZ (relax.cl:571-608): X[o] = sum_j FEs[o+j].z * W[j]
+                    const float4 *fin = P.FEs + (long long)p * P.nz;
+                    const int nout = P.nz - P.nw + 1;
+                    float *out = P.X + (long long)p * nout;
+                    for (int o2 = 0; o2 < nout; o2++) {
+                        float acc = 0.f;
+                        for (int j = 0; j < P.nw; j++) acc = fmaf(fin[o2 + j].z, P.W[j], acc);
+                        out[o2] = acc;
+                    }
+                }
+            }
+        }
+    }
+    add_iterations(P.iter_total, mine);
+}
+
+// ---------------------------------------------------------------------- host
+
+static int fill_relax_prm(RelaxPrm &P, const float *FE, const int *n, const double *cell, const double *prm,
+                          int probeStart, int relaxAlg, unsigned long long *iter_total) {
+    GridGeom g;
+    int st = make_geom(n, cell, &g);
+    if (st) return st;
+    memset(&P, 0, sizeof(P));
+    P.FE = reinterpret_cast<const float4 *>(FE);
+    P.n0 = n[0];
+    P.n1 = n[1];
+    P.n2 = n[2];
+    for (int k = 0; k < 9; k++) P.dicd[k] = g.dicell[k];
+    P.maxIters = (int)prm[0];
+    P.convF2 = prm[1];
+    P.dtmax = prm[2];
+    P.acoef0 = prm[3];
+    P.finc = prm[4];
+    P.fdec = prm[5];
+    P.falpha = prm[6];
+    P.lRad = prm[7];
+    P.kRad = prm[8];
+    for (int k = 0; k < 3; k++) {
+        P.rPP0[k] = prm[9 + k];
+        P.kSpring[k] = prm[12 + k];
+    }
+    if (relaxAlg != 0 && relaxAlg != 1) return set_error(PPGPU_ERR_ARG, "relaxAlg %d not in {0,1}", relaxAlg);
+    if (probeStart < -1 || probeStart > 1) return set_error(PPGPU_ERR_ARG, "probeStart %d not in {-1,0,1}", probeStart);
+    P.relaxAlg = relaxAlg;
+    P.probeStart = probeStart;
+    P.iter_total = iter_total;
+    P.err = device_error_word();
+    return set_ok();
+}
+
+}  // namespace ppgpu
+
+using namespace ppgpu;
+
+extern "C" int ppgpu_relax_strokes(const float *FE, const int *n, const double *cell, const double *prm,
+                                   int probeStart, int relaxAlg, int nstroke, int nstep, const double *rTips,
+                                   double *rs, double *fs, int *iters, int *itrsum,
+                                   unsigned long long *iter_total, void *stream) {
+    if (!FE || !n || !cell || !prm) return set_error(PPGPU_ERR_ARG, "relax_strokes: null argument");
+    if (nstroke < 0 || nstep < 0) return set_error(PPGPU_ERR_ARG, "relax_strokes: negative sizes");
+    if (nstroke == 0 || nstep == 0) return set_ok();
+    if (!rTips || !rs || !fs) return set_error(PPGPU_ERR_ARG, "relax_strokes: null stroke arrays");
+    RelaxPrm P;
+    int st = fill_relax_prm(P, FE, n, cell, prm, probeStart, relaxAlg, iter_total);
+    if (st) return st;
+    StrokeIO S = {nstroke, nstep, rTips, rs, fs, iters, itrsum};
+    ScanIO C;
+    memset(&C, 0, sizeof(C));
+    const unsigned nblk = (unsigned)((nstroke + RELAX_THREADS - 1) / RELAX_THREADS);
+    relax_kernel<false><<<nblk, RELAX_THREADS, 0, (cudaStream_t)stream>>>(P, S, C);
+    PPGPU_CHECK_LAUNCH("relax_kernel<strokes>");
+    return set_ok();
+}
+
+extern "C" int ppgpu_relax_scan(const float *FE, const int *n, const double *cell, const double *prm, int nx, int ny,
+                                int nz, const double *xs, const double *ys, const double *zs,
+                                const double *pos_offset, float *fzs, float *ppos, int *iters, int nw,
+                                const double *df_weights, float *df, unsigned long long *iter_total,
+                                void *stream) {
+    if (!FE || !n || !cell || !prm || !xs || !ys || !zs) return set_error(PPGPU_ERR_ARG, "relax_scan: null argument");
+    if (nx < 0 || ny < 0 || nz < 0) return set_error(PPGPU_ERR_ARG, "relax_scan: negative sizes");
+    if (df && (nw <= 0 || nw > MAX_DF_TAPS || nw > nz || !df_weights || !fzs))
+        return set_error(PPGPU_ERR_ARG, "relax_scan: df needs 1 <= nw <= min(64, nz), weights and fzs");
+    if (nx == 0 || ny == 0 || nz == 0) return set_ok();
+    RelaxPrm P;
+    int st = fill_relax_prm(P, FE, n, cell, prm, 1, 1, iter_total);
+    if (st) return st;
+    StrokeIO S;
+    memset(&S, 0, sizeof(S));
+    ScanIO C;
+    memset(&C, 0, sizeof(C));
+    C.nx = nx;
+    C.ny = ny;
+    C.nz = nz;
+    C.xs = xs;
+    C.ys = ys;
+    C.zs = zs;
+    for (int k = 0; k < 3; k++) C.off[k] = pos_offset ? pos_offset[k] : 0.0;
+    C.fzs = fzs;
+    C.ppos = ppos;
+    C.iters = iters;
+    C.df = df;
+    C.nw = df ? nw : 0;
+    for (int i = 0; i < C.nw; i++) C.W[i] = (float)df_weights[i];
+    const long long npix = (long long)nx * ny;
+    const unsigned nblk = (unsigned)((npix + RELAX_THREADS - 1) / RELAX_THREADS);
+    relax_kernel<true><<<nblk, RELAX_THREADS, 0, (cudaStream_t)stream>>>(P, S, C);
+    PPGPU_CHECK_LAUNCH("relax_kernel<scan>");
+    return set_ok();
+}
+
+extern "C" int ppgpu_relax_afm(const float *FE, const int *n, const double *inv_cell, const double *prm, int npix,
+                               const float *points, int nz, float *FEs, float *paths, int *iters, int nw,
+                               const double *weights, float *X, unsigned long long *iter_total, void *stream) {
+    if (!FE || !n || !inv_cell || !prm || (npix > 0 && !points))
+        return set_error(PPGPU_ERR_ARG, "relax_afm: null argument");
+    if (X && (nw <= 0 || nw > MAX_DF_TAPS || nw > nz || !weights || !FEs))
+        return set_error(PPGPU_ERR_ARG, "relax_afm: X needs 1 <= nw <= min(64, nz), weights and FEs");
+    if (npix <= 0 || nz <= 0) return set_ok();
+    AfmPrm P;
+    memset(&P, 0, sizeof(P));
+    P.FE = reinterpret_cast<const float4 *>(FE);
+    P.n0 = n[0];
+    P.n1 = n[1];
+    P.n2 = n[2];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) P.dic[3 * r + c] = (float)(inv_cell[3 * r + c] * n[r]);
+    P.dtmax = (float)prm[0];
+    P.damp0 = (float)prm[1];
+    for (int k = 0; k < 4; k++) {
+        P.stiff[k] = (float)prm[4 + k];
+        P.dpos0[k] = (float)prm[8 + k];
+    }
+    for (int k = 0; k < 3; k++) {
+        P.tA[k] = (float)prm[12 + k];
+        P.tB[k] = (float)prm[16 + k];
+        P.tC[k] = (float)prm[20 + k];
+    }
+    P.zstep_w = (float)prm[23];
+    P.surf = (float)prm[24];
+    P.npix = npix;
+    P.nz = nz;
+    P.points = reinterpret_cast<const float4 *>(points);
+    P.FEs = reinterpret_cast<float4 *>(FEs);
+    P.paths = reinterpret_cast<float4 *>(paths);
+    P.iters = iters;
+    P.X = X;
+    P.nw = X ? nw : 0;
+    for (int i = 0; i < P.nw; i++) P.W[i] = (float)weights[i];
+    P.iter_total = iter_total;
+    const unsigned nblk = (unsigned)((npix + RELAX_THREADS - 1) / RELAX_THREADS);
+    relax_afm_kernel<<<nblk, RELAX_THREADS, 0, (cudaStream_t)stream>>>(P);
+    PPGPU_CHECK_LAUNCH("relax_afm_kernel");
+    return set_ok();
+}

@@ -1,0 +1,194 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference ppafm package.
+
+Run where the reference checkout exists (it is read only):
+
+    python tests/golden/make_golden.py [/root/reference]
+
+The script copies the reference's ``ppafm`` package to a temporary directory, compiles
+its two C++ modules there from their own sources with g++ (ProbeParticle, GridUtils; the
+same flags as oracle/Makefile), stubs the unused ``toml`` import, and calls the
+reference's own functions on small seeded inputs.  Inputs and outputs are stored as
+float64 .npz files; the tests compare the oracle and the GPU path against them.
+"""
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def setup_reference(ref_root):
+    tmp = tempfile.mkdtemp(prefix="ppafm_golden_")
+    pkg = os.path.join(tmp, "ppafm")
+    shutil.copytree(os.path.join(ref_root, "ppafm"), pkg, ignore=shutil.ignore_patterns("*.so", "*.o", "__pycache__"))
+    cpp = os.path.join(pkg, "cpp")
+    for mod in ("ProbeParticle", "GridUtils"):
+        src = os.path.join(cpp, mod + ".cpp")
+        out = os.path.join(cpp, mod + "_lib.so")
+        subprocess.run(["g++", "-fPIC", "-std=c++11", "-O2", "-fopenmp", "-ffp-contract=off", "-shared", "-I", cpp, src, "-o", out], check=True)
+    with open(os.path.join(tmp, "toml.py"), "w") as f:
+        f.write("def load(*a, **k):\n    raise RuntimeError('toml unavailable')\n\ndef dump(*a, **k):\n    raise RuntimeError('toml unavailable')\n")
+    sys.path.insert(0, tmp)
+    return tmp
+
+
+def main(ref_root="/root/reference"):
+    tmp = setup_reference(ref_root)
+    try:
+        import ppafm.common as PPU
+        import ppafm.core as core
+        import ppafm.fieldFFT as fFFT
+        import ppafm.HighLevel as HL
+        import ppafm.io as pio
+
+        rng = np.random.default_rng(20241203)
+        # setFF_Fpointer registers a finalizer that clears the core's global grid pointer
+        # when the array dies (core.py:59-61); keep every grid alive so that rebinding a
+        # name does not clear the pointer of the grid registered next.
+        keep = []
+
+        # ---- Δf kernels and Fz -> Δf (common.py:333-430)
+        cases = [(0.1, 0.1), (1.0, 0.2), (1.0, 0.1), (0.5, 0.1), (2.0, 0.1), (1.0, 0.05), (0.3, 0.1), (1.7, 0.13)]
+        dfw = {f"w_{i}": PPU.get_df_weight(a, dz=d) for i, (a, d) in enumerate(cases)}
+        scases = [(5, 0.2), (10, 0.1), (2, 0.1), (1, 0.1), (7, 0.05)]
+        sw = {f"s_{i}": PPU.get_simple_df_weight(n=n, dz=d) for i, (n, d) in enumerate(scases)}
+        Fz = rng.normal(size=(4, 3, 30)) * 0.05
+        df1 = PPU.Fz2df(Fz, dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)
+        df2 = PPU.Fz2df(Fz, dz=0.1, k0=1800.0, f0=30300.0, amplitude=0.5)
+        np.savez_compressed(os.path.join(HERE, "df.npz"), cases=np.array(cases), scases=np.array(scases), Fz=Fz, df1=df1, df2=df2, **dfw, **sw)
+
+        # ---- atoms: species, PBC images, LJ mixing, scan grids
+        FFparams = PPU.loadSpecies()
+        species = np.array([(f[0], f[1], f[2], f[3]) for f in FFparams])
+        Zs = np.array([6, 6, 8, 1, 7, 9, 17, 1, 6, 8], dtype=np.int32)
+        Rs = np.column_stack([rng.uniform(1, 7, 10), rng.uniform(1, 7, 10), rng.uniform(-0.4, 0.4, 10)])
+        Qs = rng.uniform(-0.3, 0.3, 10)
+        Qs -= Qs.mean()
+        lvec = np.array([[0.0, 0.0, 0.0], [8.0, 0.0, 0.0], [0.7, 7.5, 0.0], [0.0, 0.0, 8.5]])
+
+        class P:  # the attributes PBCAtoms reads from a parameters object
+            nPBC = [1, 1, 1]
+
+        iZ9, R9, Q9 = PPU.PBCAtoms(Zs, Rs, Qs, avec=lvec[1], bvec=lvec[2], parameters=P())
+        cLJ9 = PPU.getAtomsLJ(8, iZ9, FFparams)
+        REAs = PPU.getAtomsREA(8, Zs, FFparams, alphaFac=-1.0)
+        cLJ_rea = PPU.REA2LJ(REAs)
+        Z3, xyz3, q3, c3, rea3 = PPU.PBCAtoms3D_np(Zs, Rs, Qs, cLJ_rea, REAs, lvec[1:], npbc=[1, 1, 0])
+
+        class S:
+            scanMin = [0.0, 0.0, 5.0]
+            scanMax = [7.5, 6.0, 7.9]
+            scanStep = [0.25, 0.5, 0.1]
+            r0Probe = [0.0, 0.0, 4.0]
+
+        xT, yT, zT, lvecScan = PPU.prepareScanGrids(parameters=S())
+        np.savez_compressed(os.path.join(HERE, "atoms.npz"), species=species, Zs=Zs, Rs=Rs, Qs=Qs, lvec=lvec, iZ9=iZ9, R9=R9, Q9=Q9, cLJ9=cLJ9, REAs=REAs, cLJ_rea=cLJ_rea, Z3=Z3, xyz3=xyz3, q3=q3, c3=c3, xT=xT, yT=yT, zT=zT, lvecScan=lvecScan)
+
+        # ---- force-field grids (ProbeParticle.cpp:508-554) on a skewed cell
+        n = np.array([16, 14, 12], dtype=np.int32)
+        Rs0 = HL.shift_positions(R9, -lvec[0])
+        out = {}
+        FF, V = HL.setFF(None, True, n=n, lvec=lvec)
+        keep += [FF, V]
+        core.getLennardJonesFF(Rs0, cLJ9)
+        out["F_lj"], out["E_lj"] = FF.copy(), V.copy()
+        for kind in (0, 1, 2):
+            FF, V = HL.setFF(None, True, n=n, lvec=lvec)
+            keep += [FF, V]
+            core.getCoulombFF(Rs0, Q9 * PPU.CoulombConst, kind=kind)
+            out[f"F_el{kind}"], out[f"E_el{kind}"] = FF.copy(), V.copy()
+        Fcl = out["F_lj"].copy()
+        pio.limit_vec_field(Fcl, Fmax=0.5)
+        np.savez_compressed(os.path.join(HERE, "ff.npz"), n=n, lvec=lvec, Rs0=Rs0, cLJs=cLJ9, kqq=Q9 * PPU.CoulombConst, F_clamped=Fcl, **out)
+
+        # ---- relaxed scan (HighLevel.py:104-184, ProbeParticle.cpp:633-701)
+        # orthogonal 10 A cell at 0.2 A; tip heights over a planar molecule
+        lv = np.array([[0.0, 0.0, 0.0], [10.0, 0.0, 0.0], [0.0, 10.0, 0.0], [0.0, 0.0, 10.0]])
+        nr = np.array([50, 50, 50], dtype=np.int32)
+        Zm = np.array([6, 6, 6, 6, 8, 1, 1, 7], dtype=np.int32)
+        ang = np.linspace(0, 2 * np.pi, 8, endpoint=False) + rng.uniform(-0.2, 0.2, 8)
+        Rm = np.column_stack([5 + 1.6 * np.cos(ang), 5 + 1.6 * np.sin(ang), np.zeros(8)])
+        Qm = rng.uniform(-0.25, 0.25, 8)
+        Qm -= Qm.mean()
+        iZr, Rr, Qr = PPU.PBCAtoms(Zm, Rm, Qm, avec=lv[1], bvec=lv[2], parameters=P())
+        cLJr = PPU.getAtomsLJ(8, iZr, FFparams)
+        FFLJ, _ = HL.setFF(None, False, n=nr, lvec=lv)
+        keep.append(FFLJ)
+        core.getLennardJonesFF(Rr, cLJr)
+        pio.limit_vec_field(FFLJ, Fmax=10.0)
+        FFLJ = FFLJ.copy()
+        FFel, _ = HL.setFF(None, False, n=nr, lvec=lv)
+        keep.append(FFel)
+        core.getCoulombFF(Rr, Qr * PPU.CoulombConst, kind=0)
+        pio.limit_vec_field(FFel, Fmax=10.0)
+        FFel = FFel.copy()
+
+        class R:
+            charge = -0.05
+            stiffness = [-1.0, -1.0, -1.0]
+            klat = 0.25
+            krad = 20.0
+            r0Probe = [0.0, 0.0, 4.0]
+            scanMin = [2.0, 2.5, 7.0]
+            scanMax = [7.8, 7.5, 9.9]
+            scanStep = [0.2, 0.25, 0.1]
+            tiltedScan = False
+            Apauli = 1.0
+            Vbias = 0.0
+
+        core.lib.setRelax(300, 1e-8, 0.5, 0.1)  # core.setRelax is broken (core.py:97-98)
+        core.lib.setFIRE(1.1, 0.5, 0.99)
+        fzs, PPpos, _, lvecScanR = HL.perform_relaxation(lv, FFLJ, FFel=FFel, parameters=R())
+        # iteration counts of a few strokes (relaxTipStroke returns the stroke's sum)
+        FF = FFLJ + FFel * R.charge
+        keep.append(FF)
+        HL.setFF(FF, lvec=lv)
+        core.setTip(kSpring=np.array((0.25, 0.25, 0.0)) / -PPU.eVA_Nm, kRadial=20.0 / -PPU.eVA_Nm, parameters=R())
+        xT, yT, zT, _ = PPU.prepareScanGrids(parameters=R())
+        picks = [(0, 0), (5, 7), (14, 3), (29, 20)]
+        itsum = []
+        for ix, iy in picks:
+            rT = np.zeros((len(zT), 3))
+            rT[:, 0] = xT[ix]
+            rT[:, 1] = yT[iy]
+            rT[:, 2] = zT[::-1]
+            itsum.append(core.relaxTipStroke(rT, np.zeros_like(rT), np.zeros_like(rT)))
+        df = PPU.Fz2df(fzs, dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)
+        np.savez_compressed(os.path.join(HERE, "relax.npz"), n=nr, lvec=lv, Zm=Zm, Rm=Rm, Qm=Qm, charge=R.charge, klat=R.klat, krad=R.krad, r0Probe=R.r0Probe, scanMin=R.scanMin, scanMax=R.scanMax, scanStep=R.scanStep, fzs=fzs, PPpos=PPpos, lvecScan=lvecScanR, picks=np.array(picks), itsum=np.array(itsum), df=df)
+
+        # ---- FFT route (fieldFFT.py:268-319)
+        fft = {}
+        for tag, dims, lvf in (
+            ("ortho", (24, 20, 16), np.array([[0.0, 0, 0], [6.0, 0, 0], [0, 5.0, 0], [0, 0, 4.0]])),
+            ("skew_odd", (15, 16, 17), np.array([[0.0, 0, 0], [6.0, 0, 0], [1.2, 5.5, 0], [0, 0.4, 4.3]])),
+        ):
+            V = rng.normal(size=dims)
+            rho = np.abs(rng.normal(size=dims))
+            fx, fy, fz, e = fFFT.potential2forces_mem(V.copy(), lvf, np.array(dims), rho=rho.copy(), doForce=True, doPot=True, deleteV=False)
+            fft.update({f"{tag}_V": V, f"{tag}_rho": rho, f"{tag}_lvec": lvf, f"{tag}_Fx": fx, f"{tag}_Fy": fy, f"{tag}_Fz": fz, f"{tag}_E": e})
+            cwd = os.getcwd()
+            os.chdir(tmp)  # potential2forces_mem writes rhoTip.xsf when it builds the tip density
+            try:
+                fx2, fy2, fz2, e2 = fFFT.potential2forces_mem(V.copy(), lvf, np.array(dims), sigma=0.7, multipole={"s": 1.0, "dz2": -0.3}, doForce=True, doPot=True, deleteV=False)
+            finally:
+                os.chdir(cwd)
+            fft.update({f"{tag}_mFx": fx2, f"{tag}_mFy": fy2, f"{tag}_mFz": fz2, f"{tag}_mE": e2})
+        np.savez_compressed(os.path.join(HERE, "fft.npz"), **fft)
+
+        # ---- clamp (io.py:766-778)
+        G = rng.normal(size=(5, 4, 3, 3)) * 20
+        Gc = G.copy()
+        pio.limit_vec_field(Gc, Fmax=10.0)
+        np.savez_compressed(os.path.join(HERE, "clamp.npz"), G=G, Gc=Gc)
+        print("golden fixtures written to", HERE)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

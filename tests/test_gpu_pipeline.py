@@ -1,0 +1,85 @@
+"""End-to-end pipelines on the GPU against the oracle: the CPU-core pipeline (LJ + Coulomb
+grids, clamps, FF composition, relaxed scan, Δf) on a scaled-down small_molecule workload,
+and the AFMulator point-charge pipeline against its float32 restatement."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_pipeline(oracle, w, relax):
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import common
+
+    Rs0, cLJs, kqq = HL.prepare_atoms(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w)
+    n = np.array(w["gridN"], np.int32)
+    lv = w["lvec"]
+    Fl, _ = oracle.lj_grid(n, lv[1:], Rs0, cLJs)
+    oracle.limit_vec_field(Fl, 10.0)
+    Fe, _ = oracle.coulomb_grid(n, lv[1:], Rs0, kqq, 0)
+    oracle.limit_vec_field(Fe, 10.0)
+    FF = Fl + w["charge"] * Fe
+    prm = HL.tip_vector(w, relax)
+    xT, yT, zT, _ = common.prepareScanGrids(w["scanMin"], w["scanMax"], w["scanStep"], w["r0Probe"])
+    fzs, pp, it = oracle.relaxed_scan(n, lv[1:], FF, prm, xT, yT, zT, lv[0])
+    df = oracle.Fz2df(fzs, w["scanStep"][2], w["kCantilever"], w["f0Cantilever"], w["Amplitude"])
+    return FF, fzs, pp, df, it
+
+
+def test_small_molecule_pipeline_vs_oracle(gpulib, oracle):
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import workloads
+
+    w = workloads.small_molecule(seed=1, scale=0.3)
+    relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    FF, fzs, pp, df, it = _oracle_pipeline(oracle, w, relax)
+    pl = HL.Pipeline(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w["gridN"], w, relax=relax, want_iters=True)
+    out = pl.run()
+    Fg, _ = pl.ff.to_host()
+    from tests.conftest import rel_err
+
+    assert rel_err(Fg, FF, 1e-2) < 1e-5
+    ppg = out["ppos"].cpu().numpy()
+    dpos = np.linalg.norm(ppg - pp, axis=-1)
+    flips = dpos > 0.05
+    assert flips.mean() <= 0.005
+    assert dpos[~flips].max() < 1e-3
+    dfg = out["df"].cpu().numpy()
+    ok = ~flips.any(axis=-1)
+    assert np.abs(dfg - df)[ok].max() < 0.1
+    itg = out["iters"].cpu().numpy()
+    assert abs(itg.mean() - it.mean()) < 0.05 * it.mean() + 0.5
+    assert pl.iterations() == int(itg.sum()) or pl.iterations() >= int(itg.sum())
+
+
+def test_afmulator_vs_oracle(gpulib, oracle):
+    from ppafm_gb300 import species
+    from ppafm_gb300.AFMulator import AFMulator
+
+    rng = np.random.default_rng(4)
+    na = 20
+    xyzs = np.column_stack([rng.uniform(4, 12, na), rng.uniform(4, 12, na), rng.uniform(-0.3, 0.3, na)])
+    Zs = rng.choice([1, 6, 7, 8], size=na)
+    qs = rng.uniform(-0.3, 0.3, na)
+    qs -= qs.mean()
+    kw = dict(pixPerAngstrome=10, scan_dim=(32, 28, 24), scan_window=((4.0, 4.0, 7.0), (12.0, 11.0, 9.4)), df_steps=8, npbc=(1, 1, 0))
+    lvec_sample = np.array([[16.0, 0, 0], [0, 16.0, 0], [0, 0, 20.0]])
+    afm = AFMulator(**kw)
+    X = afm.eval(xyzs, Zs, qs, sample_lvec=lvec_sample)
+    T = species.loadSpecies()
+    FFp = np.array([(r[0], r[1], r[2]) for r in T])
+    ora = oracle.AFMulator(FFp, **kw)
+    Xo, aux = ora.eval(xyzs, Zs, qs, sample_lvec=lvec_sample, return_all=True)
+    assert X.shape == Xo.shape == (32, 28, 24 - 8 + 1)
+    # float32 on both sides; relaxation trajectories agree to float rounding except at
+    # bistable pixels
+    d = np.abs(X - Xo)
+    bad = d > 0.1
+    assert bad.mean() < 0.01, bad.mean()
+    assert np.median(d) < 1e-2
+    # repeated eval reuses buffers and gives the same image
+    X2 = afm(xyzs, Zs, qs, sample_lvec=lvec_sample)
+    assert np.array_equal(X, X2)
+    with pytest.raises(NotImplementedError):
+        AFMulator(rho={"s": 1.0})

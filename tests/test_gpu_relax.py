@@ -1,0 +1,130 @@
+"""GPU relaxation and Δf against the reference-generated fixtures and the oracle.
+
+Bars: relaxed probe positions within 1e-3 A and Δf within 0.1 Hz of the reference, with
+bistable pixels (where float32 and float64 FIRE settle in different minima) counted and
+reported separately -- at most 0.5 % of the pixel heights may flip basin.  Grid forces at
+the relaxed positions: within 1e-4 eV/A absolute (the FIRE convergence force)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL = 1e-3
+DF_TOL = 0.1
+FLIP_FRAC = 0.005
+
+
+def _relax_fixture(oracle, golden):
+    from tests.test_oracle import _relax_golden_setup
+
+    g = golden("relax")
+    FF, prm, xT, yT, zT = _relax_golden_setup(oracle, g)
+    return g, FF, prm, xT, yT, zT
+
+
+def _split_flips(dpos):
+    """Per pixel height: position error; flips = error above 0.05 A (a different minimum)."""
+    flips = dpos > 0.05
+    return flips, dpos[~flips]
+
+
+def test_relax_scan_golden(gpulib, oracle, golden):
+    from ppafm_gb300 import common, device
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = g["lvec"]
+    ff = device.DeviceFF(g["n"], lv).from_host_f64(FF.reshape(-1, 3))
+    W = common.get_df_weight(1.0, dz=0.1) * 16.0217656 * 30000.0 / 1800.0
+    cnt = device.iter_counter()
+    out = device.relax_scan(ff, prm, xT - lv[0, 0], yT - lv[0, 1], zT[::-1] - lv[0, 2], pos_offset=lv[0], df_weights=W, want_iters=True, counter=cnt)
+    fzs = out["fzs"].cpu().numpy()
+    pp = out["ppos"].cpu().numpy()
+    it = out["iters"].cpu().numpy()
+    df = out["df"].cpu().numpy()
+    dpos = np.linalg.norm(pp - g["PPpos"], axis=-1)
+    flips, good = _split_flips(dpos)
+    assert flips.mean() <= FLIP_FRAC, f"{flips.sum()} basin flips"
+    assert good.max() < POS_TOL, good.max()
+    assert np.abs(fzs - g["fzs"])[~flips].max() < 1e-4
+    pix_ok = ~flips.any(axis=-1)
+    assert np.abs(df - g["df"])[pix_ok].max() < DF_TOL
+    # iteration counts of the sampled strokes: same FIRE, float32 vs float64 rounding
+    for (ix, iy), s in zip(g["picks"], g["itsum"]):
+        assert abs(int(it[ix, iy].sum()) - int(s)) <= 0.05 * s + 3
+    assert int(cnt.item()) >= int(it.sum())
+
+
+@pytest.mark.parametrize("probeStart,relaxAlg", [(1, 1), (0, 1), (-1, 1), (1, 0)])
+def test_dropin_relax_strokes_vs_oracle(gpulib, oracle, golden, probeStart, relaxAlg):
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import core
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = g["lvec"]
+    FFc = np.ascontiguousarray(FF)
+    HL.setFF(FFc, lvec=lv)
+    core.setRelax(300, 1e-8, 0.5 if relaxAlg == 1 else 0.1, 0.1)
+    core.setFIRE(1.1, 0.5, 0.99)
+    core.setTip(lRadial=4.0, kRadial=20.0 / -16.0217662, rPP0=np.array([0.0, 0.0, 0.0]), kSpring=np.array([0.25, 0.25, 0.0]) / -16.0217662)
+    rT = oracle.scan_tips(xT[::3], yT[::3], zT, lv[0])
+    rs = np.zeros_like(rT)
+    fs = np.zeros_like(rT)
+    core.relaxTipStrokes_omp(rT, rs, fs, probeStart=probeStart, relaxAlg=relaxAlg)
+    p2 = prm.copy()
+    if relaxAlg == 0:
+        p2[2] = 0.1
+    rs2, fs2, sums, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, p2, rT, probeStart=probeStart, relaxAlg=relaxAlg)
+    dpos = np.linalg.norm(rs - rs2, axis=-1)
+    flips, good = _split_flips(dpos)
+    assert flips.mean() <= FLIP_FRAC
+    assert good.max() < POS_TOL
+    assert np.abs(fs - fs2)[~flips].max() < 1e-4
+    assert core.last_iterations() > 0
+    # one stroke: the iteration sum is returned
+    s1 = core.relaxTipStroke(np.ascontiguousarray(rT[1, 1]), np.zeros_like(rT[1, 1]), np.zeros_like(rT[1, 1]), probeStart=probeStart, relaxAlg=relaxAlg)
+    assert abs(s1 - sums.reshape(rT.shape[0], rT.shape[1])[1, 1]) <= 0.05 * max(1, s1) + 3
+    core.deleteFF_Fpointer()
+
+
+def test_relax_edge_cases(gpulib, oracle, golden):
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import core
+    from ppafm_gb300._lib import PPGPUError
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = g["lvec"]
+    FFc = np.ascontiguousarray(FF)
+    HL.setFF(FFc, lvec=lv)
+    core.setTip(lRadial=4.0, kRadial=20.0 / -16.0217662, rPP0=np.array([0.0, 0.0, 0.0]), kSpring=np.array([0.25, 0.25, 0.0]) / -16.0217662)
+    rT = oracle.scan_tips(xT[:2], yT[:3], zT[:5], lv[0])
+    # maxIters = 0: no move; rs = start, fs = grid force there (reference loop body never runs)
+    core.setRelax(0, 1e-8, 0.5, 0.1)
+    rs = np.zeros_like(rT)
+    fs = np.zeros_like(rT)
+    core.relaxTipStrokes_omp(rT, rs, fs)
+    p0 = prm.copy()
+    p0[0] = 0
+    rs2, fs2, _, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, p0, rT)
+    assert np.abs(rs - rs2).max() < 1e-5 and np.abs(fs - fs2).max() < 1e-4
+    # empty stroke set
+    e = np.zeros((0, 3, 5, 3))
+    assert core.relaxTipStrokes_omp(e, e.copy(), e.copy()) == 0
+    # spline tips are refused, not silently ignored
+    with pytest.raises(PPGPUError):
+        core.relaxTipStrokes_omp(rT, rs, fs, tip_spline=object())
+    core.deleteFF_Fpointer()
+    with pytest.raises(PPGPUError):
+        core.relaxTipStrokes_omp(rT, rs, fs)
+
+
+def test_fz2df_gpu_golden(gpulib, golden):
+    from ppafm_gb300 import common
+
+    g = golden("df")
+    d1 = common.Fz2df(g["Fz"], dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)
+    d2 = common.Fz2df(g["Fz"], dz=0.1, k0=1800.0, f0=30300.0, amplitude=0.5)
+    assert d1.shape == g["df1"].shape and np.abs(d1 - g["df1"]).max() < 1e-3
+    assert np.abs(d2 - g["df2"]).max() < 1e-3
+    with pytest.raises(ValueError):
+        common.Fz2df(g["Fz"][..., :5], dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)

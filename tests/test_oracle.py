@@ -1,0 +1,185 @@
+"""Pins the CPU oracle: against the reference's own golden vectors (tests/test_common.py of
+ppafm), against fixtures produced by running the reference package (tests/golden), and
+bit for bit against the reference C++ core compiled from its sources (oracle/_ref)."""
+
+import numpy as np
+import pytest
+
+
+def test_df_weights_reference_test_vectors(oracle):
+    # ppafm tests/test_common.py:10-24
+    assert np.allclose(oracle.get_df_weight(0.1), np.array([-5.0, 5.0]))
+    assert np.allclose(oracle.get_df_weight(1.0, dz=0.2), np.array([-0.35594622, -0.22193265, -0.05447093, 0.05447093, 0.22193265, 0.35594622]))
+    assert np.allclose(oracle.get_simple_df_weight(n=5, dz=0.2), np.array([-0.31362841, -0.37274317, 0, 0.37274317, 0.31362841]))
+
+
+def test_df_weights_golden(oracle, golden):
+    g = golden("df")
+    for i, (a, d) in enumerate(g["cases"]):
+        assert np.array_equal(oracle.get_df_weight(a, dz=d), g[f"w_{i}"])
+    for i, (n, d) in enumerate(g["scases"]):
+        assert np.array_equal(oracle.get_simple_df_weight(n=int(n), dz=d), g[f"s_{i}"])
+
+
+def test_fz2df_golden(oracle, golden):
+    g = golden("df")
+    assert np.allclose(oracle.Fz2df(g["Fz"], 0.1, 1800.0, 30000.0, 1.0), g["df1"], rtol=1e-12, atol=1e-12)
+    assert np.allclose(oracle.Fz2df(g["Fz"], 0.1, 1800.0, 30300.0, 0.5), g["df2"], rtol=1e-12, atol=1e-12)
+    assert np.allclose(oracle.Fz2df_numpy(g["Fz"], 0.1, 1800.0, 30000.0, 1.0), g["df1"], rtol=1e-13, atol=0)
+
+
+def test_atoms_golden(oracle, golden):
+    g = golden("atoms")
+    FFp = g["species"][:, :3]
+    iZ, R, Q = oracle.PBCAtoms(g["Zs"], g["Rs"], g["Qs"], g["lvec"][1], g["lvec"][2])
+    assert np.array_equal(iZ, g["iZ9"]) and np.array_equal(R, g["R9"]) and np.array_equal(Q, g["Q9"])
+    assert np.array_equal(oracle.getAtomsLJ(8, iZ, FFp), g["cLJ9"])
+    REAs = oracle.getAtomsREA(8, g["Zs"], FFp)
+    assert np.array_equal(REAs, g["REAs"])
+    assert np.array_equal(oracle.REA2LJ(REAs), g["cLJ_rea"])
+    Z3, xyz3, q3, c3 = oracle.PBCAtoms3D_np(g["Zs"], g["Rs"], g["Qs"], g["cLJ_rea"], g["lvec"][1:], npbc=(1, 1, 0))
+    assert np.array_equal(Z3, g["Z3"]) and np.array_equal(xyz3, g["xyz3"]) and np.array_equal(q3, g["q3"]) and np.array_equal(c3, g["c3"])
+    xT, yT, zT, lv = oracle.prepareScanGrids([0.0, 0.0, 5.0], [7.5, 6.0, 7.9], [0.25, 0.5, 0.1], [0.0, 0.0, 4.0])
+    for a, b in ((xT, "xT"), (yT, "yT"), (zT, "zT"), (lv, "lvecScan")):
+        assert np.array_equal(a, g[b])
+
+
+def test_ff_grids_golden_bitexact(oracle, golden):
+    g = golden("ff")
+    n, lvec = g["n"], g["lvec"]
+    F, E = oracle.lj_grid(n, lvec[1:], g["Rs0"], g["cLJs"], gridE=np.zeros(tuple(n)))
+    assert np.array_equal(F, g["F_lj"]) and np.array_equal(E, g["E_lj"])
+    for kind in (0, 1, 2):
+        F, E = oracle.coulomb_grid(n, lvec[1:], g["Rs0"], g["kqq"], kind, gridE=np.zeros(tuple(n)))
+        assert np.array_equal(F, g[f"F_el{kind}"]), kind
+        assert np.array_equal(E, g[f"E_el{kind}"]), kind
+
+
+def test_ff_subgrid_matches_full(oracle, golden):
+    g = golden("ff")
+    n, lvec = g["n"], g["lvec"]
+    F, _ = oracle.ff_subgrid(n, lvec[1:], (3, 2, 5), (7, 9, 4), g["Rs0"], g["cLJs"], -1)
+    assert np.array_equal(F, g["F_lj"][3:10, 2:11, 5:9])
+
+
+def test_clamp_golden(oracle, golden):
+    g = golden("clamp")
+    G = g["G"].copy()
+    oracle.limit_vec_field(G, 10.0)
+    assert np.array_equal(G, g["Gc"])
+
+
+def _relax_golden_setup(oracle, g):
+    FFp = golden_species(oracle)
+    lv = g["lvec"]
+    iZ, R, Q = oracle.PBCAtoms(g["Zm"], g["Rm"], g["Qm"], lv[1], lv[2])
+    cLJ = oracle.getAtomsLJ(8, iZ, FFp)
+    n = g["n"]
+    FFLJ, _ = oracle.lj_grid(n, lv[1:], R, cLJ)
+    oracle.limit_vec_field(FFLJ, 10.0)
+    FFel, _ = oracle.coulomb_grid(n, lv[1:], R, Q * oracle.CoulombConst, 0)
+    oracle.limit_vec_field(FFel, 10.0)
+    FF = FFLJ + FFel * float(g["charge"])
+    tip = oracle.tip_params(4.0, float(g["krad"]) / -oracle.eVA_Nm, [0, 0, 0], np.array([g["klat"], g["klat"], 0.0]) / -oracle.eVA_Nm)
+    prm = oracle.relax_param_vector(tip, maxIters=300, convF2=1e-8, dt=0.5, damping=0.1)
+    xT, yT, zT, _ = oracle.prepareScanGrids(g["scanMin"], g["scanMax"], g["scanStep"], g["r0Probe"])
+    return FF, prm, xT, yT, zT
+
+
+def golden_species(oracle):
+    from ppafm_gb300 import species
+
+    t = species.loadSpecies()
+    return np.array([(r[0], r[1], r[2]) for r in t])
+
+
+def test_relax_golden_bitexact(oracle, golden):
+    g = golden("relax")
+    FF, prm, xT, yT, zT = _relax_golden_setup(oracle, g)
+    fzs, PPpos, iters = oracle.relaxed_scan(g["n"], g["lvec"][1:], FF, prm, xT, yT, zT, g["lvec"][0])
+    assert np.array_equal(fzs, g["fzs"])
+    assert np.array_equal(PPpos, g["PPpos"])
+    for (ix, iy), s in zip(g["picks"], g["itsum"]):
+        assert iters[ix, iy].sum() == s
+    assert np.allclose(oracle.Fz2df(fzs, 0.1, 1800.0, 30000.0, 1.0), g["df"], rtol=1e-12, atol=1e-12)
+
+
+def test_fft_route_golden(oracle, golden):
+    g = golden("fft")
+    for tag in ("ortho", "skew_odd"):
+        V, rho, lv = g[f"{tag}_V"], g[f"{tag}_rho"], g[f"{tag}_lvec"]
+        fx, fy, fz, e = oracle.potential2forces_mem(V, lv, V.shape, rho=rho, doPot=True)
+        for a, b in ((fx, "Fx"), (fy, "Fy"), (fz, "Fz"), (e, "E")):
+            assert np.allclose(a, g[f"{tag}_{b}"], rtol=1e-10, atol=1e-10 * np.abs(g[f"{tag}_{b}"]).max()), (tag, b)
+        fx, fy, fz, e = oracle.potential2forces_mem(V, lv, V.shape, sigma=0.7, multipole={"s": 1.0, "dz2": -0.3}, doPot=True)
+        for a, b in ((fx, "mFx"), (fy, "mFy"), (fz, "mFz"), (e, "mE")):
+            assert np.allclose(a, g[f"{tag}_{b}"], rtol=1e-10, atol=1e-10 * np.abs(g[f"{tag}_{b}"]).max()), (tag, b)
+
+
+def test_poisson_gaussian_kat(oracle):
+    """Known answer: the potential of a normalised Gaussian charge is q*k*erf(r/(sqrt2 s))/r
+    away from the periodic images (no reference counterpart for the Poisson step)."""
+    from math import erf
+
+    L, n, s = 24.0, 96, 0.8
+    x = (np.arange(n) * L / n) - L / 2
+    X, Y, Zg = np.meshgrid(x, x, x, indexing="ij")
+    r2 = X**2 + Y**2 + Zg**2
+    rho = np.exp(-r2 / (2 * s * s)) / ((2 * np.pi) ** 1.5 * s**3)
+    lv = np.array([[0, 0, 0], [L, 0, 0], [0, L, 0], [0, 0, L]], float)
+    V = oracle.poisson_hartree(rho, lv)
+    # compare potential differences (the periodic solution has an arbitrary offset and
+    # a small image/background correction that is quadratic in r)
+    i0 = n // 2
+    for k in (3, 6, 10):
+        r = x[i0 + k]
+        exact = oracle.CoulombConst * (erf(r / (np.sqrt(2) * s)) / r)
+        r1 = x[i0 + 3]
+        exact1 = oracle.CoulombConst * (erf(r1 / (np.sqrt(2) * s)) / r1)
+        num = V[i0 + k, i0, i0] - V[i0 + 3, i0, i0]
+        ana = exact - exact1
+        corr = oracle.CoulombConst * (2 * np.pi / 3) / L**3 * (r * r - r1 * r1)  # uniform neutralising background
+        assert abs(num - (ana + corr)) < 2e-3 * abs(ana) + 1e-3, (k, num, ana + corr)
+
+
+@pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).reference_available(), reason="reference library not built here")
+def test_oracle_vs_compiled_reference(oracle):
+    rng = np.random.default_rng(7)
+    ref = oracle.Reference()
+    L = ref.L
+    n = np.array([11, 13, 9], np.int32)
+    cell = np.array([[6.0, 0.3, 0.0], [0.0, 6.5, 0.2], [0.1, 0.0, 7.0]])
+    na = 17
+    Rs = rng.uniform(-1, 7, size=(na, 3))
+    cLJ = np.column_stack([rng.uniform(1, 10, na), rng.uniform(100, 3000, na)])
+    kqq = rng.uniform(-3, 3, na)
+    ref.set_grid(n, cell)
+    for kind in (-1, 0, 1, 2):
+        Fr = np.zeros(tuple(n) + (3,))
+        Er = np.zeros(tuple(n))
+        L.setFF_Fpointer(Fr)
+        L.setFF_Epointer(Er)
+        if kind < 0:
+            L.getLennardJonesFF(na, Rs, cLJ)
+            F, E = oracle.lj_grid(n, cell, Rs, cLJ, gridE=np.zeros(tuple(n)))
+        else:
+            L.getCoulombFF(na, Rs, kqq, kind)
+            F, E = oracle.coulomb_grid(n, cell, Rs, kqq, kind, gridE=np.zeros(tuple(n)))
+        assert np.array_equal(F, Fr) and np.array_equal(E, Er), kind
+    FF = np.clip(Fr, -3, 3).copy()
+    L.setFF_Fpointer(FF)
+    for maxit, dt, alg, ps in ((300, 0.5, 1, 1), (50, 0.2, 0, 0), (0, 0.5, 1, -1), (1, 0.3, 1, 1)):
+        L.setRelax(maxit, 1e-8, dt, 0.1)
+        L.setFIRE(1.1, 0.5, 0.99)
+        L.setTip(3.5, 15 / -oracle.eVA_Nm, np.array([0.2, -0.1, 0.0]), np.array([0.3, 0.3, 0]) / -oracle.eVA_Nm)
+        tip = oracle.tip_params(3.5, 15 / -oracle.eVA_Nm, [0.2, -0.1, 0], np.array([0.3, 0.3, 0]) / -oracle.eVA_Nm)
+        prm = oracle.relax_param_vector(tip, maxIters=maxit, convF2=1e-8, dt=dt, damping=0.1)
+        rT = np.zeros((3, 4, 7, 3))
+        rT[..., 0] = rng.uniform(0, 6, (3, 4, 1))
+        rT[..., 1] = rng.uniform(0, 6, (3, 4, 1))
+        rT[..., 2] = np.linspace(9.0, 8.2, 7)
+        rs = np.zeros_like(rT)
+        fs = np.zeros_like(rT)
+        L.relaxTipStrokes_omp(3, 4, ps, alg, 7, rT, rs, fs, None)
+        rs2, fs2, _, _ = oracle.relax_strokes(n, cell, FF, prm, rT, probeStart=ps, relaxAlg=alg)
+        assert np.array_equal(rs, rs2) and np.array_equal(fs, fs2), (maxit, dt, alg, ps)
