@@ -16,13 +16,14 @@
 //    to their next height instead of idling; the warp leaves the loop on a
 //    __any_sync vote once all of its lanes have finished their strokes.
 //  * Mixed precision, chosen by measurement against the float64 reference: the grid
-//    values, the trilinear weights and the FIRE mixing coefficient are float32; the FIRE
-//    state (d = r - r_tip, v, dt, acoef), the grid coordinate, the force sum and the
-//    radial-spring factor k (l - l0)/l are float64.  With a float32 state, rounding moves
-//    the stopping point of ~1.5 % of pixel heights by more than 1e-3 A inside the
-//    |F| < 1e-4 eV/A ball (the soft lateral spring leaves it ~6e-3 A wide); with this
-//    split every pixel height stays within 2e-4 A of the reference.
-//  * Trilinear weights are explicit float32 (no texture filtering).
+//    values and the FIRE mixing coefficient acoef*sqrt(vv/ff) are float32; the FIRE state
+//    (d = r - r_tip, v, dt, acoef), the grid coordinate, the trilinear weights and sum,
+//    the force sum and the radial-spring factor k (l - l0)/l are float64.  With a float32
+//    state, rounding moves the stopping point of ~1.5 % of pixel heights by more than
+//    1e-3 A inside the |F| < 1e-4 eV/A ball (the soft lateral spring leaves it ~6e-3 A
+//    wide); with this split the only difference from the reference is the float32
+//    rounding of the grid values.
+//  * Trilinear weights are explicit (no texture filtering).
 #include <cmath>
 #include <cstring>
 
@@ -67,11 +68,11 @@ struct ScanIO {  // regular scan semantics
 // ----------------------------------------------------------- interpolation
 
 // Periodic trilinear interpolation of the force (Grid.h:93-111) at the float64 grid
-// coordinate g: integer corner and float32 fractional weights.
-__device__ __forceinline__ float3 interp_force(const float4 *__restrict__ FE, int n0, int n1, int n2, double3 g) {
+// coordinate g: float32 grid values, float64 weights and accumulation.
+__device__ __forceinline__ double3 interp_force(const float4 *__restrict__ FE, int n0, int n1, int n2, double3 g) {
     const double fx = floor(g.x), fy = floor(g.y), fz = floor(g.z);
-    const float tx = (float)(g.x - fx), ty = (float)(g.y - fy), tz = (float)(g.z - fz);
-    const float mx = 1.f - tx, my = 1.f - ty, mz = 1.f - tz;
+    const double tx = g.x - fx, ty = g.y - fy, tz = g.z - fz;
+    const double mx = 1.0 - tx, my = 1.0 - ty, mz = 1.0 - tz;
     const int ix0 = wrap_index((int)fx, n0), iy0 = wrap_index((int)fy, n1), iz0 = wrap_index((int)fz, n2);
     const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
     const int iy1 = (iy0 + 1 == n1) ? 0 : iy0 + 1;
@@ -82,20 +83,16 @@ __device__ __forceinline__ float3 interp_force(const float4 *__restrict__ FE, in
     const float4 c010 = ldg4(FE + r01 + iz0), c011 = ldg4(FE + r01 + iz1);
     const float4 c110 = ldg4(FE + r11 + iz0), c111 = ldg4(FE + r11 + iz1);
     const float4 c100 = ldg4(FE + r10 + iz0), c101 = ldg4(FE + r10 + iz1);
-    const float mxmy = mx * my, mxty = mx * ty, txmy = tx * my, txty = tx * ty;
-    const float w0 = mxmy * mz, w1 = mxmy * tz, w2 = mxty * mz, w3 = mxty * tz;
-    const float w4 = txty * mz, w5 = txty * tz, w6 = txmy * mz, w7 = txmy * tz;
-    float3 o;
-    o.x = c000.x * w0;
-    o.y = c000.y * w0;
-    o.z = c000.z * w0;
-    o.x = fmaf(c001.x, w1, o.x); o.y = fmaf(c001.y, w1, o.y); o.z = fmaf(c001.z, w1, o.z);
-    o.x = fmaf(c010.x, w2, o.x); o.y = fmaf(c010.y, w2, o.y); o.z = fmaf(c010.z, w2, o.z);
-    o.x = fmaf(c011.x, w3, o.x); o.y = fmaf(c011.y, w3, o.y); o.z = fmaf(c011.z, w3, o.z);
-    o.x = fmaf(c110.x, w4, o.x); o.y = fmaf(c110.y, w4, o.y); o.z = fmaf(c110.z, w4, o.z);
-    o.x = fmaf(c111.x, w5, o.x); o.y = fmaf(c111.y, w5, o.y); o.z = fmaf(c111.z, w5, o.z);
-    o.x = fmaf(c100.x, w6, o.x); o.y = fmaf(c100.y, w6, o.y); o.z = fmaf(c100.z, w6, o.z);
-    o.x = fmaf(c101.x, w7, o.x); o.y = fmaf(c101.y, w7, o.y); o.z = fmaf(c101.z, w7, o.z);
+    const double mxmy = mx * my, mxty = mx * ty, txmy = tx * my, txty = tx * ty;
+    const double w[8] = {mxmy * mz, mxmy * tz, mxty * mz, mxty * tz, txty * mz, txty * tz, txmy * mz, txmy * tz};
+    const float4 c[8] = {c000, c001, c010, c011, c110, c111, c100, c101};
+    double3 o = make_double3(0.0, 0.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        o.x = fma((double)c[k].x, w[k], o.x);
+        o.y = fma((double)c[k].y, w[k], o.y);
+        o.z = fma((double)c[k].z, w[k], o.z);
+    }
     return o;
 }
 
@@ -137,13 +134,13 @@ __device__ __forceinline__ double3 to_grid(const RelaxPrm &P, double x, double y
 // Probe-particle force = grid force + radial spring + lateral spring (getPPforce,
 // ProbeParticle.cpp:282-294; forceRSpring, Forces.h:85-89), in float64: the radial spring
 // is stiff, so l - l0 is a small difference of ~4 A lengths.
-__device__ __forceinline__ double3 pp_force(const RelaxPrm &P, float3 F, double3 d) {
+__device__ __forceinline__ double3 pp_force(const RelaxPrm &P, double3 F, double3 d) {
     const double l = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
     const double s = P.kRad * (l - P.lRad) / l;
     double3 f;
-    f.x = fma(d.x - P.rPP0[0], P.kSpring[0], fma(d.x, s, (double)F.x));
-    f.y = fma(d.y - P.rPP0[1], P.kSpring[1], fma(d.y, s, (double)F.y));
-    f.z = fma(d.z - P.rPP0[2], P.kSpring[2], fma(d.z, s, (double)F.z));
+    f.x = fma(d.x - P.rPP0[0], P.kSpring[0], fma(d.x, s, F.x));
+    f.y = fma(d.y - P.rPP0[1], P.kSpring[1], fma(d.y, s, F.y));
+    f.z = fma(d.z - P.rPP0[2], P.kSpring[2], fma(d.z, s, F.z));
     return f;
 }
 
@@ -231,12 +228,12 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
     while (__any_sync(FULL, active)) {
         if (!active) continue;
         const double3 gd = to_grid(P, d.x, d.y, d.z);
-        const float3 F = interp_force(P.FE, P.n0, P.n1, P.n2, make_double3(gt.x + gd.x, gt.y + gd.y, gt.z + gd.z));
+        const double3 F = interp_force(P.FE, P.n0, P.n1, P.n2, make_double3(gt.x + gd.x, gt.y + gd.y, gt.z + gd.z));
         if (fin) {
             // outputs of height iz: position after the last move, grid force there
             if (SCAN) {
                 const long long o = (long long)s * nstep + (nstep - 1 - iz);
-                if (C.fzs) C.fzs[o] = F.z;
+                if (C.fzs) C.fzs[o] = (float)F.z;
                 if (C.ppos) {
                     C.ppos[3 * o + 0] = (float)((tip.x + d.x) + C.off[0]);
                     C.ppos[3 * o + 1] = (float)((tip.y + d.y) + C.off[1]);
