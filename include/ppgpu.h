@@ -177,6 +177,21 @@ int ppgpu_axpby_grid(float *FE_out, const float *FE_a, double a, const float *FE
 int ppgpu_grid_from_f64(float *FE, const double *F3, const double *E, long long npts, void *stream);
 int ppgpu_grid_to_f64(double *F3, double *E, const float *FE, long long npts, int accumulate, void *stream);
 
+/* ------------------------------------------------------------- no-allocation entry
+ * No counterpart in the reference.  The Lennard-Jones grid of getLennardJonesFF with device
+ * pointers: gridF [n0,n1,n2,3] and gridE [n0,n1,n2] (float64, either may be NULL) are
+ * ACCUMULATED into; Ratoms [natoms,3] (relative to the grid origin) and cLJs [natoms,2]
+ * (c6, c12) are float64 device arrays; n and cell are host arrays.  For callers that cannot
+ * allocate device memory at call time (an application whose allocator reserved the device
+ * memory up front; a latency-sensitive loop that cannot take the device-wide
+ * synchronisation of cudaMalloc/cudaFree): it allocates nothing and stages its scratch in a
+ * fixed 5.5 MB array that every GPU loading the library holds until exit.  Limits: natoms <=
+ * 32768 and n2 <= 262144 (larger requests return PPGPU_ERR_ARG).  The first call on a device
+ * looks up the array's device address.  All calls share the array: calls that overlap on
+ * the GPU race. */
+int ppgpu_lj_grid_f64_noalloc(double *gridF, double *gridE, const int *n, const double *cell, int natoms,
+                              const double *Ratoms, const double *cLJs, void *stream);
+
 /* ------------------------------------------------------------ measurement helper */
 /* Runs a dependent-FFMA kernel for `iters` iterations on all SMs and returns the number
  * of FP32 FMAs executed (the caller times it) -- the FP32 roofline denominator. */

@@ -62,6 +62,7 @@ SIGNATURES = {
     "ppgpu_grid_from_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_void_p], c_int),
     "ppgpu_grid_to_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_int, c_void_p], c_int),
     "ppgpu_ffma_peak": ([c_void_p, c_int, POINTER(c_longlong), c_void_p], c_int),
+    "ppgpu_lj_grid_f64_noalloc": ([c_void_p, c_void_p, _ip, _dp, c_int, c_void_p, c_void_p, c_void_p], c_int),
 }
 
 _lib = None

@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -753,4 +754,141 @@ extern "C" int ppgpu_ff_grid(float *FE, const int *n, const double *cell, const 
     if (!n) return set_error(PPGPU_ERR_ARG, "ff_grid: null n");
     return ppgpu_ff_subgrid(FE, n, cell, zero, n, atoms, natoms, ncharged, mode, coul_kind, Q, Fmax, Qs, QZs, flags,
                             stream);
+}
+
+// ===================================================================== no-allocation entry
+//
+// ppgpu_lj_grid_f64_noalloc: the Lennard-Jones grid of getLennardJonesFF, accumulated into a
+// caller-owned float64 device grid, for callers that must not allocate device memory at
+// call time -- an application whose own allocator reserved the device memory up front, or a
+// latency-sensitive loop that cannot afford the device-wide synchronisation of
+// cudaMalloc/cudaFree.  All scratch (the packed atom records, a float4 chunk of the grid and
+// the kernels' error word) lives in one fixed array below, so the call allocates nothing.
+//
+// Limits: at most NOALLOC_MAX_ATOMS atoms per call; the grid is processed in chunks of at
+// most NOALLOC_CHUNK_PTS points (one z column, n2, must fit in a chunk).  Every GPU that loads
+// the library holds the array (5.5 MB) until the process exits.  All calls share it and it
+// keeps the last call's contents: calls that overlap on the GPU (different streams, or
+// different host threads) race on it.
+
+namespace ppgpu {
+
+constexpr int NOALLOC_MAX_ATOMS = 32768;
+constexpr long long NOALLOC_CHUNK_PTS = 1LL << 18;
+constexpr size_t NOALLOC_REC_BYTES = (size_t)NOALLOC_MAX_ATOMS * FF_REC * 16;        // 1.5 MB
+constexpr size_t NOALLOC_CHUNK_BYTES = (size_t)NOALLOC_CHUNK_PTS * 16;                // 4 MB
+constexpr size_t NOALLOC_BYTES = NOALLOC_REC_BYTES + NOALLOC_CHUNK_BYTES + 256;      // + error word
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Packs LJ atoms (device float64 R [n,3], cLJ [n,2]) into the 48-byte records.
+__global__ void pack_lj_records_kernel(float *rec, const double *R, const double *cLJ, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float *o = rec + (size_t)i * 12;
+    for (int k = 0; k < 3; k++) {
+        const double x = R[3 * i + k];
+        const float hi = __double2float_rn(x);
+        o[k] = hi;
+        o[4 + k] = __double2float_rn(x - (double)hi);
+    }
+    o[3] = 0.f;
+    o[7] = 0.f;
+    const double c6 = cLJ[2 * i], c12 = cLJ[2 * i + 1];
+    o[8] = (float)c6;
+    o[9] = (float)c12;
+    o[10] = (float)(6.0 * c6);
+    o[11] = (float)(12.0 * c12);
+}
+
+static int noalloc_scratch_address(unsigned char **out) {
+    // cudaGetSymbolAddress once per device, with that device current (it allocates nothing).
+    static unsigned char *addr[64] = {nullptr};
+    static std::mutex mu;
+    int dev = 0;
+    PPGPU_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return set_error(PPGPU_ERR_NO_DEVICE, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        PPGPU_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
+        addr[dev] = (unsigned char *)p;
+    }
+    *out = addr[dev];
+    return PPGPU_OK;
+}
+
+}  // namespace ppgpu
+
+extern "C" int ppgpu_lj_grid_f64_noalloc(double *gridF, double *gridE, const int *n, const double *cell, int natoms,
+                                         const double *Ratoms, const double *cLJs, void *stream) {
+    if (!n || !cell) return set_error(PPGPU_ERR_ARG, "lj_grid_f64_noalloc: null n or cell");
+    if (!gridF && !gridE) return set_ok();
+    if (natoms < 0 || natoms > NOALLOC_MAX_ATOMS)
+        return set_error(PPGPU_ERR_ARG, "lj_grid_f64_noalloc: %d atoms; this entry point takes 0..%d", natoms,
+                         NOALLOC_MAX_ATOMS);
+    if (natoms > 0 && (!Ratoms || !cLJs)) return set_error(PPGPU_ERR_ARG, "lj_grid_f64_noalloc: null atom arrays");
+    if (n[2] > NOALLOC_CHUNK_PTS)
+        return set_error(PPGPU_ERR_ARG, "lj_grid_f64_noalloc: n2 = %d exceeds the %lld-point chunk", n[2],
+                         NOALLOC_CHUNK_PTS);
+    GridGeom g;
+    int st = make_geom(n, cell, &g);
+    if (st) return st;
+    unsigned char *base = nullptr;
+    if ((st = noalloc_scratch_address(&base))) return st;
+    float *rec = (float *)base;
+    float *chunk = (float *)(base + NOALLOC_REC_BYTES);
+    int *err = (int *)(base + NOALLOC_REC_BYTES + NOALLOC_CHUNK_BYTES);
+    cudaStream_t cs = (cudaStream_t)stream;
+    PPGPU_CUDA(cudaMemsetAsync(err, 0, sizeof(int), cs), "clear error word");
+    if (natoms > 0) {
+        pack_lj_records_kernel<<<(natoms + 127) / 128, 128, 0, cs>>>(rec, Ratoms, cLJs, natoms);
+        PPGPU_CHECK_LAUNCH("pack_lj_records_kernel");
+    }
+    FFParams prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.atoms = reinterpret_cast<const float4 *>(rec);
+    prm.natoms = natoms;
+    prm.ncharged = 0;
+    for (int k = 0; k < 3; k++) {
+        prm.dA[k] = g.dcell[k];
+        prm.dB[k] = g.dcell[3 + k];
+        prm.dC[k] = g.dcell[6 + k];
+    }
+    prm.eps = 1.0e-8f;
+    prm.eps64 = (double)1.0e-8f;
+    prm.err = err;
+    const bool with_e = gridE != nullptr;
+    const bool ortho = (g.dcell[6] == 0.0 && g.dcell[7] == 0.0);
+    // chunks: whole (iy, iz) planes when they fit, otherwise runs of whole z columns
+    const long long plane = (long long)n[1] * n[2];
+    for (int ia = 0; ia < n[0];) {
+        int na_, nb_ = n[1], ib = 0;
+        if (plane <= NOALLOC_CHUNK_PTS) {
+            na_ = (int)std::min<long long>(n[0] - ia, NOALLOC_CHUNK_PTS / plane);
+        } else {
+            na_ = 1;
+            nb_ = (int)(NOALLOC_CHUNK_PTS / n[2]);
+        }
+        for (ib = 0; ib < n[1]; ib += nb_) {
+            const int nbk = std::min(nb_, n[1] - ib);
+            prm.FE = reinterpret_cast<float4 *>(chunk);
+            prm.i0[0] = ia;
+            prm.i0[1] = ib;
+            prm.i0[2] = 0;
+            prm.ns[0] = na_;
+            prm.ns[1] = nbk;
+            prm.ns[2] = n[2];
+            prm.accumulate = 0;
+            if ((st = ff_dispatch(prm, PPGPU_FF_LJ, 0, with_e, ortho, cs))) return st;
+            const long long off = ((long long)ia * n[1] + ib) * n[2];
+            const long long m = (long long)na_ * nbk * n[2];
+            if ((st = ppgpu_grid_to_f64(gridF ? gridF + 3 * off : nullptr, gridE ? gridE + off : nullptr, chunk, m, 1,
+                                        stream)))
+                return st;
+            if (plane <= NOALLOC_CHUNK_PTS) break;
+        }
+        ia += na_;
+    }
+    return set_ok();
 }
