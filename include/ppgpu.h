@@ -83,11 +83,12 @@ long long ppgpu_last_iterations(void);
 
 /* ---------------------------------------------------------------- atom records
  * Force-field kernels read atoms as packed 48-byte records (12 floats):
- *   [x_hi, y_hi, z_hi, kqq] [x_lo, y_lo, z_lo, 0] [c6, c12, 6*c6, 12*c12]
+ *   [-x_hi, -y_hi, -x_lo, -y_lo] [-z_hi, -z_lo, -6*c6, 12*c12] [-c6, c12, kqq, 0]
  * where x = x_hi + x_lo splits the float64 coordinate (relative to the grid origin)
- * into two floats, kqq = k_e*Q_atom*(charge weight) and (c6, c12) are the
- * Lennard-Jones coefficients.  The first `ncharged` records are the atoms with
- * kqq != 0.  ppgpu_pack_atoms builds this layout on the host. */
+ * into two floats, kqq is the Coulomb coefficient of the atom (k_e*Q for the CPU-core
+ * modes, the bare charge for PPGPU_FF_QZS) and (c6, c12) are the Lennard-Jones
+ * coefficients.  The first `ncharged` records are the atoms with kqq != 0.
+ * ppgpu_pack_atoms builds this layout on the host. */
 #define PPGPU_ATOM_FLOATS 12
 int ppgpu_pack_atoms(int natoms, const double *R, const double *cLJ, const double *kqq, float *out,
                      int *ncharged_out);

@@ -39,6 +39,7 @@ constexpr int FF_THREADS = 256;
 constexpr int FF_TILE = 256;       // atoms per shared-memory stage
 constexpr int FF_REC = 3;          // float4 per atom record
 constexpr float R2CAP = 1e-4f;     // slow-path floor of r^2 (A^2)
+constexpr int SPLIT_MAX_CHARGED = 1024;  // LJC: charged atoms summed single-level up to this
 
 enum { M_LJ = 0, M_COUL = 1, M_LJC = 2, M_QZS = 3 };
 
@@ -51,7 +52,9 @@ struct FFParams {
     float eps;
     double eps64;
     float Q, Fmax;
-    float Qs[4], QZs[4];
+    float Qs[4], QZs[4];  // tip charges (times k_e) and their z offsets, zero charges dropped
+    float QZn2[4], QZnsq[4];  // -2 QZ and -QZ^2
+    float Qsum;
     int nq;
     int accumulate;
     long long nchunks;
@@ -104,117 +107,144 @@ __device__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
 }
 
 // ------------------------------------------------------------- pair interactions
+//
+// Atom record (48 B, written by ppgpu_pack_atoms), coordinates relative to the grid origin:
+//   r0 = (-x_hi, -y_hi, -x_lo, -y_lo)   r1 = (-z_hi, -z_lo, -6 c6, 12 c12)   r2 = (-c6, c12, kqq, 0)
+// The negated coordinates make the hi/lo displacement p - R a pair of packed adds, and the
+// LJ force factor 12 c12 ir6 - 6 c6 one fused multiply-add.
+//
+// Arithmetic is done on pairs of grid points with the packed float32x2 instructions
+// (fma.rn.f32x2 & co.), which issue two lanes' worth of FP32 work per instruction.
 
-// Lennard-Jones term (Forces.h:120-132) given r^2 (eps included) and dR.
-template <bool WITH_E>
-__device__ __forceinline__ void lj_term(float r2, float dx, float dy, float dz, const float4 &C, float &fx,
-                                        float &fy, float &fz, float &e) {
-    const float ir2 = rcp_approx(r2);
-    const float ir6 = ir2 * ir2 * ir2;
-    const float b = fmaf(C.w, ir6, -C.z);  // 12 c12 ir6 - 6 c6
-    const float fr = b * (ir6 * ir2);
-    fx = fmaf(fr, dx, fx);
-    fy = fmaf(fr, dy, fy);
-    fz = fmaf(fr, dz, fz);
-    if (WITH_E) e = fmaf(fmaf(C.y, ir6, -C.x), ir6, e);
-}
+__device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp2(float2 v) { return make_float2(rcp_approx(v.x), rcp_approx(v.y)); }
+__device__ __forceinline__ float2 rsqrt2(float2 v) { return make_float2(rsqrt_approx(v.x), rsqrt_approx(v.y)); }
 
-// Coulomb term (Forces.h:237-244): kqq/r and kqq dR/r^3.
-template <bool WITH_E>
-__device__ __forceinline__ void coul_term(float r2, float dx, float dy, float dz, float kqq, float &fx, float &fy,
-                                          float &fz, float &e) {
-    const float ir = rsqrt_approx(r2);
-    const float eq = kqq * ir;
-    const float fq = eq * (ir * ir);
-    fx = fmaf(fq, dx, fx);
-    fy = fmaf(fq, dy, fy);
-    fz = fmaf(fq, dz, fz);
-    if (WITH_E) e += eq;
-}
-
-// Number of accumulators per point for each mode.
-template <int MODE>
-struct NAcc {
-    static constexpr int v = (MODE == M_LJC) ? 8 : 4;
+// Accumulators for P2 pairs of points: force components and energy.
+template <int P2>
+struct Acc {
+    float2 x[P2], y[P2], z[P2], e[P2];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int p = 0; p < P2; p++) x[p] = y[p] = z[p] = e[p] = make_float2(0.f, 0.f);
+    }
+    __device__ __forceinline__ void fold_from(Acc &a) {
+#pragma unroll
+        for (int p = 0; p < P2; p++) {
+            x[p] = add2(x[p], a.x[p]);
+            y[p] = add2(y[p], a.y[p]);
+            z[p] = add2(z[p], a.z[p]);
+            e[p] = add2(e[p], a.e[p]);
+        }
+        a.zero();
+    }
 };
 
-// One atom against one point.  acc: [0..2] F (LJ or total), [3] E, [4..6] F_el, [7] E_el.
-template <int MODE, int KIND, bool WITH_E, bool CHARGED, bool CAP>
-__device__ __forceinline__ void atom_point(float dx, float dy, float dz, float dxy2, const float4 &A,
-                                           const float4 &C, const FFParams &prm, float *acc) {
-    (void)prm;
-    if (MODE == M_LJ) {
-        float r2 = fmaf(dz, dz, dxy2);
-        if (CAP) r2 = fmaxf(r2, R2CAP);
-        lj_term<WITH_E>(r2, dx, dy, dz, C, acc[0], acc[1], acc[2], acc[3]);
-    } else if (MODE == M_COUL) {
-        if (KIND == 0) {
-            float r2 = fmaf(dz, dz, dxy2);
-            if (CAP) r2 = fmaxf(r2, R2CAP);
-            coul_term<WITH_E>(r2, dx, dy, dz, A.w, acc[0], acc[1], acc[2], acc[3]);
-        } else if (KIND == 1) {  // pz: C(dz-0.1, -kqq) + C(dz+0.1, +kqq)  (x10 at the end)
-            float dm = dz - 0.1f, dp = dz + 0.1f;
-            float r2m = fmaf(dm, dm, dxy2), r2p = fmaf(dp, dp, dxy2);
-            if (CAP) {
-                r2m = fmaxf(r2m, R2CAP);
-                r2p = fmaxf(r2p, R2CAP);
-            }
-            coul_term<WITH_E>(r2m, dx, dy, dm, -A.w, acc[0], acc[1], acc[2], acc[3]);
-            coul_term<WITH_E>(r2p, dx, dy, dp, A.w, acc[0], acc[1], acc[2], acc[3]);
-        } else {  // dz2: C(dz,-2kqq) + C(dz-0.1,kqq) + C(dz+0.1,kqq)  (x100 at the end)
-            float dm = dz - 0.1f, dp = dz + 0.1f;
-            float r20 = fmaf(dz, dz, dxy2), r2m = fmaf(dm, dm, dxy2), r2p = fmaf(dp, dp, dxy2);
-            if (CAP) {
-                r20 = fmaxf(r20, R2CAP);
-                r2m = fmaxf(r2m, R2CAP);
-                r2p = fmaxf(r2p, R2CAP);
-            }
-            coul_term<WITH_E>(r20, dx, dy, dz, -2.f * A.w, acc[0], acc[1], acc[2], acc[3]);
-            coul_term<WITH_E>(r2m, dx, dy, dm, A.w, acc[0], acc[1], acc[2], acc[3]);
-            coul_term<WITH_E>(r2p, dx, dy, dp, A.w, acc[0], acc[1], acc[2], acc[3]);
-        }
-    } else if (MODE == M_LJC) {
-        float r2 = fmaf(dz, dz, dxy2);
-        if (CAP) r2 = fmaxf(r2, R2CAP);
-        if (CHARGED) {
-            const float ir = rsqrt_approx(r2);
-            const float ir2 = ir * ir;
-            const float ir6 = ir2 * ir2 * ir2;
-            const float b = fmaf(C.w, ir6, -C.z);
-            const float fr = b * (ir6 * ir2);
-            acc[0] = fmaf(fr, dx, acc[0]);
-            acc[1] = fmaf(fr, dy, acc[1]);
-            acc[2] = fmaf(fr, dz, acc[2]);
-            if (WITH_E) acc[3] = fmaf(fmaf(C.y, ir6, -C.x), ir6, acc[3]);
-            const float eq = A.w * ir;
-            const float fq = eq * ir2;
-            acc[4] = fmaf(fq, dx, acc[4]);
-            acc[5] = fmaf(fq, dy, acc[5]);
-            acc[6] = fmaf(fq, dz, acc[6]);
-            if (WITH_E) acc[7] += eq;
-        } else {
-            lj_term<WITH_E>(r2, dx, dy, dz, C, acc[0], acc[1], acc[2], acc[3]);
-        }
-    } else {  // M_QZS: LJ + sum_q Qs[q] * Coulomb(dz + QZs[q])
-        float r2 = fmaf(dz, dz, dxy2);
-        if (CAP) r2 = fmaxf(r2, R2CAP);
-        lj_term<WITH_E>(r2, dx, dy, dz, C, acc[0], acc[1], acc[2], acc[3]);
-        if (CHARGED) {
+// This thread's P2 pairs of points: hi/lo coordinates of the first point and offsets.
+template <int P2>
+struct Pts {
+    float2 hxy, lxy;
+    float hz, lz;
+    float2 ox[P2], oy[P2], oz[P2];
+};
+
+// Per-atom displacement to the first point and the shared in-plane terms.
+struct AtomGeo {
+    float2 dxv, dyv, dz0v, dxy2v;
+};
+
+template <int P2>
+__device__ __forceinline__ AtomGeo atom_geo(const Pts<P2> &q, const float4 &r0, const float4 &r1, float eps) {
+    const float2 dxy = add2(add2(q.hxy, make_float2(r0.x, r0.y)), add2(q.lxy, make_float2(r0.z, r0.w)));
+    const float dz0 = (q.hz + r1.x) + (q.lz + r1.y);
+    AtomGeo g;
+    g.dxv = bc(dxy.x);
+    g.dyv = bc(dxy.y);
+    g.dz0v = bc(dz0);
+    g.dxy2v = bc(fmaf(dxy.x, dxy.x, fmaf(dxy.y, dxy.y, eps)));
+    return g;
+}
+
+// Displacement of pair p and its r^2.
+template <bool ORTHO, int P2>
+__device__ __forceinline__ void pair_geo(const Pts<P2> &q, const AtomGeo &g, int p, float eps, float2 &dx, float2 &dy,
+                                         float2 &dz, float2 &r2) {
+    dz = add2(g.dz0v, q.oz[p]);
+    if (ORTHO) {
+        dx = g.dxv;
+        dy = g.dyv;
+        r2 = fma2(dz, dz, g.dxy2v);
+    } else {
+        dx = add2(g.dxv, q.ox[p]);
+        dy = add2(g.dyv, q.oy[p]);
+        r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, bc(eps))));
+    }
+}
+
+// LJ (Forces.h:120-132) of one atom on pair p, from ir2 = 1/r^2.
+template <bool WITH_E, int P2>
+__device__ __forceinline__ void lj_ir2(float2 ir2, float2 dx, float2 dy, float2 dz, float2 c6n6, float2 c12x12,
+                                       float2 c6n, float2 c12, Acc<P2> &a, int p) {
+    const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
+    const float2 fr = mul2(fma2(c12x12, ir6, c6n6), mul2(ir6, ir2));  // (12 c12 ir6 - 6 c6) ir8
+    a.x[p] = fma2(fr, dx, a.x[p]);
+    a.y[p] = fma2(fr, dy, a.y[p]);
+    a.z[p] = fma2(fr, dz, a.z[p]);
+    if (WITH_E) a.e[p] = fma2(fma2(c12, ir6, c6n), ir6, a.e[p]);  // c12 ir12 - c6 ir6
+}
+
+// Coulomb (Forces.h:237-244) of one atom on pair p, from ir = 1/r.
+template <bool WITH_E, int P2>
+__device__ __forceinline__ void coul_ir(float2 ir, float2 ir2, float2 dx, float2 dy, float2 dz, float2 kqq,
+                                        Acc<P2> &a, int p) {
+    const float2 eq = mul2(kqq, ir);
+    const float2 fq = mul2(eq, ir2);
+    a.x[p] = fma2(fq, dx, a.x[p]);
+    a.y[p] = fma2(fq, dy, a.y[p]);
+    a.z[p] = fma2(fq, dz, a.z[p]);
+    if (WITH_E) a.e[p] = add2(a.e[p], eq);
+}
+
+// The AFMulator tip charges (FF.cl:366-423): sum_k Qs_k Coulomb(dz + QZ_k) of one atom.
+// Written as Qsum*C(dz) + sum_k Qs_k [C(dz + QZ_k) - C(dz)] with the differences in a
+// cancellation-free form, because a neutral multipole tip (e.g. -10, +20, -10 e at
+// +-0.1 A) otherwise loses ~(r/QZ)^2 of the float32 significand.
+template <bool WITH_E, int P2>
+__device__ __forceinline__ void qzs_tip(const FFParams &prm, float q, float2 r2, float2 dx, float2 dy, float2 dz,
+                                        float2 dxy2, Acc<P2> &a, int p) {
+    const float2 ir0 = rsqrt2(r2);
+    const float2 a0 = mul2(r2, ir0);
+    const float2 ir03 = mul2(mul2(ir0, ir0), ir0);
+    if (prm.Qsum != 0.f) {
+        const float2 w = bc(q * prm.Qsum);
+        const float2 f = mul2(w, ir03);
+        a.x[p] = fma2(f, dx, a.x[p]);
+        a.y[p] = fma2(f, dy, a.y[p]);
+        a.z[p] = fma2(f, dz, a.z[p]);
+        if (WITH_E) a.e[p] = fma2(w, ir0, a.e[p]);
+    }
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (q < prm.nq) {
-                    const float dq = dz + prm.QZs[q];
-                    float rq = fmaf(dq, dq, dxy2);
-                    if (CAP) rq = fmaxf(rq, R2CAP);
-                    const float ir = rsqrt_approx(rq);
-                    const float eq = A.w * ir * prm.Qs[q];
-                    const float fq = eq * (ir * ir);
-                    acc[0] = fmaf(fq, dx, acc[0]);
-                    acc[1] = fmaf(fq, dy, acc[1]);
-                    acc[2] = fmaf(fq, dq, acc[2]);
-                    if (WITH_E) acc[3] += eq;
-                }
-            }
+    for (int k = 0; k < 4; k++) {
+        if (k < prm.nq) {
+            const float2 dq = add2(dz, bc(prm.QZs[k]));
+            const float2 r2q = fma2(dq, dq, dxy2);
+            const float2 irq = rsqrt2(r2q);
+            const float2 aq = mul2(r2q, irq);
+            const float2 num = fma2(bc(prm.QZn2[k]), dz, bc(prm.QZnsq[k]));  // r0^2 - rq^2 = -(2 dz QZ + QZ^2)
+            const float2 da = mul2(num, rcp2(add2(a0, aq)));                  // a0 - aq
+            const float2 d1 = mul2(da, mul2(ir0, irq));                      // 1/aq - 1/a0
+            const float2 irq3 = mul2(mul2(irq, irq), irq);
+            const float2 s3 = add2(add2(r2, r2q), mul2(a0, aq));              // a0^2 + a0 aq + aq^2
+            const float2 d3 = mul2(mul2(da, s3), mul2(ir03, irq3));           // 1/aq^3 - 1/a0^3
+            const float2 w = bc(q * prm.Qs[k]);
+            const float2 wd3 = mul2(w, d3);
+            a.x[p] = fma2(wd3, dx, a.x[p]);
+            a.y[p] = fma2(wd3, dy, a.y[p]);
+            a.z[p] = fma2(w, fma2(dz, d3, mul2(bc(prm.QZs[k]), irq3)), a.z[p]);  // (dz+QZ)/aq^3 - dz/a0^3
+            if (WITH_E) a.e[p] = fma2(w, d1, a.e[p]);
         }
     }
 }
@@ -234,59 +264,87 @@ __device__ __forceinline__ void clamp_vec(float &x, float &y, float &z, float Fm
     }
 }
 
-// Combines the accumulators of one point into (Fx,Fy,Fz,E).
-template <int MODE, int KIND, bool WITH_E>
-__device__ __forceinline__ float4 finalize(const float *t, const FFParams &prm) {
-    float4 o;
-    if (MODE == M_LJC) {
-        float ax = t[0], ay = t[1], az = t[2], bx = t[4], by = t[5], bz = t[6];
-        if (prm.Fmax > 0.f) {
-            clamp_vec(ax, ay, az, prm.Fmax);
-            clamp_vec(bx, by, bz, prm.Fmax);
-        }
-        o.x = fmaf(prm.Q, bx, ax);
-        o.y = fmaf(prm.Q, by, ay);
-        o.z = fmaf(prm.Q, bz, az);
-        o.w = WITH_E ? fmaf(prm.Q, t[7], t[3]) : 0.f;
-    } else {
-        const float s = (MODE == M_COUL && KIND == 1) ? 10.f : ((MODE == M_COUL && KIND == 2) ? 100.f : 1.f);
-        o.x = t[0] * s;
-        o.y = t[1] * s;
-        o.z = t[2] * s;
-        o.w = WITH_E ? t[3] * s : 0.f;
-    }
-    return o;
-}
-
 __device__ __forceinline__ bool finite4(const float4 &v) {
     return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w);
 }
 
-// Slow path for one point: all atoms from global memory, r^2 floored at R2CAP.
-template <int MODE, int KIND, bool WITH_E>
-__device__ float4 point_slow(const FFParams &prm, const float3 ph, const float3 pl) {
-    constexpr int NA = NAcc<MODE>::v;
-    float acc[NA];
-#pragma unroll
-    for (int c = 0; c < NA; c++) acc[c] = 0.f;
-    const int nat = (MODE == M_COUL) ? prm.ncharged : prm.natoms;
-    for (int j = 0; j < nat; j++) {
-        const float4 A = prm.atoms[3 * j], B = prm.atoms[3 * j + 1], C = prm.atoms[3 * j + 2];
-        const float dx = (ph.x - A.x) + (pl.x - B.x);
-        const float dy = (ph.y - A.y) + (pl.y - B.y);
-        const float dz = (ph.z - A.z) + (pl.z - B.z);
-        const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
-        if (j < prm.ncharged)
-            atom_point<MODE, KIND, WITH_E, true, true>(dx, dy, dz, dxy2, A, C, prm, acc);
-        else
-            atom_point<MODE, KIND, WITH_E, false, true>(dx, dy, dz, dxy2, A, C, prm, acc);
+// Final value of one point from its LJ-or-total sums t and (LJC) electrostatic sums u.
+template <int MODE, bool WITH_E>
+__device__ __forceinline__ float4 finalize(float tx, float ty, float tz, float te, float ux, float uy, float uz,
+                                           float ue, const FFParams &prm) {
+    float4 o;
+    if (MODE == M_LJC) {
+        if (prm.Fmax > 0.f) {
+            clamp_vec(tx, ty, tz, prm.Fmax);
+            clamp_vec(ux, uy, uz, prm.Fmax);
+        }
+        o.x = fmaf(prm.Q, ux, tx);
+        o.y = fmaf(prm.Q, uy, ty);
+        o.z = fmaf(prm.Q, uz, tz);
+        o.w = WITH_E ? fmaf(prm.Q, ue, te) : 0.f;
+    } else {
+        o = make_float4(tx, ty, tz, WITH_E ? te : 0.f);
     }
-    return finalize<MODE, KIND, WITH_E>(acc, prm);
+    return o;
 }
 
-template <int MODE, int KIND, bool WITH_E, bool ORTHO, int P>
+// Slow path for one point: all atoms from global memory, scalar, r^2 floored at R2CAP.
+template <int MODE, bool WITH_E>
+__device__ float4 point_slow(const FFParams &prm, double px, double py, double pz) {
+    const float hx = __double2float_rn(px), hy = __double2float_rn(py), hz = __double2float_rn(pz);
+    const float lx = __double2float_rn(px - (double)hx), ly = __double2float_rn(py - (double)hy),
+                lz = __double2float_rn(pz - (double)hz);
+    float t[4] = {0, 0, 0, 0}, u[4] = {0, 0, 0, 0};
+    const int nat = (MODE == M_COUL) ? prm.ncharged : prm.natoms;
+    for (int j = 0; j < nat; j++) {
+        const float4 r0 = prm.atoms[3 * j], r1 = prm.atoms[3 * j + 1], r2r = prm.atoms[3 * j + 2];
+        const float dx = (hx + r0.x) + (lx + r0.z);
+        const float dy = (hy + r0.y) + (ly + r0.w);
+        const float dz = (hz + r1.x) + (lz + r1.y);
+        const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
+        const float r2 = fmaxf(fmaf(dz, dz, dxy2), R2CAP);
+        const bool charged = j < prm.ncharged;
+        if (MODE != M_COUL) {
+            const float ir2 = 1.f / r2, ir6 = ir2 * ir2 * ir2;
+            const float fr = fmaf(r1.w, ir6, r1.z) * (ir6 * ir2);
+            t[0] = fmaf(fr, dx, t[0]);
+            t[1] = fmaf(fr, dy, t[1]);
+            t[2] = fmaf(fr, dz, t[2]);
+            t[3] = fmaf(fmaf(r2r.y, ir6, r2r.x), ir6, t[3]);
+        }
+        if ((MODE == M_COUL || MODE == M_LJC) && charged) {
+            const float ir = rsqrtf(r2);
+            const float eq = r2r.z * ir, fq = eq * ir * ir;
+            float *a = (MODE == M_LJC) ? u : t;
+            a[0] = fmaf(fq, dx, a[0]);
+            a[1] = fmaf(fq, dy, a[1]);
+            a[2] = fmaf(fq, dz, a[2]);
+            a[3] += eq;
+        }
+        if (MODE == M_QZS && charged) {
+            for (int k = 0; k < prm.nq; k++) {
+                const float dq = dz + prm.QZs[k];
+                const float rq = fmaxf(fmaf(dq, dq, dxy2), R2CAP);
+                const float ir = rsqrtf(rq);
+                const float eq = r2r.z * ir * prm.Qs[k], fq = eq * ir * ir;
+                t[0] = fmaf(fq, dx, t[0]);
+                t[1] = fmaf(fq, dy, t[1]);
+                t[2] = fmaf(fq, dq, t[2]);
+                t[3] += eq;
+            }
+        }
+    }
+    return finalize<MODE, WITH_E>(t[0], t[1], t[2], t[3], u[0], u[1], u[2], u[3], prm);
+}
+
+// The force-field kernel.  SPLIT (LJC only): the atom tiles that hold charged atoms are
+// summed single-level into the totals and the electrostatic sums are then parked in the
+// output slots of this thread's points, so the long neutral-atom phase holds only the
+// LJ partial and total sums (used when the charged atoms are at most SPLIT_MAX_CHARGED
+// and the output is not accumulated).
+template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT>
 __global__ void __launch_bounds__(FF_THREADS) ff_kernel(const FFParams prm) {
-    constexpr int NA = NAcc<MODE>::v;
+    constexpr int P = 2 * P2;
     __shared__ __align__(128) float4 s_at[2][FF_TILE * FF_REC];
     __shared__ __align__(8) uint64_t s_bar[2];
     __shared__ int s_abort;
@@ -304,35 +362,35 @@ __global__ void __launch_bounds__(FF_THREADS) ff_kernel(const FFParams prm) {
         lb = (int)(col - (long long)la * prm.ns[1]);
     }
     const double ga = prm.i0[0] + la, gb = prm.i0[1] + lb, gc = prm.i0[2] + lz0;
-    double p[3];
+    double pd[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) p[k] = ((prm.dA[k] * ga) + prm.dB[k] * gb) + prm.dC[k] * gc;
-    float3 ph, pl;
-    ph.x = __double2float_rn(p[0]);
-    ph.y = __double2float_rn(p[1]);
-    ph.z = __double2float_rn(p[2]);
-    pl.x = __double2float_rn(p[0] - (double)ph.x);
-    pl.y = __double2float_rn(p[1] - (double)ph.y);
-    pl.z = __double2float_rn(p[2] - (double)ph.z);
-    float off[3][P];
+    for (int k = 0; k < 3; k++) pd[k] = ((prm.dA[k] * ga) + prm.dB[k] * gb) + prm.dC[k] * gc;
+    Pts<P2> q;
+    {
+        const float hx = __double2float_rn(pd[0]), hy = __double2float_rn(pd[1]), hz = __double2float_rn(pd[2]);
+        q.hxy = make_float2(hx, hy);
+        q.lxy = make_float2(__double2float_rn(pd[0] - (double)hx), __double2float_rn(pd[1] - (double)hy));
+        q.hz = hz;
+        q.lz = __double2float_rn(pd[2] - (double)hz);
 #pragma unroll
-    for (int k = 0; k < P; k++) {
-        off[0][k] = __double2float_rn(prm.dC[0] * k);
-        off[1][k] = __double2float_rn(prm.dC[1] * k);
-        off[2][k] = __double2float_rn(prm.dC[2] * k);
+        for (int p = 0; p < P2; p++) {
+            q.ox[p] = make_float2(__double2float_rn(prm.dC[0] * (2 * p)), __double2float_rn(prm.dC[0] * (2 * p + 1)));
+            q.oy[p] = make_float2(__double2float_rn(prm.dC[1] * (2 * p)), __double2float_rn(prm.dC[1] * (2 * p + 1)));
+            q.oz[p] = make_float2(__double2float_rn(prm.dC[2] * (2 * p)), __double2float_rn(prm.dC[2] * (2 * p + 1)));
+        }
     }
 
-    float acc[P][NA], tot[P][NA];
-#pragma unroll
-    for (int k = 0; k < P; k++)
-#pragma unroll
-        for (int c = 0; c < NA; c++) {
-            acc[k][c] = 0.f;
-            tot[k][c] = 0.f;
-        }
+    Acc<P2> tot, acc;
+    tot.zero();
+    acc.zero();
+    Acc<(MODE == M_LJC) ? P2 : 1> el;  // LJC electrostatic sums
+    el.zero();
+    Acc<(MODE == M_LJC && !SPLIT) ? P2 : 1> elacc;
+    elacc.zero();
 
     const int nat = (MODE == M_COUL) ? prm.ncharged : prm.natoms;
     const int ntiles = (nat + FF_TILE - 1) / FF_TILE;
+    const float eps = prm.eps;
 
     if (tid == 0) {
         mbar_init(&s_bar[0], 1);
@@ -349,100 +407,194 @@ __global__ void __launch_bounds__(FF_THREADS) ff_kernel(const FFParams prm) {
     }
     __syncthreads();
 
-    for (int t = 0; t < ntiles; t++) {
+    // Waits for tile t; false (after a bounded drain) if the copy never landed.
+    auto acquire = [&](int t) -> bool {
         const int s = t & 1;
         if (tid == 0) {
             if (!mbar_wait_bounded(&s_bar[s], (uint32_t)((t >> 1) & 1))) s_abort = 1;
         }
         __syncthreads();
         if (s_abort) {
-            // Drain: give any copy still in flight a bounded chance to land before exit.
             if (tid == 0) {
                 raise_device_error(prm.err, PPGPU_ERR_DEVICE_TIMEOUT);
                 for (int u = t; u < t + 2 && u < ntiles; u++) mbar_wait_bounded(&s_bar[u & 1], (uint32_t)((u >> 1) & 1));
             }
-            return;
+            return false;
         }
-        const int base = t * FF_TILE;
-        const int nj = min(FF_TILE, nat - base);
-        const int jc = max(0, min(nj, prm.ncharged - base));  // charged atoms of this tile
-        const float4 *S = &s_at[s][0];
-
-        auto run_atoms = [&](int j0, int j1, auto charged_tag) {
-            constexpr bool CH = decltype(charged_tag)::value;
-            for (int j = j0; j < j1; j++) {
-                const float4 A = S[3 * j], B = S[3 * j + 1], C = S[3 * j + 2];
-                if (ORTHO) {
-                    const float dx = (ph.x - A.x) + (pl.x - B.x);
-                    const float dy = (ph.y - A.y) + (pl.y - B.y);
-                    const float dz0 = (ph.z - A.z) + (pl.z - B.z);
-                    const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
-#pragma unroll
-                    for (int k = 0; k < P; k++)
-                        atom_point<MODE, KIND, WITH_E, CH, false>(dx, dy, dz0 + off[2][k], dxy2, A, C, prm, acc[k]);
-                } else {
-                    const float dx0 = (ph.x - A.x) + (pl.x - B.x);
-                    const float dy0 = (ph.y - A.y) + (pl.y - B.y);
-                    const float dz0 = (ph.z - A.z) + (pl.z - B.z);
-#pragma unroll
-                    for (int k = 0; k < P; k++) {
-                        const float dx = dx0 + off[0][k], dy = dy0 + off[1][k];
-                        const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, prm.eps));
-                        atom_point<MODE, KIND, WITH_E, CH, false>(dx, dy, dz0 + off[2][k], dxy2, A, C, prm, acc[k]);
-                    }
-                }
-            }
-        };
-        if (MODE == M_LJ) {
-            run_atoms(0, nj, std::false_type{});
-        } else if (MODE == M_COUL) {
-            run_atoms(0, nj, std::true_type{});
-        } else {
-            run_atoms(0, jc, std::true_type{});
-            run_atoms(jc, nj, std::false_type{});
-        }
-#pragma unroll
-        for (int k = 0; k < P; k++)
-#pragma unroll
-            for (int c = 0; c < NA; c++) {
-                tot[k][c] += acc[k][c];
-                acc[k][c] = 0.f;
-            }
-        __syncthreads();  // every thread is done with stage s
+        return true;
+    };
+    // Frees stage t & 1 and starts the copy of tile t + 2 into it.
+    auto release = [&](int t) {
+        __syncthreads();
         if (tid == 0 && t + 2 < ntiles) {
+            const int s = t & 1;
             const int nj2 = min(FF_TILE, nat - (t + 2) * FF_TILE);
             const uint32_t bytes = (uint32_t)nj2 * FF_REC * 16u;
             mbar_expect_tx(&s_bar[s], bytes);
             bulk_g2s(&s_at[s][0], prm.atoms + (size_t)(t + 2) * FF_TILE * FF_REC, bytes, &s_bar[s]);
+        }
+    };
+
+    // LJ of atoms [j0, j1) of a tile into accumulator set a (rcp path).
+    auto run_lj = [&](const float4 *S, int j0, int j1, Acc<P2> &a) {
+        for (int j = j0; j < j1; j++) {
+            const float4 r0 = S[3 * j], r1 = S[3 * j + 1];
+            float2 c6n = bc(0.f), c12 = bc(0.f);
+            if (WITH_E) {
+                const float4 r2r = S[3 * j + 2];
+                c6n = bc(r2r.x);
+                c12 = bc(r2r.y);
+            }
+            const AtomGeo g = atom_geo<P2>(q, r0, r1, eps);
+            const float2 c6n6 = bc(r1.z), c12x12 = bc(r1.w);
+#pragma unroll
+            for (int p = 0; p < P2; p++) {
+                float2 dx, dy, dz, r2;
+                pair_geo<ORTHO, P2>(q, g, p, eps, dx, dy, dz, r2);
+                lj_ir2<WITH_E, P2>(rcp2(r2), dx, dy, dz, c6n6, c12x12, c6n, c12, a, p);
+            }
+        }
+    };
+    // LJ + Coulomb of charged atoms [j0, j1) (rsqrt path) into a (LJ) and u (electrostatic).
+    auto run_ljc = [&](const float4 *S, int j0, int j1, Acc<P2> &a, auto &u) {
+        for (int j = j0; j < j1; j++) {
+            const float4 r0 = S[3 * j], r1 = S[3 * j + 1], r2r = S[3 * j + 2];
+            const AtomGeo g = atom_geo<P2>(q, r0, r1, eps);
+            const float2 c6n6 = bc(r1.z), c12x12 = bc(r1.w), c6n = bc(r2r.x), c12 = bc(r2r.y), kqq = bc(r2r.z);
+#pragma unroll
+            for (int p = 0; p < P2; p++) {
+                float2 dx, dy, dz, r2;
+                pair_geo<ORTHO, P2>(q, g, p, eps, dx, dy, dz, r2);
+                const float2 ir = rsqrt2(r2);
+                const float2 ir2 = mul2(ir, ir);
+                lj_ir2<WITH_E, P2>(ir2, dx, dy, dz, c6n6, c12x12, c6n, c12, a, p);
+                coul_ir<WITH_E, P2>(ir, ir2, dx, dy, dz, kqq, u, p);
+            }
+        }
+    };
+
+    if constexpr (MODE == M_LJC && SPLIT) {
+        const int ta = (prm.ncharged + FF_TILE - 1) / FF_TILE;
+        int t = 0;
+        for (; t < ta; t++) {  // tiles holding charged atoms: single-level
+            if (!acquire(t)) return;
+            const int base = t * FF_TILE, nj = min(FF_TILE, nat - base);
+            const int jc = min(nj, prm.ncharged - base);
+            const float4 *S = &s_at[t & 1][0];
+            run_ljc(S, 0, jc, tot, el);
+            run_lj(S, jc, nj, tot);
+            release(t);
+        }
+        // park the electrostatic sums in this thread's output slots
+        if (valid) {
+            const long long colbase = ((long long)la * prm.ns[1] + lb) * prm.ns[2];
+#pragma unroll
+            for (int p = 0; p < P2; p++) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int lz = lz0 + 2 * p + h;
+                    if (lz < prm.ns[2]) {
+                        const float4 v = h ? make_float4(el.x[p].y, el.y[p].y, el.z[p].y, el.e[p].y)
+                                           : make_float4(el.x[p].x, el.y[p].x, el.z[p].x, el.e[p].x);
+                        prm.FE[colbase + lz] = v;
+                    }
+                }
+            }
+        }
+        for (; t < ntiles; t++) {  // neutral atoms: two-level
+            if (!acquire(t)) return;
+            const int nj = min(FF_TILE, nat - t * FF_TILE);
+            run_lj(&s_at[t & 1][0], 0, nj, acc);
+            tot.fold_from(acc);
+            release(t);
+        }
+    } else {
+        for (int t = 0; t < ntiles; t++) {
+            if (!acquire(t)) return;
+            const int base = t * FF_TILE, nj = min(FF_TILE, nat - base);
+            const float4 *S = &s_at[t & 1][0];
+            if constexpr (MODE == M_LJ) {
+                run_lj(S, 0, nj, acc);
+            } else if constexpr (MODE == M_COUL) {
+                for (int j = 0; j < nj; j++) {
+                    const float4 r0 = S[3 * j], r1 = S[3 * j + 1], r2r = S[3 * j + 2];
+                    const AtomGeo g = atom_geo<P2>(q, r0, r1, eps);
+                    const float2 kqq = bc(r2r.z);
+#pragma unroll
+                    for (int p = 0; p < P2; p++) {
+                        float2 dx, dy, dz, r2;
+                        pair_geo<ORTHO, P2>(q, g, p, eps, dx, dy, dz, r2);
+                        const float2 ir = rsqrt2(r2);
+                        coul_ir<WITH_E, P2>(ir, mul2(ir, ir), dx, dy, dz, kqq, acc, p);
+                    }
+                }
+            } else if constexpr (MODE == M_LJC) {  // not split: two-level for both sums
+                const int jc = max(0, min(nj, prm.ncharged - base));
+                run_ljc(S, 0, jc, acc, elacc);
+                run_lj(S, jc, nj, acc);
+                el.fold_from(elacc);
+            } else {  // M_QZS
+                const int jc = max(0, min(nj, prm.ncharged - base));
+                run_lj(S, 0, nj, acc);
+                for (int j = 0; j < jc; j++) {
+                    const float4 r0 = S[3 * j], r1 = S[3 * j + 1], r2r = S[3 * j + 2];
+                    const AtomGeo g = atom_geo<P2>(q, r0, r1, eps);
+#pragma unroll
+                    for (int p = 0; p < P2; p++) {
+                        float2 dx, dy, dz, r2;
+                        pair_geo<ORTHO, P2>(q, g, p, eps, dx, dy, dz, r2);
+                        const float2 dxy2 = ORTHO ? g.dxy2v : fma2(dy, dy, fma2(dx, dx, bc(eps)));
+                        qzs_tip<WITH_E, P2>(prm, r2r.z, r2, dx, dy, dz, dxy2, acc, p);
+                    }
+                }
+            }
+            tot.fold_from(acc);
+            release(t);
         }
     }
 
     if (!valid) return;
     const long long colbase = ((long long)la * prm.ns[1] + lb) * prm.ns[2];
 #pragma unroll
-    for (int k = 0; k < P; k++) {
-        const int lz = lz0 + k;
-        if (lz >= prm.ns[2]) break;
-        float4 o = finalize<MODE, KIND, WITH_E>(tot[k], prm);
-        if (!finite4(o)) {
-            float3 pk_h, pk_l;
-            double q[3];
+    for (int p = 0; p < P2; p++) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) q[c] = ((prm.dA[c] * ga) + prm.dB[c] * gb) + prm.dC[c] * (gc + k);
-            pk_h = make_float3(__double2float_rn(q[0]), __double2float_rn(q[1]), __double2float_rn(q[2]));
-            pk_l = make_float3(__double2float_rn(q[0] - (double)pk_h.x), __double2float_rn(q[1] - (double)pk_h.y),
-                               __double2float_rn(q[2] - (double)pk_h.z));
-            o = point_slow<MODE, KIND, WITH_E>(prm, pk_h, pk_l);
+        for (int h = 0; h < 2; h++) {
+            const int lz = lz0 + 2 * p + h;
+            if (lz >= prm.ns[2]) continue;
+            float ux = 0.f, uy = 0.f, uz = 0.f, ue = 0.f;
+            if constexpr (MODE == M_LJC) {
+                if constexpr (SPLIT) {
+                    const float4 v = prm.FE[colbase + lz];
+                    ux = v.x;
+                    uy = v.y;
+                    uz = v.z;
+                    ue = v.w;
+                } else {
+                    ux = h ? el.x[p].y : el.x[p].x;
+                    uy = h ? el.y[p].y : el.y[p].x;
+                    uz = h ? el.z[p].y : el.z[p].x;
+                    ue = h ? el.e[p].y : el.e[p].x;
+                }
+            }
+            const float tx = h ? tot.x[p].y : tot.x[p].x, ty = h ? tot.y[p].y : tot.y[p].x;
+            const float tz = h ? tot.z[p].y : tot.z[p].x, te = h ? tot.e[p].y : tot.e[p].x;
+            float4 o = finalize<MODE, WITH_E>(tx, ty, tz, te, ux, uy, uz, ue, prm);
+            if (!finite4(o)) {
+                double qd[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) qd[c] = ((prm.dA[c] * ga) + prm.dB[c] * gb) + prm.dC[c] * (gc + 2 * p + h);
+                o = point_slow<MODE, WITH_E>(prm, qd[0], qd[1], qd[2]);
+            }
+            float4 *dst = prm.FE + colbase + lz;
+            if (prm.accumulate) {
+                const float4 old = *dst;
+                o.x += old.x;
+                o.y += old.y;
+                o.z += old.z;
+                o.w += old.w;
+            }
+            *dst = o;
         }
-        float4 *dst = prm.FE + colbase + lz;
-        if (prm.accumulate) {
-            const float4 old = *dst;
-            o.x += old.x;
-            o.y += old.y;
-            o.z += old.z;
-            o.w += old.w;
-        }
-        *dst = o;
     }
 }
 
@@ -490,28 +642,29 @@ __global__ void __launch_bounds__(FF_THREADS) ff_f64_kernel(const FFParams prm) 
         for (int i = tid; i < nj * FF_REC; i += FF_THREADS) s_at[i] = prm.atoms[(size_t)base * FF_REC + i];
         __syncthreads();
         for (int j = 0; j < nj; j++) {
-            const float4 A = s_at[3 * j], B = s_at[3 * j + 1], C = s_at[3 * j + 2];
-            const double dx = p[0] - ((double)A.x + (double)B.x);
-            const double dy = p[1] - ((double)A.y + (double)B.y);
-            double dz = p[2] - ((double)A.z + (double)B.z);
+            const float4 r0 = s_at[3 * j], r1 = s_at[3 * j + 1], r2r = s_at[3 * j + 2];
+            const double dx = p[0] + ((double)r0.x + (double)r0.z);
+            const double dy = p[1] + ((double)r0.y + (double)r0.w);
+            double dz = p[2] + ((double)r1.x + (double)r1.y);
+            const double c6 = -(double)r2r.x, c12 = (double)r2r.y, kqqa = (double)r2r.z;
             const bool charged = (base + j) < prm.ncharged;
             if (MODE == M_LJ || MODE == M_LJC || MODE == M_QZS) {
                 const double ir2 = 1.0 / (((dx * dx + dy * dy) + dz * dz) + prm.eps64);
                 const double ir6 = ir2 * ir2 * ir2;
-                const double e6 = (double)C.x * ir6;
-                const double e12 = (double)C.y * ir6 * ir6;
+                const double e6 = c6 * ir6;
+                const double e12 = c12 * ir6 * ir6;
                 const double fr = (12 * e12 - 6 * e6) * ir2;
                 F[0] += dx * fr;
                 F[1] += dy * fr;
                 F[2] += dz * fr;
                 E += e12 - e6;
             }
-            if (MODE == M_LJC && charged) Ge += coul64(dx, dy, dz, (double)A.w, G[0], G[1], G[2]);
+            if (MODE == M_LJC && charged) Ge += coul64(dx, dy, dz, kqqa, G[0], G[1], G[2]);
             if (MODE == M_QZS && charged) {
                 for (int k = 0; k < prm.nq; k++) {
                     const double dq = dz + (double)prm.QZs[k];
                     const double ir2 = 1.0 / (((dx * dx + dy * dy) + dq * dq) + prm.eps64);
-                    const double eq = (double)A.w * sqrt(ir2) * (double)prm.Qs[k];
+                    const double eq = kqqa * sqrt(ir2) * (double)prm.Qs[k];
                     const double fq = eq * ir2;
                     F[0] += dx * fq;
                     F[1] += dy * fq;
@@ -520,7 +673,7 @@ __global__ void __launch_bounds__(FF_THREADS) ff_f64_kernel(const FFParams prm) 
                 }
             }
             if (MODE == M_COUL) {
-                const double kqq = (double)A.w;
+                const double kqq = kqqa;
                 if (KIND == 0) {
                     E += coul64(dx, dy, dz, kqq, F[0], F[1], F[2]);
                 } else if (KIND == 1) {
@@ -604,47 +757,40 @@ static int ff64_dispatch(const FFParams &prm, int mode, int kind, cudaStream_t s
 
 // ------------------------------------------------------------------------ host
 
-template <int MODE, int KIND, bool WITH_E, int P>
-static int launch_ff(const FFParams &prm, bool ortho, cudaStream_t st) {
+template <int MODE, bool WITH_E, int P2, bool SPLIT>
+static int launch_ff(FFParams &prm, bool ortho, cudaStream_t st) {
+    prm.nzc = (prm.ns[2] + 2 * P2 - 1) / (2 * P2);
+    prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
     const long long nblk = (prm.nchunks + FF_THREADS - 1) / FF_THREADS;
     if (nblk <= 0) return set_ok();
     if (nblk > 0x7fffffffLL) return set_error(PPGPU_ERR_ARG, "ff grid too large (%lld blocks)", nblk);
     if (ortho)
-        ff_kernel<MODE, KIND, WITH_E, true, P><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+        ff_kernel<MODE, WITH_E, true, P2, SPLIT><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
     else
-        ff_kernel<MODE, KIND, WITH_E, false, P><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+        ff_kernel<MODE, WITH_E, false, P2, SPLIT><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
     PPGPU_CHECK_LAUNCH("ff_kernel launch");
     return set_ok();
 }
 
-template <int MODE, int KIND, int P>
-static int launch_ff_e(const FFParams &prm, bool with_e, bool ortho, cudaStream_t st) {
-    return with_e ? launch_ff<MODE, KIND, true, P>(prm, ortho, st) : launch_ff<MODE, KIND, false, P>(prm, ortho, st);
+template <int MODE, int P2, bool SPLIT = false>
+static int launch_ff_e(FFParams &prm, bool with_e, bool ortho, cudaStream_t st) {
+    return with_e ? launch_ff<MODE, true, P2, SPLIT>(prm, ortho, st) : launch_ff<MODE, false, P2, SPLIT>(prm, ortho, st);
 }
 
 static int ff_dispatch(FFParams &prm, int mode, int kind, bool with_e, bool ortho, cudaStream_t st) {
-    constexpr int P8 = 8, P4 = 4;
     switch (mode) {
         case PPGPU_FF_LJ:
-            prm.nzc = (prm.ns[2] + P8 - 1) / P8;
-            prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
-            return launch_ff_e<M_LJ, 0, P8>(prm, with_e, ortho, st);
+            return launch_ff_e<M_LJ, 4>(prm, with_e, ortho, st);
         case PPGPU_FF_COULOMB:
-            if (kind == 0) {
-                prm.nzc = (prm.ns[2] + P8 - 1) / P8;
-                prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
-                return launch_ff_e<M_COUL, 0, P8>(prm, with_e, ortho, st);
-            }
+            if (kind == 0) return launch_ff_e<M_COUL, 4>(prm, with_e, ortho, st);
             if (kind == 1 || kind == 2) return ff64_dispatch(prm, mode, kind, st);
             return set_error(PPGPU_ERR_ARG, "coulomb kind %d not in {0,1,2}", kind);
         case PPGPU_FF_LJC:
-            prm.nzc = (prm.ns[2] + P4 - 1) / P4;
-            prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
-            return launch_ff_e<M_LJC, 0, P4>(prm, with_e, ortho, st);
+            if (prm.ncharged <= SPLIT_MAX_CHARGED && !prm.accumulate)
+                return launch_ff_e<M_LJC, 4, true>(prm, with_e, ortho, st);
+            return launch_ff_e<M_LJC, 2, false>(prm, with_e, ortho, st);
         case PPGPU_FF_QZS:
-            prm.nzc = (prm.ns[2] + P8 - 1) / P8;
-            prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
-            return launch_ff_e<M_QZS, 0, P8>(prm, with_e, ortho, st);
+            return launch_ff_e<M_QZS, 4>(prm, with_e, ortho, st);
         default:
             return set_error(PPGPU_ERR_ARG, "unknown force-field mode %d", mode);
     }
@@ -667,19 +813,25 @@ extern "C" int ppgpu_pack_atoms(int natoms, const double *R, const double *cLJ, 
     for (int r = 0; r < natoms; r++) {
         const int i = order[r];
         float *o = out + (size_t)r * PPGPU_ATOM_FLOATS;
+        float hi[3], lo[3];
         for (int k = 0; k < 3; k++) {
             const double x = R[3 * i + k];
-            const float hi = (float)x;
-            o[k] = hi;
-            o[4 + k] = (float)(x - (double)hi);
+            hi[k] = (float)x;
+            lo[k] = (float)(x - (double)hi[k]);
         }
-        o[3] = kqq ? (float)kqq[i] : 0.f;
-        o[7] = 0.f;
         const double c6 = cLJ ? cLJ[2 * i] : 0.0, c12 = cLJ ? cLJ[2 * i + 1] : 0.0;
-        o[8] = (float)c6;
+        o[0] = -hi[0];
+        o[1] = -hi[1];
+        o[2] = -lo[0];
+        o[3] = -lo[1];
+        o[4] = -hi[2];
+        o[5] = -lo[2];
+        o[6] = (float)(-6.0 * c6);
+        o[7] = (float)(12.0 * c12);
+        o[8] = (float)(-c6);
         o[9] = (float)c12;
-        o[10] = (float)(6.0 * c6);
-        o[11] = (float)(12.0 * c12);
+        o[10] = kqq ? (float)kqq[i] : 0.f;
+        o[11] = 0.f;
     }
     if (ncharged_out) *ncharged_out = nch;
     return set_ok();
@@ -723,12 +875,17 @@ extern "C" int ppgpu_ff_subgrid(float *FE, const int *n, const double *cell, con
     prm.Q = (float)Q;
     prm.Fmax = (float)Fmax;
     prm.nq = 0;
+    prm.Qsum = 0.f;
     if (mode == PPGPU_FF_QZS) {
         // Coulomb constant of FF.cl:2, folded into the tip charges; zero charges dropped.
         for (int q = 0; q < 4; q++) {
             if (Qs[q] != 0.0) {
+                const float qz = (float)QZs[q];
                 prm.Qs[prm.nq] = (float)Qs[q] * 14.399644f;
-                prm.QZs[prm.nq] = (float)QZs[q];
+                prm.QZs[prm.nq] = qz;
+                prm.QZn2[prm.nq] = -2.f * qz;
+                prm.QZnsq[prm.nq] = -qz * qz;
+                prm.Qsum += prm.Qs[prm.nq];
                 prm.nq++;
             }
         }
@@ -786,19 +943,25 @@ __global__ void pack_lj_records_kernel(float *rec, const double *R, const double
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float *o = rec + (size_t)i * 12;
+    float hi[3], lo[3];
     for (int k = 0; k < 3; k++) {
         const double x = R[3 * i + k];
-        const float hi = __double2float_rn(x);
-        o[k] = hi;
-        o[4 + k] = __double2float_rn(x - (double)hi);
+        hi[k] = __double2float_rn(x);
+        lo[k] = __double2float_rn(x - (double)hi[k]);
     }
-    o[3] = 0.f;
-    o[7] = 0.f;
     const double c6 = cLJ[2 * i], c12 = cLJ[2 * i + 1];
-    o[8] = (float)c6;
+    o[0] = -hi[0];
+    o[1] = -hi[1];
+    o[2] = -lo[0];
+    o[3] = -lo[1];
+    o[4] = -hi[2];
+    o[5] = -lo[2];
+    o[6] = (float)(-6.0 * c6);
+    o[7] = (float)(12.0 * c12);
+    o[8] = (float)(-c6);
     o[9] = (float)c12;
-    o[10] = (float)(6.0 * c6);
-    o[11] = (float)(12.0 * c12);
+    o[10] = 0.f;
+    o[11] = 0.f;
 }
 
 static int noalloc_scratch_address(unsigned char **out) {

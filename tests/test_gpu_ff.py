@@ -145,9 +145,12 @@ def test_qzs_grid_vs_oracle(gpulib, oracle):
     ref64 = oracle.afm_ff_qzs64(nD, lvec, xyz, q, cLJ, np.array(Qs, np.float32).astype(np.float64), QZs, points=pts)
     ok = np.linalg.norm(ref64[:, :3], axis=-1) < 1e30
     assert rel_err(g64[pts[:, 0], pts[:, 1], pts[:, 2], :3][ok], ref64[ok, :3], FLOOR) < 1e-6
-    # float32 kernel vs the float64 twin
+    # float32 kernel vs the float64 twin.  The tip (-10, +20, -10 e at +-0.1 A) is a second
+    # difference of Coulomb terms; the kernel removes the (r/QZ)^2 cancellation, the first
+    # order (r/QZ ~ 30) remains: held to 5e-5, against ~3e-3 for the reference's own float32
+    # form (checked next).
     ok = np.linalg.norm(g64[..., :3], axis=-1) < 1e30
-    assert rel_err(g32[..., :3][ok], g64[..., :3][ok], FLOOR) < TOL
+    assert rel_err(g32[..., :3][ok], g64[..., :3][ok], FLOOR) < 5e-5
     # the float32 restatement of the reference (absolute coordinates, like the OpenCL
     # kernel) is itself only good to ~1e-3 near the cores
     ref = np.transpose(oracle.afm_ff_qzs(nD, lvec, xyz, q, cLJ, Qs, QZs), (2, 1, 0, 3)).astype(np.float64)

@@ -71,11 +71,12 @@ def test_pack_atoms_layout():
     assert nch[0] == 3
     order = [1, 3, 6, 0, 2, 4, 5, 7, 8]
     for r, i in enumerate(order):
-        hi, lo = out[r, 0:3].astype(np.float64), out[r, 4:7].astype(np.float64)
+        hi = -out[r, [0, 1, 4]].astype(np.float64)
+        lo = -out[r, [2, 3, 5]].astype(np.float64)
         assert np.allclose(hi + lo, R[i], rtol=0, atol=1e-12)
-        assert out[r, 3] == np.float32(kqq[i])
-        assert out[r, 8] == np.float32(cLJ[i, 0]) and out[r, 9] == np.float32(cLJ[i, 1])
-        assert out[r, 10] == np.float32(6 * cLJ[i, 0]) and out[r, 11] == np.float32(12 * cLJ[i, 1])
+        assert out[r, 10] == np.float32(kqq[i])
+        assert out[r, 8] == np.float32(-cLJ[i, 0]) and out[r, 9] == np.float32(cLJ[i, 1])
+        assert out[r, 6] == np.float32(-6 * cLJ[i, 0]) and out[r, 7] == np.float32(12 * cLJ[i, 1])
     # argument errors are reported, not crashed on
     assert L.ppgpu_pack_atoms(-1, None, None, None, None, None) == _lib.PPGPU_ERR_ARG
     assert "bad arguments" in _lib.last_error()
