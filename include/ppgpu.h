@@ -165,6 +165,33 @@ int ppgpu_relax_afm(const float *FE, const int *n, const double *inv_cell, const
                     const float *points, int nz, float *FEs, float *paths, int *iters, int nw,
                     const double *weights, float *X, unsigned long long *iter_total, void *stream);
 
+/* ------------------------------------------------------------------ FFT route
+ * A plan handle owns the cuFFT plans and spectrum buffers of one grid shape n (C order
+ * [n0][n1][n2], float32 real grids).  lvec: 4x3 float64 (origin, a, b, c). */
+#define PPGPU_FFT_F64 1 /* transforms and spectra in float64 (grids stay float32) */
+int ppgpu_fft_create(const int *n, int flags, void **handle);
+int ppgpu_fft_destroy(void *handle);
+/* potential2forces_mem (ppafm/fieldFFT.py:268-319): FE = (ACCUMULATE ? FE : 0)
+ * + scale * (Fx, Fy, Fz, E) of the cross-correlation of V with rho (E only with WITH_E). */
+int ppgpu_fft_potential2forces(void *handle, const float *V, const float *rho, const double *lvec, double scale,
+                               int flags, float *FE, void *stream);
+/* getProbeDensity (fieldFFT.py:99-118): normalised Gaussian of width sigma times the
+ * multipole coefficients (s, px, py, pz, dz2, dx2, dy2, dxy, dxz, dyz; NULL = pure s). */
+int ppgpu_fft_probe_density(void *handle, float *rho, const double *lvec, double sigma, const double *multipole,
+                            void *stream);
+/* handle_negative_density (ppafm/cli/conv_rho.py:18-22) when fix_negative, then rho^B (:63-64). */
+int ppgpu_fft_density_power(void *handle, float *rho, double B, int fix_negative, void *stream);
+/* Hartree potential (volts) of a periodic charge density (e/A^3): V_G = 4 pi k_e rho_G / G^2,
+ * zero mean.  No counterpart in the reference (it reads potentials from DFT files). */
+int ppgpu_fft_poisson(void *handle, const float *rho_charge, const double *lvec, float *V, void *stream);
+
+/* Sum of normalised 3-D Gaussians on a periodic grid (minimum-image distances): atoms is a
+ * DEVICE float64 array [natoms][5] = (x, y, z relative to the origin, sigma, weight).  Builds
+ * synthetic electron and tip densities; no counterpart in the reference (it reads densities
+ * from DFT files). */
+int ppgpu_gaussian_density(float *rho, const int *n, const double *lvec, int natoms, const double *atoms,
+                           int accumulate, void *stream);
+
 /* -------------------------------------------------------------- grid utilities */
 /* Fz -> df along the last axis: out[c][j] = scale * sum_i F[c][j+i] * W[nw-1-i]. */
 int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const double *W, double scale, float *out,

@@ -439,18 +439,42 @@ def handle_negative_density(rho):
 
 
 def poisson_hartree(rho_charge, lvec):
-    """Hartree potential V (eV per unit charge) of a periodic charge density (e/A^3) on an
-    orthogonal cell: V_k = 4*pi*k_e*rho_k/|G|^2, G = 2*pi*freq, zero mean.
-    No reference counterpart (ppafm has no Poisson solver); parity of this step is unpinned."""
+    """Hartree potential V (eV per unit charge) of a periodic charge density (e/A^3) on a
+    general cell: V_k = 4*pi*k_e*rho_k/|G|^2 with G = sum_j m_j b_j (b_j the reciprocal
+    basis, 2*pi included, m_j numpy's FFT frequency indices), zero mean.
+    No reference counterpart (ppafm has no Poisson solver); pinned by a Gaussian-charge
+    known answer instead."""
     n = rho_charge.shape
-    L = np.linalg.norm(np.asarray(lvec, dtype=np.float64)[1:4], axis=1)
-    g = [2 * np.pi * np.fft.fftfreq(n[k], d=L[k] / n[k]) for k in range(3)]
-    G2 = g[0][:, None, None] ** 2 + g[1][None, :, None] ** 2 + g[2][None, None, :] ** 2
+    cell = np.asarray(lvec, dtype=np.float64)[1:4]
+    B = 2 * np.pi * np.linalg.inv(cell).T  # rows b_j, a_i . b_j = 2 pi delta_ij
+    m = [np.fft.fftfreq(n[k], d=1.0 / n[k]) for k in range(3)]
+    M0, M1, M2 = np.meshgrid(m[0], m[1], m[2], indexing="ij")
+    G = M0[..., None] * B[0] + M1[..., None] * B[1] + M2[..., None] * B[2]
+    G2 = np.sum(G * G, axis=-1)
     rk = np.fft.fftn(rho_charge)
     with np.errstate(divide="ignore", invalid="ignore"):
         Vk = 4 * np.pi * CoulombConst * rk / G2
     Vk[0, 0, 0] = 0
     return np.real(np.fft.ifftn(Vk))
+
+
+def gaussian_density(n, lvec, atoms):
+    """Sum of normalised 3-D Gaussians on the periodic grid (minimum-image distance):
+    rho(p) = sum_i w_i exp(-|p - R_i|^2 / (2 s_i^2)) / ((2 pi)^1.5 s_i^3), grid point
+    p = (i/n0) a + (j/n1) b + (k/n2) c; atoms rows (x, y, z relative to the origin, s, w).
+    Synthetic-input generator of the density-overlap workload (no reference counterpart:
+    the reference reads densities from files)."""
+    n = tuple(int(x) for x in n)
+    cell = np.asarray(lvec, dtype=np.float64)[1:4]
+    inv = np.linalg.inv(cell)
+    F = np.stack(np.meshgrid(*[np.arange(n[k]) / n[k] for k in range(3)], indexing="ij"), axis=-1)
+    rho = np.zeros(n)
+    for x, y, z, s, w in np.asarray(atoms, dtype=np.float64):
+        g = F - np.array([x, y, z]) @ inv
+        g -= np.rint(g)
+        d = g @ cell
+        rho += w * np.exp(-np.sum(d * d, axis=-1) / (2 * s * s)) / ((2 * np.pi) ** 1.5 * s**3)
+    return rho
 
 
 # -------------------------------------------------- AFMulator point-charge (OpenCL, FP32)

@@ -21,6 +21,7 @@ PPGPU_ERR_NO_DEVICE = 5
 
 FF_LJ, FF_COULOMB, FF_LJC, FF_QZS = 0, 1, 2, 3
 FF_WITH_E, FF_ACCUMULATE, FF_F64 = 1, 2, 4
+FFT_F64 = 1
 ATOM_FLOATS = 12
 RELAX_NPARAM = 15
 AFM_NPARAM = 28
@@ -62,6 +63,13 @@ SIGNATURES = {
     "ppgpu_grid_from_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_void_p], c_int),
     "ppgpu_grid_to_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_int, c_void_p], c_int),
     "ppgpu_ffma_peak": ([c_void_p, c_int, POINTER(c_longlong), c_void_p], c_int),
+    "ppgpu_fft_create": ([_ip, c_int, POINTER(c_void_p)], c_int),
+    "ppgpu_fft_destroy": ([c_void_p], c_int),
+    "ppgpu_fft_potential2forces": ([c_void_p, c_void_p, c_void_p, _dp, c_double, c_int, c_void_p, c_void_p], c_int),
+    "ppgpu_fft_probe_density": ([c_void_p, c_void_p, _dp, c_double, _dp, c_void_p], c_int),
+    "ppgpu_fft_density_power": ([c_void_p, c_void_p, c_double, c_int, c_void_p], c_int),
+    "ppgpu_fft_poisson": ([c_void_p, c_void_p, _dp, c_void_p, c_void_p], c_int),
+    "ppgpu_gaussian_density": ([c_void_p, _ip, _dp, c_int, c_void_p, c_int, c_void_p], c_int),
     "ppgpu_lj_grid_f64_noalloc": ([c_void_p, c_void_p, _ip, _dp, c_int, c_void_p, c_void_p, c_void_p], c_int),
 }
 

@@ -180,3 +180,43 @@ def molecule_batch(seed=0, nmol=256, scale=1.0):
         w.update(_scan((cell[0], cell[1]), (npx, npx), 7.5, 20, 0.1))
         out.append(w)
     return out
+
+
+# Valence electrons and Gaussian widths (A) of the synthetic densities of density_overlap.
+SIGMA_E = {1: 0.5, 6: 0.7, 7: 0.65, 8: 0.6, 9: 0.55, 17: 0.9}
+VALENCE_Z = {1: 1, 6: 4, 7: 5, 8: 6, 9: 7, 17: 7}
+SIGMA_CORE = 0.3
+
+
+def density_overlap(seed=0, scale=1.0):
+    """FFT density-overlap route: a 40-atom planar C/N/O/H molecule as Gaussian densities on a
+    256^3 grid of a 30 A cube; tip = 6 electrons as two Gaussians on z, 1.15 A apart.
+
+    Sample electron density: per atom a normalised Gaussian (sigma 0.5-0.9 A by element)
+    holding (valence - q) electrons, q uniform +-0.3 e neutralised.  Sample charge density
+    (for the Hartree potential): cores of +valence (sigma 0.3 A) minus the electron density,
+    net charge 0.  Pauli: A = 12 eV A^3, B = 1.  Electrostatics: the Hartree potential
+    correlated with the tip density normalised to one charge, times the probe charge Q.
+    Scan: 160x160 pixels over the central 20x20 A, 30 z steps of 0.1 A."""
+    rng = np.random.default_rng(seed)
+    L = 30.0
+    Zs, R = _planar_molecule(rng, dict(C=22, N=4, O=4, H=10), 14.0, (L / 2, L / 2), 0.0, jitter=0.1, lattice=True)
+    Qs = _neutralize(rng.uniform(-0.3, 0.3, size=len(Zs)))
+    origin = np.array([0.0, 0.0, -L / 2])
+    rel = R - origin
+    val = np.array([VALENCE_Z[int(z)] for z in Zs], dtype=np.float64)
+    sig = np.array([SIGMA_E[int(z)] for z in Zs])
+    rho_e_atoms = np.column_stack([rel, sig, val - Qs])
+    core_atoms = np.column_stack([rel, np.full(len(Zs), SIGMA_CORE), val])
+    tip_atoms = np.array([[0.0, 0.0, 0.575, 0.7, 3.0], [0.0, 0.0, -0.575, 0.7, 3.0]])
+    ng = max(16, int(round(256 * scale)))
+    npx = max(4, int(round(160 * scale)))
+    w = dict(name="density_overlap", seed=seed, Zs=Zs, Rs=R, Qs=Qs, lvec=np.array([origin, [L, 0, 0], [0, L, 0], [0, 0, L]]), gridN=(ng, ng, ng), rho_e_atoms=rho_e_atoms, core_atoms=core_atoms, tip_atoms=tip_atoms, tip_electrons=6.0, Apauli=12.0, Bpauli=1.0)
+    w.update(PROBE)
+    w.update(FIRE)
+    w.update(DF)
+    scan = _scan((20.0, 20.0), (npx, npx), 7.0, 30, 0.1)
+    scan["scanMin"] = (5.0, 5.0, scan["scanMin"][2])
+    scan["scanMax"] = (5.0 + scan["scanMax"][0], 5.0 + scan["scanMax"][1], scan["scanMax"][2])
+    w.update(scan)
+    return w

@@ -183,3 +183,28 @@ def test_oracle_vs_compiled_reference(oracle):
         L.relaxTipStrokes_omp(3, 4, ps, alg, 7, rT, rs, fs, None)
         rs2, fs2, _, _ = oracle.relax_strokes(n, cell, FF, prm, rT, probeStart=ps, relaxAlg=alg)
         assert np.array_equal(rs, rs2) and np.array_equal(fs, fs2), (maxit, dt, alg, ps)
+
+
+def test_poisson_plane_wave_skewed_cell(oracle):
+    """rho = cos(G.r), G a reciprocal-lattice vector of a skewed cell: V = 4 pi k cos(G.r)/|G|^2."""
+    dims = (12, 10, 9)
+    cell = np.array([[7.0, 0, 0], [1.5, 6.0, 0], [0.3, 0.4, 5.5]])
+    lv = np.vstack([np.zeros(3), cell])
+    Bm = 2 * np.pi * np.linalg.inv(cell).T
+    for m in ((1, 0, 0), (2, -1, 3), (0, 4, -2)):
+        Gv = m[0] * Bm[0] + m[1] * Bm[1] + m[2] * Bm[2]
+        f = np.stack(np.meshgrid(*[np.arange(dims[k]) / dims[k] for k in range(3)], indexing="ij"), axis=-1)
+        rho = np.cos((f @ cell) @ Gv)
+        V = oracle.poisson_hartree(rho, lv)
+        assert np.allclose(V, 4 * np.pi * oracle.CoulombConst * rho / (Gv @ Gv), atol=1e-12 * np.abs(V).max())
+
+
+def test_gaussian_density_kat(oracle):
+    """A normalised Gaussian on a grid node: peak w/((2 pi)^1.5 s^3), integral w, periodic wrap."""
+    L, n, s, w = 10.0, 50, 0.7, 3.0
+    lv = np.array([[0.0, 0, 0], [L, 0, 0], [0, L, 0], [0, 0, L]])
+    rho = oracle.gaussian_density((n, n, n), lv, [[0.0, 0.0, 0.2 * 9, s, w]])
+    k = 9  # z index of the atom
+    assert np.isclose(rho[0, 0, k], w / ((2 * np.pi) ** 1.5 * s**3), rtol=1e-12)
+    assert np.isclose(rho.sum() * (L / n) ** 3, w, rtol=1e-6)
+    assert np.isclose(rho[1, 0, k], rho[-1, 0, k], rtol=1e-12)  # minimum image across x = 0
