@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule"])
+    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0)
@@ -112,9 +112,9 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": float(max(smax)) if smax else None, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def read_profile_traffic(workload):
-    """DRAM bytes per force-field launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", f"ff_kernel_{workload}.txt")
+def read_profile_traffic(kernel, workload):
+    """DRAM bytes per launch of a kernel from its committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -124,6 +124,15 @@ def read_profile_traffic(workload):
             except ValueError:
                 return None
     return None
+
+
+def read_measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def ffma_peak_tflops(torch, lib, check, tptr, stream_handle):
@@ -149,6 +158,77 @@ def ffma_peak_tflops(torch, lib, check, tptr, stream_handle):
     return best
 
 
+class PointChargeJob:
+    """LJ + point-charge force field (one fused kernel), relaxed scan + Δf."""
+
+    def __init__(self, w, relax, HL, torch):
+        self.w = w
+        self.torch = torch
+        self.HL = HL
+        self.pl = HL.Pipeline(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w["gridN"], w, relax=relax, want_iters=False)
+        self.npts = int(np.prod(self.pl.gridN))
+        self.natoms = self.pl.natoms
+        self.nch = self.pl.ncharged
+        self.ff_name = "ff_kernel<LJC> (force field)" if self.pl.Q != 0.0 else "ff_kernel<LJ> (force field)"
+        self.launches_per_step = 2
+        self.rec_pinned = torch.empty(self.pl.atoms.shape, dtype=self.pl.atoms.dtype, pin_memory=True)
+        self.host_in = {k: np.asarray(w[k]).copy() for k in ("Zs", "Rs", "Qs")}
+
+    def e2e_inputs(self):
+        """Host prep (PBC images, LJ mixing, packing) + H2D of the atom records; bytes copied."""
+        from ppafm_gb300.device import pack_atoms
+
+        pl = self.pl
+        Rs0, cLJs, kqq = self.HL.prepare_atoms(self.host_in["Zs"], self.host_in["Rs"], self.host_in["Qs"], pl.lvec, self.w)
+        rec, _, _ = pack_atoms(Rs0, cLJs, kqq if pl.Q != 0.0 else None, device="cpu")
+        self.rec_pinned.copy_(rec)
+        pl.atoms.copy_(self.rec_pinned, non_blocking=True)
+        return int(self.rec_pinned.numel() * self.rec_pinned.element_size())
+
+    def ff_roofline(self, t_ff, peak_fp32):
+        if self.pl.Q != 0.0:
+            flops = self.npts * ((self.natoms - self.nch) * FLOPS_LJ_PAIR + self.nch * FLOPS_LJC_PAIR)
+        else:
+            flops = self.npts * self.natoms * FLOPS_LJ_PAIR
+        achieved = flops / t_ff / 1e12
+        return {"bound": "fp32", "kernel": self.ff_name, "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None, "peak_source": "FFMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP32 figure)", "flops_per_launch": flops}
+
+    def config(self):
+        return {"atoms": len(self.w["Zs"]), "atoms_with_images": self.natoms, "charged_atoms_with_images": self.nch}
+
+    def extra(self, t_ff):
+        return {"ff_grid_pt_atoms_per_s": self.npts * self.natoms / t_ff}
+
+
+class OverlapJob:
+    """FFT density-overlap route: Pauli + Hartree force field (cuFFT + fused k-space
+    kernels), relaxed scan + Δf.  Inputs of a step: the three density grids."""
+
+    def __init__(self, w, relax, HL, torch):
+        self.w = w
+        self.torch = torch
+        self.pl = HL.DensityOverlapPipeline.from_workload(w, relax=relax, want_iters=False)
+        self.npts = int(np.prod(self.pl.gridN))
+        self.launches_per_step = 13  # 2 copies, 2 x (sums + power), 2 x (2 R2C, spectra, C2R x4, pack), R2C + poisson + C2R, relax (cuFFT launches counted as one each)
+        self.host = [torch.empty(self.pl.gridN, dtype=torch.float32, pin_memory=True) for _ in range(3)]
+        for h, d in zip(self.host, (self.pl.rho_s, self.pl.rho_q, self.pl.rho_t)):
+            h.copy_(d)
+
+    def e2e_inputs(self):
+        for h, d in zip(self.host, (self.pl.rho_s, self.pl.rho_q, self.pl.rho_t)):
+            d.copy_(h, non_blocking=True)
+        return int(sum(h.numel() * h.element_size() for h in self.host))
+
+    def ff_roofline(self, t_ff, peak_fp32):
+        return None
+
+    def config(self):
+        return {"atoms": len(self.w["Zs"]), "fft": "float32 complex (cuFFT R2C/C2R)", "A_pauli": self.w["Apauli"], "B_pauli": self.w["Bpauli"]}
+
+    def extra(self, t_ff):
+        return {}
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -163,12 +243,11 @@ def run_ours(args, rank, world, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w = make_workload(args.workload, args.seed + rank, args.scale)
     relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
-    pl = HL.Pipeline(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w["gridN"], w, relax=relax, want_iters=False)
+    job = (OverlapJob if args.workload == "density_overlap" else PointChargeJob)(w, relax, HL, torch)
+    pl = job.pl
     nx, ny, nz = pl.scan_shape
     units = nx * ny * nz
-    npts = int(np.prod(pl.gridN))
-    natoms = pl.natoms
-    nch = pl.ncharged
+    npts = job.npts
     st = torch.cuda.current_stream()
 
     def barrier():
@@ -203,20 +282,11 @@ def run_ours(args, rank, world, local):
     _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
 
     # ---------------- end to end through the host API
-    import ctypes  # noqa: F401
-
-    host_in = {k: np.asarray(w[k]).copy() for k in ("Zs", "Rs", "Qs")}
     pin_out = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in pl.out.items()}
-    rec_pinned = torch.empty(pl.atoms.shape, dtype=pl.atoms.dtype, pin_memory=True)
+    h2d = [0]
 
     def e2e_step():
-        # host prep (PBC images, LJ mixing, packing) + H2D of the atom records
-        Rs0, cLJs, kqq = HL.prepare_atoms(host_in["Zs"], host_in["Rs"], host_in["Qs"], pl.lvec, w)
-        from ppafm_gb300.device import pack_atoms
-
-        rec, _, _ = pack_atoms(Rs0, cLJs, kqq if pl.Q != 0.0 else None, device="cpu")
-        rec_pinned.copy_(rec)
-        pl.atoms.copy_(rec_pinned, non_blocking=True)
+        h2d[0] = job.e2e_inputs()
         pl.run()
         for k, v in pl.out.items():
             pin_out[k].copy_(v, non_blocking=True)
@@ -235,7 +305,6 @@ def run_ours(args, rank, world, local):
     b.synchronize()
     barrier()
     t_e2e = a.elapsed_time(b) * 1e-3
-    h2d = int(rec_pinned.numel() * rec_pinned.element_size())
     d2h = int(sum(v.numel() * v.element_size() for v in pin_out.values()))
 
     # ---------------- max over ranks
@@ -255,15 +324,23 @@ def run_ours(args, rank, world, local):
             torch.distributed.destroy_process_group()
         return None
 
-    # ---------------- roofline (force-field kernel, float32 FMA bound)
-    peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
+    # ---------------- roofline of the dominant kernel
     t_ff_avg = float(np.mean(t_ff))
-    if pl.Q != 0.0:
-        flops = npts * ((natoms - nch) * FLOPS_LJ_PAIR + nch * FLOPS_LJC_PAIR)
+    t_rx_avg = float(np.mean(t_rx))
+    if t_ff_avg >= t_rx_avg and job.ff_roofline(t_ff_avg, 1.0) is not None:
+        peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
+        roof = job.ff_roofline(t_ff_avg, peak)
+        roof["traffic"] = read_profile_traffic("ff_kernel", args.workload)
     else:
-        flops = npts * natoms * FLOPS_LJ_PAIR
-    achieved = flops / t_ff_avg / 1e12
-    traffic = read_profile_traffic(args.workload)
+        # relaxation: gathers of 8 float4 corners per FIRE iteration + 32 B out per pixel-z
+        peaks = read_measured_peaks()
+        hbm = peaks.get("hbm_gbs")
+        moved = 128.0 * iters_total / K + 32.0 * units
+        achieved = moved / t_rx_avg / 1e9
+        roof = {"bound": "hbm", "kernel": "relax_kernel<scan> (FIRE + fused df)", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else "fallback 6800 GB/s", "bytes_per_launch": moved, "traffic": read_profile_traffic("relax_kernel", args.workload)}
+        if not hbm:
+            roof["peak"] = 6800.0
+            roof["frac"] = achieved / 6800.0
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -271,10 +348,25 @@ def run_ours(args, rank, world, local):
             from oracle import cpu_baseline
 
             s = cpu_baseline.sample_pipeline(w, budget_s=args.cpu_budget)
-            cpu = {"value": s["pixel_z_per_s"], "unit": UNIT, "cores": s["cores"], "kind": s["kind"], "sample": s["sample"], "ff_grid_pt_atoms_per_s": s["ff_pairs_per_s"], "seconds_full_job": s["seconds_full_job"]}
+            cpu = {"value": s["pixel_z_per_s"], "unit": UNIT, "cores": s["cores"], "kind": s["kind"], "sample": s["sample"], "seconds_full_job": s["seconds_full_job"]}
+            if "ff_pairs_per_s" in s:
+                cpu["ff_grid_pt_atoms_per_s"] = s["ff_pairs_per_s"]
         except Exception as e:  # the baseline is reported, never fatal
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
 
+    config = {"workload": args.workload}
+    config.update(job.config())
+    config.update(
+        {
+            "grid": list(pl.gridN),
+            "scan": [nx, ny, nz],
+            "fire": relax,
+            "probe": {"klat": w["klat"], "krad": w["krad"], "r0": list(w["r0Probe"]), "Q": w["charge"]},
+            "df": {"f0": w["f0Cantilever"], "k": w["kCantilever"], "A": w["Amplitude"]},
+            "l2": ("inputs larger than L2 (force field %.2f GB)" if npts * 16 > 129e6 else "force field %.2f GB fits in L2; no flush between steps") % (npts * 16 / 1e9),
+            "parallelism": f"replicas x{world}",
+        }
+    )
     line = {
         "metric": METRIC,
         "value": value,
@@ -288,39 +380,21 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {
-            "workload": args.workload,
-            "atoms": len(w["Zs"]),
-            "atoms_with_images": natoms,
-            "charged_atoms_with_images": nch,
-            "grid": list(pl.gridN),
-            "scan": [nx, ny, nz],
-            "fire": relax,
-            "probe": {"klat": w["klat"], "krad": w["krad"], "r0": list(w["r0Probe"]), "Q": w["charge"]},
-            "df": {"f0": w["f0Cantilever"], "k": w["kCantilever"], "A": w["Amplitude"]},
-            "l2": "inputs larger than L2 (force field %.2f GB)" % (npts * 16 / 1e9),
-            "parallelism": f"replicas x{world}",
-        },
-        "ff_grid_pt_atoms_per_s": npts * natoms / t_ff_avg,
-        "fire_iters_per_pixel_z": iters_total / (units * K),
-        "stage_ms": {"force_field": 1e3 * t_ff_avg, "relax_and_df": 1e3 * float(np.mean(t_rx))},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 2 * K,
-        "roofline": {
-            "bound": "fp32",
-            "kernel": "ff_kernel<LJC> (force field)",
-            "achieved": achieved,
-            "peak": peak,
-            "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None,
-            "peak_source": "FFMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP32 figure)",
-            "flops_per_launch": flops,
-            "traffic": traffic,
-        },
-        "cpu_baseline": cpu,
-        "clocks": clk,
-        "wall_s": wall,
+        "config": config,
     }
+    line.update(job.extra(t_ff_avg))
+    line.update(
+        {
+            "fire_iters_per_pixel_z": iters_total / (units * K),
+            "stage_ms": {"force_field": 1e3 * t_ff_avg, "relax_and_df": 1e3 * t_rx_avg},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d[0], "d2h_bytes_per_step": d2h},
+            "gpu_launches": job.launches_per_step * K,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "wall_s": wall,
+        }
+    )
     if world > 1:
         torch.distributed.destroy_process_group()
     return line

@@ -15,6 +15,11 @@ Sample, chosen so one call takes roughly ``budget_s`` seconds:
     the strokes are relaxed with the reference's FIRE;
   * Fz -> Δf: numpy convolution on the sampled columns.
 Each stage's time per unit (grid point, pixel-height) is scaled to the full workload.
+
+The density-overlap workload (FFT route) is timed by ``sample_overlap``: the whole force
+field at full size with the reference's numpy algorithm (negative-density fix and power,
+potential2forces_mem for Pauli and for the Hartree potential, the Poisson solve), then the
+relaxation on pixel blocks of that force field as above.
 """
 
 import ctypes
@@ -61,9 +66,102 @@ def _ff_slab(ref, n, cell, R, coefs, kind, iz0, nzs, nthreads):
     return F
 
 
+def _relax_blocks(ref, w, n, cell, FF, xT, yT, zT, nthreads, seed, nb=4):
+    """Relaxes two nb x nb pixel blocks on a full float64 force field; (seconds, relaxed
+    pixel-heights, Fz columns)."""
+    lv = np.asarray(w["lvec"], np.float64)
+    Z = len(zT)
+    rng = np.random.default_rng(seed)
+    blocks = [(len(xT) // 2 - nb // 2, len(yT) // 2 - nb // 2), (int(rng.integers(0, len(xT) - nb)), int(rng.integers(0, len(yT) - nb)))]
+    r0 = w["r0Probe"]
+    stiff = [w["klat"], w["klat"], w["krad"]]
+    tip = O.tip_params(r0[2], stiff[2] / -O.eVA_Nm, [r0[0], r0[1], 0.0], np.array([stiff[0], stiff[1], 0.0]) / -O.eVA_Nm)
+    prm = O.relax_param_vector(tip, maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    t_relax, nrel, cols = 0.0, 0, []
+    for bx, by in blocks:
+        rT = np.zeros((nb, nb, Z, 3))
+        rT[..., 0] = (xT[bx : bx + nb] - lv[0, 0])[:, None, None]
+        rT[..., 1] = (yT[by : by + nb] - lv[0, 1])[None, :, None]
+        rT[..., 2] = (zT[::-1] - lv[0, 2])[None, None, :]
+        t0 = time.perf_counter()
+        if ref is not None:
+            L = ref.L
+            ref.set_grid(n, cell)
+            L.setFF_Fpointer(FF)
+            L.setRelax(int(w["maxIters"]), float(w["convF2"]), float(w["dt"]), float(w["damping"]))
+            L.setFIRE(1.1, 0.5, 0.99)
+            L.setTip(float(r0[2]), stiff[2] / -O.eVA_Nm, np.array([r0[0], r0[1], 0.0]), np.array([stiff[0], stiff[1], 0.0]) / -O.eVA_Nm)
+            rs = np.zeros_like(rT)
+            fs = np.zeros_like(rT)
+            L.relaxTipStrokes_omp(nb, nb, 1, 1, Z, rT, rs, fs, None)
+        else:
+            rs, fs, _, _ = O.relax_strokes(n, cell, FF, prm, rT, nthreads=nthreads)
+        t_relax += time.perf_counter() - t0
+        nrel += nb * nb * Z
+        cols.append(fs[:, :, ::-1, 2].reshape(-1, Z))
+    return t_relax, nrel, np.concatenate(cols), len(blocks)
+
+
+def sample_overlap(w, budget_s=20.0, nthreads=0, use_reference=True, seed=0):
+    """Density-overlap (FFT) route: full-size force field with the reference's numpy
+    algorithm, relaxation sampled on pixel blocks.  Same return keys as sample_pipeline."""
+    ref = _ref_lib() if use_reference else None
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(nthreads)
+    n = np.array(w["gridN"], np.int32)
+    lv = np.asarray(w["lvec"], np.float64)
+    cell = lv[1:4]
+    dims = tuple(int(x) for x in n)
+    # inputs (not timed): float32 densities like the device path
+    rho_s = O.gaussian_density(dims, lv, w["rho_e_atoms"]).astype(np.float32).astype(np.float64)
+    neg = np.array(w["rho_e_atoms"])
+    neg[:, 4] *= -1
+    rho_q = (O.gaussian_density(dims, lv, w["core_atoms"]) + O.gaussian_density(dims, lv, neg)).astype(np.float32).astype(np.float64)
+    rho_t = O.gaussian_density(dims, lv, w["tip_atoms"]).astype(np.float32).astype(np.float64)
+    t0 = time.perf_counter()
+    ws = O.handle_negative_density(rho_s.copy()) ** w["Bpauli"]
+    wt = O.handle_negative_density(rho_t.copy()) ** w["Bpauli"]
+    t_pow = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fx, fy, fz, _ = O.potential2forces_mem(ws, lv, dims, rho=wt, doPot=True)
+    FF = w["Apauli"] * np.stack([fx, fy, fz], axis=-1)
+    t_pauli = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    V = O.poisson_hartree(rho_q, lv)
+    t_poisson = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fx, fy, fz, _ = O.potential2forces_mem(V, lv, dims, rho=rho_t, doPot=True)
+    FF += (w["charge"] / w["tip_electrons"]) * np.stack([fx, fy, fz], axis=-1)
+    t_el = time.perf_counter() - t0
+    del fx, fy, fz, V, ws, wt
+    FF = np.ascontiguousarray(FF)
+    from ppafm_gb300 import common as C
+
+    xT, yT, zT, _ = C.prepareScanGrids(w["scanMin"], w["scanMax"], w["scanStep"], w["r0Probe"])
+    P = len(xT) * len(yT)
+    Z = len(zT)
+    t_relax, nrel, fz_cols, nblocks = _relax_blocks(ref, w, n, cell, FF, xT, yT, zT, nthreads, seed)
+    t0 = time.perf_counter()
+    O.Fz2df_numpy(fz_cols[:, None, :], w["scanStep"][2], w["kCantilever"], w["f0Cantilever"], w["Amplitude"])
+    t_df = time.perf_counter() - t0
+    full = dict(density_power=t_pow, ff_pauli_fft=t_pauli, poisson_fft=t_poisson, ff_hartree_fft=t_el, relax=t_relax * (P * Z) / nrel, df=t_df * P / len(fz_cols))
+    total = sum(full.values())
+    return dict(
+        kind="port",
+        cores=nthreads,
+        seconds_full_job=full,
+        total_s=total,
+        pixel_z_per_s=P * Z / total,
+        sample=f"force field: full {dims[0]}x{dims[1]}x{dims[2]} grid with numpy float64 FFTs (single-threaded like the reference's numpy); relax: {nblocks} blocks of 4x4 pixels x {Z} heights with the {'reference' if ref is not None else 'restated'} FIRE on {nthreads} threads; extrapolated per pixel-height",
+    )
+
+
 def sample_pipeline(w, budget_s=20.0, nthreads=0, use_reference=True, seed=0):
     """Returns a dict with per-stage seconds for the full job, pixel-z/s, pair rate,
     cores, kind and a description of the sample."""
+    if w.get("name") == "density_overlap":
+        return sample_overlap(w, budget_s, nthreads, use_reference, seed)
     ref = _ref_lib() if use_reference else None
     kind = "reference" if ref is not None else "port"
     if nthreads <= 0:

@@ -1,0 +1,78 @@
+// pp_df.cuh -- double-float (float32 pair) arithmetic for the relaxation kernel.
+//
+// GB300 issues float64 at 1/64 of its float32 rate, so float64-accurate quantities of the
+// FIRE loop (probe position, grid coordinate, trilinear interpolation, springs, force sum)
+// are carried as unevaluated sums hi + lo of two floats (about 48 significant bits) built
+// from the error-free transformations of Knuth (TwoSum), Dekker (FastTwoSum) and the
+// FMA-based TwoProduct (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26 (2005)).  Every operation uses the explicitly rounded intrinsics so that the
+// compiler can neither contract nor reorder them.
+#pragma once
+
+namespace ppgpu {
+
+struct dfl {
+    float h, l;
+};
+
+__device__ __forceinline__ dfl two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ dfl fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dfl two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const dfl s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+
+// a + b without the final renormalisation (lo may exceed half an ulp of hi; the value is exact
+// to the same order).  Used inside reductions that renormalise once at the end.
+__device__ __forceinline__ dfl df_add_raw(dfl a, dfl b) {
+    const dfl s = two_sum(a.h, b.h);
+    return {s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l))};
+}
+
+__device__ __forceinline__ dfl df_add_f(dfl a, float b) {
+    const dfl s = two_sum(a.h, b);
+    return fast_two_sum(s.h, __fadd_rn(s.l, a.l));
+}
+
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const dfl p = two_prod(a.h, b.h);
+    const float e = __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.l, p.l));
+    return fast_two_sum(p.h, e);
+}
+
+__device__ __forceinline__ dfl df_mul_f(dfl a, float b) {
+    const dfl p = two_prod(a.h, b);
+    return fast_two_sum(p.h, __fmaf_rn(a.l, b, p.l));
+}
+
+__device__ __forceinline__ dfl df_sq(dfl a) {
+    const dfl p = two_prod(a.h, a.h);
+    return fast_two_sum(p.h, __fmaf_rn(__fadd_rn(a.h, a.h), a.l, p.l));
+}
+
+__host__ __device__ __forceinline__ dfl df_from(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+__device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
+
+__device__ __forceinline__ float df_round(dfl a) { return __fadd_rn(a.h, a.l); }
+
+}  // namespace ppgpu

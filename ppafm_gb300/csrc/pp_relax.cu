@@ -15,19 +15,23 @@
 //    the interleaved float4 grid), so lanes that converge early at one height move on
 //    to their next height instead of idling; the warp leaves the loop on a
 //    __any_sync vote once all of its lanes have finished their strokes.
-//  * Mixed precision, chosen by measurement against the float64 reference: the grid
-//    values and the FIRE mixing coefficient acoef*sqrt(vv/ff) are float32; the FIRE state
-//    (d = r - r_tip, v, dt, acoef), the grid coordinate, the trilinear weights and sum,
-//    the force sum and the radial-spring factor k (l - l0)/l are float64.  With a float32
-//    state, rounding moves the stopping point of ~1.5 % of pixel heights by more than
-//    1e-3 A inside the |F| < 1e-4 eV/A ball (the soft lateral spring leaves it ~6e-3 A
-//    wide); with this split the only difference from the reference is the float32
-//    rounding of the grid values.
+//  * Precision, chosen by measurement against the float64 reference on a GB300, whose
+//    float64 rate is 1/64 of its float32 rate: the probe displacement d = r - r_tip, the grid
+//    coordinate, the trilinear weights and interpolation sum, the springs and the force sum
+//    are double-float (pp_df.cuh: two floats, ~48 significant bits); the FIRE state
+//    (velocity, dt, mixing coefficient) and the residual force it consumes are float32.
+//    Rounding noise in the interpolated force of ~3e-8 relative (plain float32) moves the
+//    stopping point of a few pixel heights in 1e5 by more than 1e-3 A inside the
+//    |F| < 1e-4 eV/A ball (the soft lateral spring leaves it ~6e-3 A wide); 1e-9 relative
+//    noise moves none, and neither does a float32 FIRE state.  The only difference from the
+//    reference left is the float32 storage of the grid values.  Float64 is used once per
+//    height (tip grid coordinate), not per iteration.
 //  * Trilinear weights are explicit (no texture filtering).
 #include <cmath>
 #include <cstring>
 
 #include "pp_common.cuh"
+#include "pp_df.cuh"
 
 namespace ppgpu {
 
@@ -46,6 +50,12 @@ struct RelaxPrm {
     int relaxAlg, probeStart;
     unsigned long long *iter_total;
     int *err;
+    // per-iteration constants
+    dfl dic[9];  // dicd as double-floats
+    int diag;    // dicd is diagonal
+    dfl kRadf, nl0;        // kRad, -lRad
+    dfl nr0[3], kSf[3];    // -rPP0, kSpring
+    float convF2f, dtmaxf, acoef0f, fincf, fdecf, falphaf;
 };
 
 struct StrokeIO {  // relaxTipStrokes semantics (float64 in/out)
@@ -67,33 +77,57 @@ struct ScanIO {  // regular scan semantics
 
 // ----------------------------------------------------------- interpolation
 
-// Periodic trilinear interpolation of the force (Grid.h:93-111) at the float64 grid
-// coordinate g: float32 grid values, float64 weights and accumulation.
-__device__ __forceinline__ double3 interp_force(const float4 *__restrict__ FE, int n0, int n1, int n2, double3 g) {
-    const double fx = floor(g.x), fy = floor(g.y), fz = floor(g.z);
-    const double tx = g.x - fx, ty = g.y - fy, tz = g.z - fz;
-    const double mx = 1.0 - tx, my = 1.0 - ty, mz = 1.0 - tz;
-    const int ix0 = wrap_index((int)fx, n0), iy0 = wrap_index((int)fy, n1), iz0 = wrap_index((int)fz, n2);
+// Periodic trilinear interpolation of the force (Grid.h:93-111) at the grid coordinate
+// base + u (base integer, u double-float): float32 grid values, double-float weights and
+// compensated sums, so the only rounding left is that of the stored grid values.
+__device__ __forceinline__ void interp_force_df(const float4 *__restrict__ FE, int n0, int n1, int n2,
+                                                const int base[3], const dfl u[3], dfl F[3]) {
+    int ci[3];
+    dfl t[3], m[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float fl = floorf(u[k].h);
+        float th = __fsub_rn(u[k].h, fl);  // exact: the fraction bits of u.h
+        const float tl = u[k].l;
+        if (th == 0.f && tl < 0.f) {  // just below the cell boundary
+            th = 1.f;
+            fl = __fsub_rn(fl, 1.f);
+        }
+        ci[k] = base[k] + (int)fl;
+        t[k] = {th, tl};
+        const dfl o = two_sum(1.f, -th);
+        m[k] = {o.h, __fsub_rn(o.l, tl)};
+    }
+    const int ix0 = wrap_index(ci[0], n0), iy0 = wrap_index(ci[1], n1), iz0 = wrap_index(ci[2], n2);
     const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
     const int iy1 = (iy0 + 1 == n1) ? 0 : iy0 + 1;
     const int iz1 = (iz0 + 1 == n2) ? 0 : iz0 + 1;
     const long long r00 = ((long long)ix0 * n1 + iy0) * n2, r01 = ((long long)ix0 * n1 + iy1) * n2;
     const long long r10 = ((long long)ix1 * n1 + iy0) * n2, r11 = ((long long)ix1 * n1 + iy1) * n2;
-    const float4 c000 = ldg4(FE + r00 + iz0), c001 = ldg4(FE + r00 + iz1);
-    const float4 c010 = ldg4(FE + r01 + iz0), c011 = ldg4(FE + r01 + iz1);
-    const float4 c110 = ldg4(FE + r11 + iz0), c111 = ldg4(FE + r11 + iz1);
-    const float4 c100 = ldg4(FE + r10 + iz0), c101 = ldg4(FE + r10 + iz1);
-    const double mxmy = mx * my, mxty = mx * ty, txmy = tx * my, txty = tx * ty;
-    const double w[8] = {mxmy * mz, mxmy * tz, mxty * mz, mxty * tz, txty * mz, txty * tz, txmy * mz, txmy * tz};
-    const float4 c[8] = {c000, c001, c010, c011, c110, c111, c100, c101};
-    double3 o = make_double3(0.0, 0.0, 0.0);
+    // corner order (x, y, z bits): 000 001 010 011 100 101 110 111
+    const float4 c[8] = {ldg4(FE + r00 + iz0), ldg4(FE + r00 + iz1), ldg4(FE + r01 + iz0), ldg4(FE + r01 + iz1),
+                         ldg4(FE + r10 + iz0), ldg4(FE + r10 + iz1), ldg4(FE + r11 + iz0), ldg4(FE + r11 + iz1)};
+    const dfl wxy[4] = {df_mul(m[0], m[1]), df_mul(m[0], t[1]), df_mul(t[0], m[1]), df_mul(t[0], t[1])};
+    dfl w[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        o.x = fma((double)c[k].x, w[k], o.x);
-        o.y = fma((double)c[k].y, w[k], o.y);
-        o.z = fma((double)c[k].z, w[k], o.z);
+    for (int k = 0; k < 4; k++) {
+        w[2 * k] = df_mul(wxy[k], m[2]);
+        w[2 * k + 1] = df_mul(wxy[k], t[2]);
     }
-    return o;
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++) {
+        dfl p[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const float v = comp == 0 ? c[k].x : (comp == 1 ? c[k].y : c[k].z);
+            p[k] = two_prod(w[k].h, v);
+            p[k].l = __fmaf_rn(w[k].l, v, p[k].l);
+        }
+        const dfl a0 = df_add_raw(p[0], p[1]), a1 = df_add_raw(p[2], p[3]);
+        const dfl a2 = df_add_raw(p[4], p[5]), a3 = df_add_raw(p[6], p[7]);
+        const dfl r = df_add_raw(df_add_raw(a0, a1), df_add_raw(a2, a3));
+        F[comp] = two_sum(r.h, r.l);
+    }
 }
 
 // Same, all four channels, at a float grid coordinate (AFMulator path).
@@ -131,57 +165,86 @@ __device__ __forceinline__ double3 to_grid(const RelaxPrm &P, double x, double y
                         fma(z, P.dicd[8], fma(y, P.dicd[7], x * P.dicd[6])));
 }
 
+// Grid coordinate of the displacement d relative to tf (double-float): u_k = tf_k + dic_k . d.
+__device__ __forceinline__ void grid_coord_df(const RelaxPrm &P, const dfl tf[3], const dfl d[3], dfl u[3]) {
+    if (P.diag) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) u[k] = df_add(tf[k], df_mul(P.dic[4 * k], d[k]));
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const dfl a = df_add_raw(df_mul(P.dic[3 * k], d[0]), df_mul(P.dic[3 * k + 1], d[1]));
+            u[k] = df_add(tf[k], df_add(a, df_mul(P.dic[3 * k + 2], d[2])));
+        }
+    }
+}
+
 // Probe-particle force = grid force + radial spring + lateral spring (getPPforce,
-// ProbeParticle.cpp:282-294; forceRSpring, Forces.h:85-89), in float64: the radial spring
-// is stiff, so l - l0 is a small difference of ~4 A lengths.
-__device__ __forceinline__ double3 pp_force(const RelaxPrm &P, double3 F, double3 d) {
-    const double l = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
-    const double s = P.kRad * (l - P.lRad) / l;
-    double3 f;
-    f.x = fma(d.x - P.rPP0[0], P.kSpring[0], fma(d.x, s, F.x));
-    f.y = fma(d.y - P.rPP0[1], P.kSpring[1], fma(d.y, s, F.y));
-    f.z = fma(d.z - P.rPP0[2], P.kSpring[2], fma(d.z, s, F.z));
-    return f;
+// ProbeParticle.cpp:282-294; forceRSpring, Forces.h:85-89) in double-float, returned as the
+// float32 residual: the radial spring is stiff, so l - l0 is a small difference of ~4 A
+// lengths, and the force is a small difference of the grid force and the springs.
+__device__ __forceinline__ float3 pp_force_df(const RelaxPrm &P, const dfl F[3], const dfl d[3]) {
+    const dfl l2 = df_add(df_add(df_sq(d[0]), df_sq(d[1])), df_sq(d[2]));
+    // l = sqrt(l2): float32 root, one Newton correction from the exact residual
+    const float L = __fsqrt_rn(l2.h);
+    const dfl LL = two_prod(L, L);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(l2.h, LL.h), LL.l), l2.l);
+    const dfl l = fast_two_sum(L, __fmul_rn(res, __fdiv_rn(0.5f, L)));
+    const dfl x = df_add(l, P.nl0);  // l - l0
+    // q = (l - l0) / l: float32 quotient plus the correction from its exact remainder
+    const float qh = __fdiv_rn(x.h, l.h);
+    const dfl ql = two_prod(qh, l.h);
+    const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(x.h, ql.h), ql.l), x.l), __fmul_rn(qh, l.l));
+    const dfl s = df_mul(P.kRadf, fast_two_sum(qh, __fdiv_rn(rem, l.h)));
+    float f[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        dfl fk = df_add(F[k], df_mul(d[k], s));
+        fk = df_add(fk, df_mul(df_add(d[k], P.nr0[k]), P.kSf[k]));
+        f[k] = df_round(fk);
+    }
+    return make_float3(f[0], f[1], f[2]);
 }
 
 // One FIRE move (FIREstate::move, ProbeParticle.cpp:153-172; relaxAlg 1) or damped
-// leap-frog (RELAX::move, ProbeParticle.cpp:84-88; relaxAlg 0).  The state is float64;
-// the FIRE mixing coefficient acoef*sqrt(vv/ff) is formed in float32.  Returns |f|^2.
-__device__ __forceinline__ double relax_move(const RelaxPrm &P, double3 f, double3 &d, double3 &v, double &dt,
-                                             double &acoef) {
-    const double ff = f.x * f.x + f.y * f.y + f.z * f.z;
-    double h;
+// leap-frog (RELAX::move, ProbeParticle.cpp:84-88; relaxAlg 0): float32 velocity, dt and
+// mixing coefficient; the displacement d += v dt is accumulated in double-float.
+// Returns |f|^2.
+__device__ __forceinline__ float relax_move_df(const RelaxPrm &P, float3 f, dfl d[3], float3 &v, float &dt,
+                                               float &acoef) {
+    const float ff = f.x * f.x + f.y * f.y + f.z * f.z;
+    float h;
     if (P.relaxAlg == 1) {
-        const double vv = v.x * v.x + v.y * v.y + v.z * v.z;
-        const double vf = f.x * v.x + f.y * v.y + f.z * v.z;
-        if (vf < 0.0) {
-            v = make_double3(0.0, 0.0, 0.0);
-            dt = dt * P.fdec;
-            acoef = P.acoef0;
+        const float vv = v.x * v.x + v.y * v.y + v.z * v.z;
+        const float vf = f.x * v.x + f.y * v.y + f.z * v.z;
+        if (vf < 0.f) {
+            v = make_float3(0.f, 0.f, 0.f);
+            dt = dt * P.fdecf;
+            acoef = P.acoef0f;
         } else {
             // ff == 0 gives cf = 0 (the reference would divide by zero)
-            const double cf = (ff > 0.0) ? (double)((float)acoef * sqrtf((float)vv / (float)ff)) : 0.0;
-            const double cv = 1.0 - acoef;
-            v.x = fma(f.x, cf, v.x * cv);
-            v.y = fma(f.y, cf, v.y * cv);
-            v.z = fma(f.z, cf, v.z * cv);
-            dt = fmin(dt * P.finc, P.dtmax);
-            acoef = acoef * P.falpha;
+            const float cf = (ff > 0.f) ? acoef * sqrtf(vv / ff) : 0.f;
+            const float cv = 1.f - acoef;
+            v.x = fmaf(f.x, cf, v.x * cv);
+            v.y = fmaf(f.y, cf, v.y * cv);
+            v.z = fmaf(f.z, cf, v.z * cv);
+            dt = fminf(dt * P.fincf, P.dtmaxf);
+            acoef = acoef * P.falphaf;
         }
         h = dt;
     } else {
-        const double c = 1.0 - P.acoef0;
+        const float c = 1.f - P.acoef0f;
         v.x *= c;
         v.y *= c;
         v.z *= c;
-        h = P.dtmax;
+        h = P.dtmaxf;
     }
-    v.x = fma(f.x, h, v.x);
-    v.y = fma(f.y, h, v.y);
-    v.z = fma(f.z, h, v.z);
-    d.x = fma(v.x, h, d.x);
-    d.y = fma(v.y, h, d.y);
-    d.z = fma(v.z, h, d.z);
+    v.x = fmaf(f.x, h, v.x);
+    v.y = fmaf(f.y, h, v.y);
+    v.z = fmaf(f.z, h, v.z);
+    d[0] = df_add_f(d[0], v.x * h);
+    d[1] = df_add_f(d[1], v.y * h);
+    d[2] = df_add_f(d[2], v.z * h);
     return ff;
 }
 
@@ -211,43 +274,60 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
         const double *t = S.rTips + ((long long)s * nstep + iz) * 3;
         return make_double3(t[0], t[1], t[2]);
     };
+    // grid coordinate of the tip (float64, once per height) = base (integer) + tf (fraction)
+    int base[3] = {0, 0, 0};
+    dfl tf[3];
+    auto set_tip = [&](double3 tp) {
+        const double3 g = to_grid(P, tp.x, tp.y, tp.z);
+        const double gg[3] = {g.x, g.y, g.z};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double fl = floor(gg[k]);
+            base[k] = (int)fl;
+            tf[k] = df_from(gg[k] - fl);
+        }
+    };
 
-    double3 tip = make_double3(0.0, 0.0, 0.0), gt = tip;
-    double3 d = make_double3(P.rPP0[0], P.rPP0[1], P.rPP0[2]);  // first start: r = tip + rPP0
-    double3 v = make_double3(0.0, 0.0, 0.0);
-    double dt = P.dtmax, acoef = P.acoef0;
+    double3 tip = make_double3(0.0, 0.0, 0.0);
+    dfl d[3] = {df_from(P.rPP0[0]), df_from(P.rPP0[1]), df_from(P.rPP0[2])};  // first start: r = tip + rPP0
+    float3 v = make_float3(0.f, 0.f, 0.f);
+    float dt = P.dtmaxf, acoef = P.acoef0f;
     int iz = 0, it = 0, itcount = 0;
     bool fin = P.maxIters <= 0;
     int itsum = 0;
     unsigned long long mine = 0;
     if (active) {
         tip = tip_at(0);
-        gt = to_grid(P, tip.x, tip.y, tip.z);
+        set_tip(tip);
+    } else {
+        tf[0] = tf[1] = tf[2] = dfl{0.f, 0.f};
     }
 
     while (__any_sync(FULL, active)) {
         if (!active) continue;
-        const double3 gd = to_grid(P, d.x, d.y, d.z);
-        const double3 F = interp_force(P.FE, P.n0, P.n1, P.n2, make_double3(gt.x + gd.x, gt.y + gd.y, gt.z + gd.z));
+        dfl u[3], F[3];
+        grid_coord_df(P, tf, d, u);
+        interp_force_df(P.FE, P.n0, P.n1, P.n2, base, u, F);
         if (fin) {
             // outputs of height iz: position after the last move, grid force there
+            const double dx = df_to(d[0]), dy = df_to(d[1]), dz = df_to(d[2]);
             if (SCAN) {
                 const long long o = (long long)s * nstep + (nstep - 1 - iz);
-                if (C.fzs) C.fzs[o] = (float)F.z;
+                if (C.fzs) C.fzs[o] = df_round(F[2]);
                 if (C.ppos) {
-                    C.ppos[3 * o + 0] = (float)((tip.x + d.x) + C.off[0]);
-                    C.ppos[3 * o + 1] = (float)((tip.y + d.y) + C.off[1]);
-                    C.ppos[3 * o + 2] = (float)((tip.z + d.z) + C.off[2]);
+                    C.ppos[3 * o + 0] = (float)((tip.x + dx) + C.off[0]);
+                    C.ppos[3 * o + 1] = (float)((tip.y + dy) + C.off[1]);
+                    C.ppos[3 * o + 2] = (float)((tip.z + dz) + C.off[2]);
                 }
                 if (C.iters) C.iters[o] = itcount;
             } else {
                 const long long o = (long long)s * nstep + iz;
-                S.rs[3 * o + 0] = tip.x + d.x;
-                S.rs[3 * o + 1] = tip.y + d.y;
-                S.rs[3 * o + 2] = tip.z + d.z;
-                S.fs[3 * o + 0] = F.x;
-                S.fs[3 * o + 1] = F.y;
-                S.fs[3 * o + 2] = F.z;
+                S.rs[3 * o + 0] = tip.x + dx;
+                S.rs[3 * o + 1] = tip.y + dy;
+                S.rs[3 * o + 2] = tip.z + dz;
+                S.fs[3 * o + 0] = df_to(F[0]);
+                S.fs[3 * o + 1] = df_to(F[1]);
+                S.fs[3 * o + 2] = df_to(F[2]);
                 if (S.iters) S.iters[o] = itcount;
             }
             itsum += itcount;
@@ -271,24 +351,28 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
             // next height: warm start (relaxTipStroke, ProbeParticle.cpp:643-655)
             const double3 nt = tip_at(iz);
             if (P.probeStart == 0) {
-                d = make_double3(P.rPP0[0], P.rPP0[1], P.rPP0[2]);
+                d[0] = df_from(P.rPP0[0]);
+                d[1] = df_from(P.rPP0[1]);
+                d[2] = df_from(P.rPP0[2]);
             } else if (P.probeStart == -1) {  // the probe stays where it was
-                d = make_double3((tip.x + d.x) - nt.x, (tip.y + d.y) - nt.y, (tip.z + d.z) - nt.z);
+                d[0] = df_from((tip.x + dx) - nt.x);
+                d[1] = df_from((tip.y + dy) - nt.y);
+                d[2] = df_from((tip.z + dz) - nt.z);
             }  // probeStart == 1: d = r - r_tip carries over unchanged
             tip = nt;
-            gt = to_grid(P, tip.x, tip.y, tip.z);
-            v = make_double3(0.0, 0.0, 0.0);
-            dt = P.dtmax;
-            acoef = P.acoef0;
+            set_tip(tip);
+            v = make_float3(0.f, 0.f, 0.f);
+            dt = P.dtmaxf;
+            acoef = P.acoef0f;
             it = 0;
             fin = P.maxIters <= 0;
             itcount = 0;
             continue;
         }
-        const double3 f = pp_force(P, F, d);
-        const double ff = relax_move(P, f, d, v, dt, acoef);
+        const float3 f = pp_force_df(P, F, d);
+        const float ff = relax_move_df(P, f, d, v, dt, acoef);
         mine++;
-        if (ff < P.convF2) {
+        if (ff < P.convF2f) {
             itcount = it;
             fin = true;
         } else if (++it >= P.maxIters) {
@@ -457,6 +541,21 @@ static int fill_relax_prm(RelaxPrm &P, const float *FE, const int *n, const doub
     P.probeStart = probeStart;
     P.iter_total = iter_total;
     P.err = device_error_word();
+    for (int k = 0; k < 9; k++) P.dic[k] = df_from(P.dicd[k]);
+    P.diag = P.dicd[1] == 0.0 && P.dicd[2] == 0.0 && P.dicd[3] == 0.0 && P.dicd[5] == 0.0 && P.dicd[6] == 0.0 &&
+             P.dicd[7] == 0.0;
+    P.kRadf = df_from(P.kRad);
+    P.nl0 = df_from(-P.lRad);
+    for (int k = 0; k < 3; k++) {
+        P.nr0[k] = df_from(-P.rPP0[k]);
+        P.kSf[k] = df_from(P.kSpring[k]);
+    }
+    P.convF2f = (float)P.convF2;
+    P.dtmaxf = (float)P.dtmax;
+    P.acoef0f = (float)P.acoef0;
+    P.fincf = (float)P.finc;
+    P.fdecf = (float)P.fdec;
+    P.falphaf = (float)P.falpha;
     return set_ok();
 }
 

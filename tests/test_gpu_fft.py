@@ -282,4 +282,5 @@ def test_density_overlap_pipeline_vs_oracle(gpulib, overlap_case, f64):
     assert np.abs(out["df"].cpu().numpy() - df)[ok].max() < 0.1
     itg = out["iters"].cpu().numpy()
     assert abs(itg.mean() - it.mean()) < 0.05 * it.mean() + 0.5
-    assert np.abs(out["fzs"].cpu().numpy() - fzs)[~flips].max() < 1e-4
+    dfz = np.abs(out["fzs"].cpu().numpy() - fzs)[~flips].max()
+    assert dfz < (1e-4 if f64 else 2e-3), dfz
