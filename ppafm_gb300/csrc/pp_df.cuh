@@ -75,4 +75,30 @@ __device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.
 
 __device__ __forceinline__ float df_round(dfl a) { return __fadd_rn(a.h, a.l); }
 
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
+
+// floor(x) as a float and an int for |x| < 2^22 with float32 adds only (no conversion
+// instructions): x + 1.5*2^23 rounds x to the nearest integer, held in the low mantissa bits.
+__device__ __forceinline__ float floor_small(float x, int &i) {
+    const float M = 12582912.0f;
+    const float xm = __fadd_rn(x, M);
+    float r = __fsub_rn(xm, M);
+    int ri = __float_as_int(xm) - 0x4B400000;
+    const bool over = r > x;
+    r = over ? __fsub_rn(r, 1.f) : r;
+    i = over ? ri - 1 : ri;
+    return r;
+}
+
+// Integer + fraction of a double-float coordinate g: g = i + (t.h + t.l), t.h in [0, 1]
+// exactly representable (the fraction bits of g.h), t.l = g.l.  |g| < 2^22.
+__device__ __forceinline__ dfl split_cell(dfl g, int &i) {
+    const float fl = floor_small(g.h, i);
+    float th = __fsub_rn(g.h, fl);
+    const bool below = (th == 0.f) && (g.l < 0.f);  // just under the boundary: previous cell
+    th = below ? 1.f : th;
+    i = below ? i - 1 : i;
+    return {th, g.l};
+}
+
 }  // namespace ppgpu

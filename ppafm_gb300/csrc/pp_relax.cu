@@ -35,7 +35,7 @@
 
 namespace ppgpu {
 
-constexpr int RELAX_THREADS = 128;
+constexpr int RELAX_THREADS = 64;  // small blocks spread the strokes evenly over the SMs
 constexpr int MAX_DF_TAPS = 64;
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -55,6 +55,7 @@ struct RelaxPrm {
     int diag;    // dicd is diagonal
     dfl kRadf, nl0;        // kRad, -lRad
     dfl nr0[3], kSf[3];    // -rPP0, kSpring
+    dfl r0[3];             // rPP0
     float convF2f, dtmaxf, acoef0f, fincf, fdecf, falphaf;
 };
 
@@ -69,6 +70,7 @@ struct ScanIO {  // regular scan semantics
     int nx, ny, nz;
     const double *xs, *ys, *zs;
     double off[3];
+    dfl offd[3];
     float *fzs, *ppos, *df;
     int *iters;
     int nw;
@@ -86,17 +88,10 @@ __device__ __forceinline__ void interp_force_df(const float4 *__restrict__ FE, i
     dfl t[3], m[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        float fl = floorf(u[k].h);
-        float th = __fsub_rn(u[k].h, fl);  // exact: the fraction bits of u.h
-        const float tl = u[k].l;
-        if (th == 0.f && tl < 0.f) {  // just below the cell boundary
-            th = 1.f;
-            fl = __fsub_rn(fl, 1.f);
-        }
-        ci[k] = base[k] + (int)fl;
-        t[k] = {th, tl};
-        const dfl o = two_sum(1.f, -th);
-        m[k] = {o.h, __fsub_rn(o.l, tl)};
+        t[k] = split_cell(u[k], ci[k]);
+        ci[k] += base[k];
+        const dfl o = two_sum(1.f, -t[k].h);
+        m[k] = {o.h, __fsub_rn(o.l, t[k].l)};
     }
     const int ix0 = wrap_index(ci[0], n0), iy0 = wrap_index(ci[1], n1), iz0 = wrap_index(ci[2], n2);
     const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
@@ -185,23 +180,33 @@ __device__ __forceinline__ void grid_coord_df(const RelaxPrm &P, const dfl tf[3]
 // lengths, and the force is a small difference of the grid force and the springs.
 __device__ __forceinline__ float3 pp_force_df(const RelaxPrm &P, const dfl F[3], const dfl d[3]) {
     const dfl l2 = df_add(df_add(df_sq(d[0]), df_sq(d[1])), df_sq(d[2]));
-    // l = sqrt(l2): float32 root, one Newton correction from the exact residual
-    const float L = __fsqrt_rn(l2.h);
+    // l = sqrt(l2) and 1/l: approximate float32 root, then one correction from the exact
+    // residual l2 - L^2 (error ~ the square of the approximation's)
+    const float rs = rsqrt_approx(l2.h);
+    const float L = __fmul_rn(l2.h, rs);
     const dfl LL = two_prod(L, L);
     const float res = __fadd_rn(__fsub_rn(__fsub_rn(l2.h, LL.h), LL.l), l2.l);
-    const dfl l = fast_two_sum(L, __fmul_rn(res, __fdiv_rn(0.5f, L)));
+    const dfl l = fast_two_sum(L, __fmul_rn(res, __fmul_rn(0.5f, rs)));
     const dfl x = df_add(l, P.nl0);  // l - l0
-    // q = (l - l0) / l: float32 quotient plus the correction from its exact remainder
-    const float qh = __fdiv_rn(x.h, l.h);
+    // q = (l - l0) / l: approximate quotient plus the correction from its exact remainder
+    const float qh = __fmul_rn(x.h, rs);
     const dfl ql = two_prod(qh, l.h);
     const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(x.h, ql.h), ql.l), x.l), __fmul_rn(qh, l.l));
-    const dfl s = df_mul(P.kRadf, fast_two_sum(qh, __fdiv_rn(rem, l.h)));
+    const dfl s = df_mul(P.kRadf, two_sum(qh, __fmul_rn(rem, rs)));
+    // f = F + d s + (d - r0) kS: the three high parts summed error-free, every low part and
+    // product error added once at the end (the result is rounded to float32)
     float f[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        dfl fk = df_add(F[k], df_mul(d[k], s));
-        fk = df_add(fk, df_mul(df_add(d[k], P.nr0[k]), P.kSf[k]));
-        f[k] = df_round(fk);
+        const dfl b = two_prod(d[k].h, s.h);
+        const float bl = __fmaf_rn(d[k].l, s.h, __fmaf_rn(d[k].h, s.l, b.l));
+        const dfl r = two_sum(d[k].h, P.nr0[k].h);  // d - r0
+        const float rl = __fadd_rn(r.l, __fadd_rn(d[k].l, P.nr0[k].l));
+        const dfl c = two_prod(r.h, P.kSf[k].h);
+        const float cl = __fmaf_rn(rl, P.kSf[k].h, __fmaf_rn(r.h, P.kSf[k].l, c.l));
+        const dfl s1 = two_sum(F[k].h, b.h);
+        const dfl s2 = two_sum(s1.h, c.h);
+        f[k] = __fadd_rn(s2.h, __fadd_rn(__fadd_rn(s1.l, s2.l), __fadd_rn(F[k].l, __fadd_rn(bl, cl))));
     }
     return make_float3(f[0], f[1], f[2]);
 }
@@ -222,8 +227,10 @@ __device__ __forceinline__ float relax_move_df(const RelaxPrm &P, float3 f, dfl 
             dt = dt * P.fdecf;
             acoef = P.acoef0f;
         } else {
-            // ff == 0 gives cf = 0 (the reference would divide by zero)
-            const float cf = (ff > 0.f) ? acoef * sqrtf(vv / ff) : 0.f;
+            // cf f has length acoef |v|; vv ff below 1e-30 gives cf = 0 instead of an
+            // overflow (the reference divides by zero at ff == 0, and cf = 0 at vv == 0)
+            const float vf2 = vv * ff;  // sqrt(vv/ff) = vv / sqrt(vv ff)
+            const float cf = (vf2 > 1e-30f) ? acoef * vv * rsqrt_approx(vf2) : 0.f;
             const float cv = 1.f - acoef;
             v.x = fmaf(f.x, cf, v.x * cv);
             v.y = fmaf(f.y, cf, v.y * cv);
@@ -257,11 +264,42 @@ __device__ __forceinline__ void add_iterations(unsigned long long *total, unsign
 
 // --------------------------------------------------------- CPU-core semantics
 
+// Tip grid coordinate g = dic . tip split into an integer cell (base) and a fraction (tf).
+__device__ __forceinline__ void tip_cell(const RelaxPrm &P, const dfl g[3], int base[3], dfl tf[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) tf[k] = split_cell(g[k], base[k]);
+}
+
+__device__ __forceinline__ void grid_of(const RelaxPrm &P, const dfl r[3], dfl g[3]) {
+    if (P.diag) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) g[k] = df_mul(P.dic[4 * k], r[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            g[k] = df_add(df_add(df_mul(P.dic[3 * k], r[0]), df_mul(P.dic[3 * k + 1], r[1])), df_mul(P.dic[3 * k + 2], r[2]));
+    }
+}
+
+// Scan mode keeps a per-height table in shared memory: (z, g_z0, g_z1, g_z2) as
+// double-floats, g_z = dic . (0, 0, z), so a height change needs no float64.
+constexpr int ZTAB = 4;
+
 template <bool SCAN>
 __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, const StrokeIO S, const ScanIO C) {
+    extern __shared__ dfl ztab[];
     const int s = blockIdx.x * RELAX_THREADS + threadIdx.x;
     const int nstroke = SCAN ? C.nx * C.ny : S.nstroke;
     const int nstep = SCAN ? C.nz : S.nstep;
+    if (SCAN) {
+        for (int i = threadIdx.x; i < nstep; i += RELAX_THREADS) {
+            const dfl z = df_from(C.zs[i]);
+            ztab[ZTAB * i] = z;
+#pragma unroll
+            for (int k = 0; k < 3; k++) ztab[ZTAB * i + 1 + k] = df_mul(P.dic[3 * k + 2], z);
+        }
+        __syncthreads();
+    }
     bool active = s < nstroke && nstep > 0;
 
     int ix = 0, iy = 0;
@@ -269,27 +307,27 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
         ix = s / C.ny;
         iy = s - ix * C.ny;
     }
-    auto tip_at = [&](int iz) {
-        if (SCAN) return make_double3(C.xs[ix], C.ys[iy], C.zs[iz]);
-        const double *t = S.rTips + ((long long)s * nstep + iz) * 3;
-        return make_double3(t[0], t[1], t[2]);
-    };
-    // grid coordinate of the tip (float64, once per height) = base (integer) + tf (fraction)
-    int base[3] = {0, 0, 0};
+    // tip (double-float) and its grid coordinate: base cell + fraction
+    dfl tip[3], gxy[3];
+    int base[3];
     dfl tf[3];
-    auto set_tip = [&](double3 tp) {
-        const double3 g = to_grid(P, tp.x, tp.y, tp.z);
-        const double gg[3] = {g.x, g.y, g.z};
+    auto set_height = [&](int iz) {
+        dfl g[3];
+        if (SCAN) {
+            tip[2] = ztab[ZTAB * iz];
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const double fl = floor(gg[k]);
-            base[k] = (int)fl;
-            tf[k] = df_from(gg[k] - fl);
+            for (int k = 0; k < 3; k++) g[k] = df_add(gxy[k], ztab[ZTAB * iz + 1 + k]);
+        } else {
+            const double *t = S.rTips + ((long long)s * nstep + iz) * 3;
+            tip[0] = df_from(t[0]);
+            tip[1] = df_from(t[1]);
+            tip[2] = df_from(t[2]);
+            grid_of(P, tip, g);
         }
+        tip_cell(P, g, base, tf);
     };
 
-    double3 tip = make_double3(0.0, 0.0, 0.0);
-    dfl d[3] = {df_from(P.rPP0[0]), df_from(P.rPP0[1]), df_from(P.rPP0[2])};  // first start: r = tip + rPP0
+    dfl d[3] = {P.r0[0], P.r0[1], P.r0[2]};  // first start: r = tip + rPP0
     float3 v = make_float3(0.f, 0.f, 0.f);
     float dt = P.dtmaxf, acoef = P.acoef0f;
     int iz = 0, it = 0, itcount = 0;
@@ -297,10 +335,13 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
     int itsum = 0;
     unsigned long long mine = 0;
     if (active) {
-        tip = tip_at(0);
-        set_tip(tip);
-    } else {
-        tf[0] = tf[1] = tf[2] = dfl{0.f, 0.f};
+        if (SCAN) {
+            tip[0] = df_from(C.xs[ix]);
+            tip[1] = df_from(C.ys[iy]);
+            const dfl r[3] = {tip[0], tip[1], {0.f, 0.f}};
+            grid_of(P, r, gxy);
+        }
+        set_height(0);
     }
 
     while (__any_sync(FULL, active)) {
@@ -310,21 +351,21 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
         interp_force_df(P.FE, P.n0, P.n1, P.n2, base, u, F);
         if (fin) {
             // outputs of height iz: position after the last move, grid force there
-            const double dx = df_to(d[0]), dy = df_to(d[1]), dz = df_to(d[2]);
+            const dfl r[3] = {df_add(tip[0], d[0]), df_add(tip[1], d[1]), df_add(tip[2], d[2])};
             if (SCAN) {
                 const long long o = (long long)s * nstep + (nstep - 1 - iz);
                 if (C.fzs) C.fzs[o] = df_round(F[2]);
                 if (C.ppos) {
-                    C.ppos[3 * o + 0] = (float)((tip.x + dx) + C.off[0]);
-                    C.ppos[3 * o + 1] = (float)((tip.y + dy) + C.off[1]);
-                    C.ppos[3 * o + 2] = (float)((tip.z + dz) + C.off[2]);
+                    C.ppos[3 * o + 0] = df_round(df_add(r[0], C.offd[0]));
+                    C.ppos[3 * o + 1] = df_round(df_add(r[1], C.offd[1]));
+                    C.ppos[3 * o + 2] = df_round(df_add(r[2], C.offd[2]));
                 }
                 if (C.iters) C.iters[o] = itcount;
             } else {
                 const long long o = (long long)s * nstep + iz;
-                S.rs[3 * o + 0] = tip.x + dx;
-                S.rs[3 * o + 1] = tip.y + dy;
-                S.rs[3 * o + 2] = tip.z + dz;
+                S.rs[3 * o + 0] = df_to(r[0]);
+                S.rs[3 * o + 1] = df_to(r[1]);
+                S.rs[3 * o + 2] = df_to(r[2]);
                 S.fs[3 * o + 0] = df_to(F[0]);
                 S.fs[3 * o + 1] = df_to(F[1]);
                 S.fs[3 * o + 2] = df_to(F[2]);
@@ -349,18 +390,15 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
                 continue;
             }
             // next height: warm start (relaxTipStroke, ProbeParticle.cpp:643-655)
-            const double3 nt = tip_at(iz);
+            set_height(iz);
             if (P.probeStart == 0) {
-                d[0] = df_from(P.rPP0[0]);
-                d[1] = df_from(P.rPP0[1]);
-                d[2] = df_from(P.rPP0[2]);
-            } else if (P.probeStart == -1) {  // the probe stays where it was
-                d[0] = df_from((tip.x + dx) - nt.x);
-                d[1] = df_from((tip.y + dy) - nt.y);
-                d[2] = df_from((tip.z + dz) - nt.z);
+                d[0] = P.r0[0];
+                d[1] = P.r0[1];
+                d[2] = P.r0[2];
+            } else if (P.probeStart == -1) {  // the probe stays where it was: d = r_old - tip_new
+#pragma unroll
+                for (int k = 0; k < 3; k++) d[k] = df_add(r[k], df_neg(tip[k]));
             }  // probeStart == 1: d = r - r_tip carries over unchanged
-            tip = nt;
-            set_tip(tip);
             v = make_float3(0.f, 0.f, 0.f);
             dt = P.dtmaxf;
             acoef = P.acoef0f;
@@ -548,6 +586,7 @@ static int fill_relax_prm(RelaxPrm &P, const float *FE, const int *n, const doub
     P.nl0 = df_from(-P.lRad);
     for (int k = 0; k < 3; k++) {
         P.nr0[k] = df_from(-P.rPP0[k]);
+        P.r0[k] = df_from(P.rPP0[k]);
         P.kSf[k] = df_from(P.kSpring[k]);
     }
     P.convF2f = (float)P.convF2;
@@ -606,7 +645,10 @@ extern "C" int ppgpu_relax_scan(const float *FE, const int *n, const double *cel
     C.xs = xs;
     C.ys = ys;
     C.zs = zs;
-    for (int k = 0; k < 3; k++) C.off[k] = pos_offset ? pos_offset[k] : 0.0;
+    for (int k = 0; k < 3; k++) {
+        C.off[k] = pos_offset ? pos_offset[k] : 0.0;
+        C.offd[k] = df_from(C.off[k]);
+    }
     C.fzs = fzs;
     C.ppos = ppos;
     C.iters = iters;
@@ -615,7 +657,9 @@ extern "C" int ppgpu_relax_scan(const float *FE, const int *n, const double *cel
     for (int i = 0; i < C.nw; i++) C.W[i] = (float)df_weights[i];
     const long long npix = (long long)nx * ny;
     const unsigned nblk = (unsigned)((npix + RELAX_THREADS - 1) / RELAX_THREADS);
-    relax_kernel<true><<<nblk, RELAX_THREADS, 0, (cudaStream_t)stream>>>(P, S, C);
+    const size_t smem = (size_t)nz * ZTAB * sizeof(dfl);
+    if (smem > 48 * 1024) return set_error(PPGPU_ERR_ARG, "relax_scan: nz = %d heights exceed the table limit (1536)", nz);
+    relax_kernel<true><<<nblk, RELAX_THREADS, smem, (cudaStream_t)stream>>>(P, S, C);
     PPGPU_CHECK_LAUNCH("relax_kernel<scan>");
     return set_ok();
 }
