@@ -192,6 +192,39 @@ int ppgpu_fft_poisson(void *handle, const float *rho_charge, const double *lvec,
 int ppgpu_gaussian_density(float *rho, const int *n, const double *lvec, int natoms, const double *atoms,
                            int accumulate, void *stream);
 
+/* ------------------------------------------------------------ batched systems
+ * Many systems (molecules of uneven atom counts, cells and grids) in ONE persistent launch:
+ * the LJC force field of each (the PPGPU_FF_LJC mode of ppgpu_ff_grid, no energy, no
+ * accumulation), then its relaxed scan with ppgpu_relax_scan semantics and the fused df.
+ * Replaces the per-molecule loop of the reference's batched caller (ppafm/ml/Generator.py:
+ * 68-144 calling AFMulator once per molecule; relaxTipStrokes_omp, ProbeParticle.cpp:682-701,
+ * per system).  Orthogonal cells only; at most 1024 charged atoms (with images) per system.
+ * Tip coordinates are HOST arrays (copied at creation); FE, atoms and outputs are device
+ * memory.  ppgpu_batch_run allocates nothing and does not synchronise (CUDA-graph safe). */
+typedef struct {
+    float *FE;            /* device float4 grid [n0][n1][n2], written */
+    const float *atoms;   /* device atom records (ppgpu_pack_atoms), charged first */
+    int natoms, ncharged;
+    int n[3];
+    double cell[9];       /* rows a, b, c: diagonal */
+    int nx, ny, nz;
+    const double *xs, *ys, *zs; /* host; relative to the grid origin; zs in approach order */
+    double pos_offset[3];
+    float *fzs, *ppos, *df; /* device outputs as in ppgpu_relax_scan (nullable) */
+    int *iters;
+} ppgpu_batch_job;
+/* tuning[4] (NULL = defaults 2, 8, 4, 64): CTAs per SM (1-2), pixel tile width and height of
+ * the stroke order, strokes per warp chunk.  prm: PPGPU_RELAX_NPARAM relaxation parameters;
+ * Q, Fmax: probe charge and force clamp of the LJC field; df_weights: nw taps (nw 0 = no df). */
+int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const double *prm, double Q, double Fmax, int nw,
+                       const double *df_weights, const int *tuning, void **handle);
+int ppgpu_batch_run(void *handle, void *stream);
+/* out4 = (force-field items, strokes incl. tile padding, CTAs, systems) */
+int ppgpu_batch_info(void *handle, long long *out4);
+/* FIRE iterations of the last run (synchronises the stream). */
+int ppgpu_batch_iterations(void *handle, unsigned long long *out, void *stream);
+int ppgpu_batch_destroy(void *handle);
+
 /* -------------------------------------------------------------- grid utilities */
 /* Fz -> df along the last axis: out[c][j] = scale * sum_i F[c][j+i] * W[nw-1-i]. */
 int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const double *W, double scale, float *out,

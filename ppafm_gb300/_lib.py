@@ -71,7 +71,36 @@ SIGNATURES = {
     "ppgpu_fft_poisson": ([c_void_p, c_void_p, _dp, c_void_p, c_void_p], c_int),
     "ppgpu_gaussian_density": ([c_void_p, _ip, _dp, c_int, c_void_p, c_int, c_void_p], c_int),
     "ppgpu_lj_grid_f64_noalloc": ([c_void_p, c_void_p, _ip, _dp, c_int, c_void_p, c_void_p, c_void_p], c_int),
+    "ppgpu_batch_create": ([c_void_p, c_int, _dp, c_double, c_double, c_int, _dp, _ip, POINTER(c_void_p)], c_int),
+    "ppgpu_batch_run": ([c_void_p, c_void_p], c_int),
+    "ppgpu_batch_info": ([c_void_p, POINTER(c_longlong)], c_int),
+    "ppgpu_batch_iterations": ([c_void_p, POINTER(c_ulonglong), c_void_p], c_int),
+    "ppgpu_batch_destroy": ([c_void_p], c_int),
 }
+
+
+class BatchJob(ctypes.Structure):
+    """ppgpu_batch_job of include/ppgpu.h."""
+
+    _fields_ = [
+        ("FE", c_void_p),
+        ("atoms", c_void_p),
+        ("natoms", c_int),
+        ("ncharged", c_int),
+        ("n", c_int * 3),
+        ("cell", c_double * 9),
+        ("nx", c_int),
+        ("ny", c_int),
+        ("nz", c_int),
+        ("xs", _dp),
+        ("ys", _dp),
+        ("zs", _dp),
+        ("pos_offset", c_double * 3),
+        ("fzs", c_void_p),
+        ("ppos", c_void_p),
+        ("df", c_void_p),
+        ("iters", c_void_p),
+    ]
 
 _lib = None
 
