@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap"])
+    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap", "molecule_batch"])
+    ap.add_argument("--nmol", type=int, default=256)
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0)
@@ -229,6 +230,213 @@ class OverlapJob:
         return {}
 
 
+def cpu_batch_sample(systems, budget_s, seed=0):
+    """The reference pipeline on the host cores for 4 molecules of the batch (each sampled by
+    oracle/cpu_baseline.py), as pixel-heights per second."""
+    try:
+        from oracle import cpu_baseline
+
+        picks = systems[:: max(1, len(systems) // 4)][:4]
+        tot_s, tot_pz, info = 0.0, 0.0, None
+        for m in picks:
+            s = cpu_baseline.sample_pipeline(m, budget_s=budget_s / len(picks), seed=seed)
+            tot_s += s["total_s"]
+            tot_pz += s["pixel_z_per_s"] * s["total_s"]
+            info = s
+        return {"value": tot_pz / tot_s, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": f"{len(picks)} of {len(systems)} molecules, each: " + info["sample"]}
+    except Exception as e:  # the baseline is reported, never fatal
+        return {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+
+
+class BatchBench:
+    """256-molecule batch: one persistent launch (force fields + relaxed scans + df of every
+    molecule) replayed from a CUDA graph, launch shape from the autotuner.  Also times the
+    plain GPU form (one HighLevel.Pipeline per molecule) for comparison."""
+
+    def __init__(self, systems, relax, HL, torch):
+        from ppafm_gb300 import batch as BT
+
+        self.w = systems[0]
+        self.systems = systems
+        self.torch = torch
+        self.tuning, self.tune_ms = BT.autotune(systems, self.w, relax, reps=2)
+        self.pl = BT.BatchPipeline(systems, self.w, relax=relax, want_ppos=True, tuning=self.tuning)
+        self.pl.capture()
+        self.units = self.pl.pixel_z
+        self.npts = int(sum(np.prod(s["n"]) for s in self.pl.systems))
+        self.pairs = int(sum(np.prod(s["n"]) * s["natoms"] for s in self.pl.systems))
+        self.launches_per_step = 1
+        self.BT = BT
+        self.relax = relax
+        pin = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s["out"].items()} for s in self.pl.systems]
+        self.pin_out = pin
+
+    def step(self):
+        self.pl.replay()
+
+    def e2e_step(self):
+        """Public API end to end: host atoms of every molecule -> packed records (H2D) ->
+        the batched launch -> outputs to pinned host memory (D2H)."""
+        from ppafm_gb300.device import pack_atoms
+
+        h2d = 0
+        for s, w in zip(self.pl.systems, self.systems):
+            Rs0, cLJs, kqq = self.HL.prepare_atoms(w["Zs"], w["Rs"], w["Qs"], w["lvec"], self.w)
+            rec, _, _ = pack_atoms(Rs0, cLJs, kqq, device="cpu")
+            s.setdefault("rec_pin", self.torch.empty(rec.shape, dtype=rec.dtype, pin_memory=True))
+            s["rec_pin"].copy_(rec)
+            h2d += rec.numel() * rec.element_size()
+        for s in self.pl.systems:
+            s["rec"].copy_(s["rec_pin"], non_blocking=True)
+        self.pl.replay()
+        d2h = 0
+        for s, pin in zip(self.pl.systems, self.pin_out):
+            for k, v in s["out"].items():
+                pin[k].copy_(v, non_blocking=True)
+                d2h += v.numel() * v.element_size()
+        self.torch.cuda.current_stream().synchronize()
+        return h2d, d2h
+
+    def plain_ms(self, reps=2):
+        pls = self.BT.plain_loop(self.systems, self.w, self.relax)
+        torch = self.torch
+        for p in pls:
+            p.run()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        best = float("inf")
+        for _ in range(reps):
+            a.record()
+            for p in pls:
+                p.run()
+            b.record()
+            b.synchronize()
+            best = min(best, a.elapsed_time(b))
+        return best
+
+
+def run_batch(args, rank, world, local):
+    import torch
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import _lib, workloads
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    systems = workloads.molecule_batch(seed=args.seed + rank, nmol=args.nmol, scale=args.scale)
+    w = systems[0]
+    relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    job = BatchBench(systems, relax, HL, torch)
+    job.HL = HL
+    st = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        job.step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for a, b in ev:
+        a.record(st)
+        job.step()
+        b.record(st)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    t_step = sum(a.elapsed_time(b) * 1e-3 for a, b in ev)
+    iters = job.pl.iterations()
+    _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
+    # end to end
+    for _ in range(max(1, args.warmup)):
+        job.e2e_step()
+    barrier()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(args.steps):
+        h2d, d2h = job.e2e_step()
+    b.record(st)
+    b.synchronize()
+    t_e2e = a.elapsed_time(b) * 1e-3
+    t_step_max, t_e2e_max = t_step, t_e2e
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step_max, t_e2e_max = float(tt[0]), float(tt[1])
+    K = args.steps
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return None
+    plain = job.plain_ms()
+    peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
+    flops = job.pairs * FLOPS_LJC_PAIR
+    line = {
+        "metric": METRIC,
+        "value": job.units * world * K / t_step_max,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_step_max / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {
+            "workload": "molecule_batch",
+            "molecules": len(systems),
+            "atoms": [int(min(len(s["Zs"]) for s in systems)), int(max(len(s["Zs"]) for s in systems))],
+            "grid_points": job.npts,
+            "pixel_z": job.units,
+            "scan_per_molecule": list(job.pl.systems[0]["scan_shape"]),
+            "fire": relax,
+            "tuning": {"ctas_per_sm": job.tuning[0], "tile": [job.tuning[1], job.tuning[2]], "chunk": job.tuning[3]},
+            "l2": "inputs larger than L2 (force fields %.2f GB)" % (job.npts * 16 / 1e9),
+            "parallelism": f"replicas x{world}",
+        },
+        "plain_gpu_loop": {"ms_per_step": plain, "value": job.units / (plain * 1e-3), "speedup_of_batched": plain / (1e3 * t_step_max / K)},
+        "fire_iters_per_pixel_z": iters / job.units,
+        "e2e": {"value": job.units * world * K / t_e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": job.launches_per_step * K,
+        "roofline": {
+            "bound": "fp32",
+            "kernel": "batch_kernel (force-field phase + relaxation phase, one launch)",
+            "achieved": flops / (t_step_max / K) / 1e12,
+            "peak": peak,
+            "unit": "TFLOP/s",
+            "frac": flops / (t_step_max / K) / 1e12 / peak if peak else None,
+            "peak_source": "FFMA microbenchmark measured in this run; achieved counts only the force-field flops over the whole step",
+            "flops_per_launch": flops,
+            "traffic": None,
+        },
+        "cpu_baseline": None,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_batch_sample(systems, args.cpu_budget)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return line
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -405,6 +613,36 @@ def run_reference(args, rank, world):
         return None
     from oracle import cpu_baseline
 
+    if args.workload == "molecule_batch":
+        from ppafm_gb300 import workloads
+
+        systems = workloads.molecule_batch(seed=args.seed, nmol=args.nmol, scale=args.scale)
+        vals = [cpu_batch_sample(systems, args.cpu_budget / 2, seed=i) for i in range(args.warmup + args.steps)][args.warmup :]
+        v = float(np.median([x["value"] for x in vals]))
+        from ppafm_gb300 import common as C
+
+        units = 0
+        for m in systems:
+            xT, yT, zT, _ = C.prepareScanGrids(m["scanMin"], m["scanMax"], m["scanStep"], m["r0Probe"])
+            units += len(xT) * len(yT) * len(zT)
+        return {
+            "impl": "reference",
+            "metric": METRIC,
+            "value": v,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": 1e3 * units / v,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "molecule_batch", "molecules": len(systems), "parallelism": "host cores"},
+            "cpu_baseline": dict(vals[-1], value=v),
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     w = make_workload(args.workload, args.seed, args.scale)
     vals = []
     info = None
@@ -443,6 +681,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.workload == "molecule_batch":
+        line = run_batch(args, rank, world, local)
     else:
         line = run_ours(args, rank, world, local)
     if line is not None:

@@ -95,7 +95,7 @@ class BatchPipeline:
             J.df = out["df"].data_ptr() if "df" in out else None
             J.iters = out["iters"].data_ptr() if "iters" in out else None
             self._keep += [xs, ys, zs, rec]
-            self.systems.append(dict(FE=FE, n=n, lvec=lvec, natoms=natoms, ncharged=nch, out=out, scan_shape=(nx, ny, nz), lvecScan=lvecScan))
+            self.systems.append(dict(FE=FE, rec=rec, n=n, lvec=lvec, natoms=natoms, ncharged=nch, out=out, scan_shape=(nx, ny, nz), lvecScan=lvecScan))
         self._jobs = jobs
         self.handle = ctypes.c_void_p()
         tun = np.ascontiguousarray(self.tuning, dtype=np.int32)
