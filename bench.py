@@ -55,10 +55,9 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from ppafm_gb300.ranks import dist_env as env
+
+    return env()
 
 
 def make_workload(name, seed, scale):
@@ -371,13 +370,9 @@ def run_batch(args, rank, world, local):
     b.record(st)
     b.synchronize()
     t_e2e = a.elapsed_time(b) * 1e-3
-    t_step_max, t_e2e_max = t_step, t_e2e
-    if world > 1:
-        import torch.distributed as dist
+    from ppafm_gb300.ranks import max_over_ranks
 
-        tt = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step_max, t_e2e_max = float(tt[0]), float(tt[1])
+    t_step_max, t_e2e_max = max_over_ranks([t_step, t_e2e], device="cuda")
     K = args.steps
     if rank != 0:
         if world > 1:
@@ -516,13 +511,9 @@ def run_ours(args, rank, world, local):
     d2h = int(sum(v.numel() * v.element_size() for v in pin_out.values()))
 
     # ---------------- max over ranks
-    t_step_max, t_e2e_max = t_step, t_e2e
-    if world > 1:
-        import torch.distributed as dist
+    from ppafm_gb300.ranks import max_over_ranks
 
-        tt = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step_max, t_e2e_max = float(tt[0]), float(tt[1])
+    t_step_max, t_e2e_max = max_over_ranks([t_step, t_e2e], device="cuda")
     K = args.steps
     value = units * world * K / t_step_max
     e2e_value = units * world * K / t_e2e_max

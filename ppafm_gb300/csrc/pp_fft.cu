@@ -60,6 +60,12 @@ static unsigned blocks_for(long long n) {
     return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
+// One thread per half-spectrum element: x over the last axis, y and z over the rows.
+static dim3 spec_grid(const FFTPlan *P) {
+    const int nh2 = P->n[2] / 2 + 1;
+    return dim3((unsigned)((nh2 + FFT_THREADS - 1) / FFT_THREADS), (unsigned)P->n[1], (unsigned)P->n[0]);
+}
+
 // Rolled coordinate index of getMGrid (fieldFFT.py:32-49): i for i < n/2, i - n above.
 __device__ __forceinline__ double rolled(int i, int n) { return (double)(i < n / 2 ? i : i - n); }
 __device__ __forceinline__ double rolled_odd(int i, int n) {
@@ -90,26 +96,29 @@ struct Cx<cufftDoubleComplex> {
     static __device__ __forceinline__ cufftDoubleComplex make(double x, double y) { return make_cuDoubleComplex(x, y); }
 };
 
-// Four output spectra from FFT(V) and FFT(rho).
+// Four output spectra from FFT(V) and FFT(rho).  Grid (ceil(nh2/FFT_THREADS), n1, n0): one
+// thread per half-spectrum element of row (i, j).  The arithmetic is done in the precision
+// of the transforms (float32 spectra: float; float64 spectra: double).
 template <typename C>
 __global__ void spectra_kernel(const C *__restrict__ Vk, const C *__restrict__ Rk, C *__restrict__ S4, long long Nh,
                                SpecPrm P) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Nh; q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % P.nh2);
-        const int j = (int)((q / P.nh2) % P.n1);
-        const int i = (int)(q / ((long long)P.nh2 * P.n1));
-        const C a = Vk[q], b = Rk[q];
-        // C = a conj(b)
-        const double cr = (double)a.x * b.x + (double)a.y * b.y;
-        const double ci = (double)a.y * b.x - (double)a.x * b.y;
-        const double xo = rolled_odd(i, P.n0), yo = rolled_odd(j, P.n1), zo = rolled_odd(k, P.n2);
-        S4[q] = Cx<C>::make(cr * P.sE, ci * P.sE);
+    using R = typename Cx<C>::real;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.nh2) return;
+    const int j = blockIdx.y, i = blockIdx.z;
+    const long long q = ((long long)i * P.n1 + j) * P.nh2 + k;
+    const C a = Vk[q], b = Rk[q];
+    // C = a conj(b)
+    const R cr = a.x * b.x + a.y * b.y;
+    const R ci = a.y * b.x - a.x * b.y;
+    const R xo = (R)rolled_odd(i, P.n0), yo = (R)rolled_odd(j, P.n1), zo = (R)rolled_odd(k, P.n2);
+    const R sE = (R)P.sE, sF = (R)P.sF;
+    S4[q] = Cx<C>::make(cr * sE, ci * sE);
 #pragma unroll
-        for (int ax = 0; ax < 3; ax++) {
-            const double zeta = P.z[3 * ax] * xo + P.z[3 * ax + 1] * yo + P.z[3 * ax + 2] * zo;
-            // zeta C (-2 pi i) = zeta (2 pi ci, -2 pi cr)
-            S4[(ax + 1) * Nh + q] = Cx<C>::make(zeta * ci * P.sF, -zeta * cr * P.sF);
-        }
+    for (int ax = 0; ax < 3; ax++) {
+        const R zeta = ((R)P.z[3 * ax] * xo + (R)P.z[3 * ax + 1] * yo + (R)P.z[3 * ax + 2] * zo) * sF;
+        // zeta C (-2 pi i) = zeta (2 pi ci, -2 pi cr)
+        S4[(ax + 1) * Nh + q] = Cx<C>::make(zeta * ci, -zeta * cr);
     }
 }
 
@@ -200,25 +209,32 @@ __global__ void tip_density_kernel(float *rho, TipPrm P, long long N, const doub
 
 // ------------------------------------------------------------- density pre-processing
 
+// Sum and positive sum of a float grid: compensated float32 sums per thread (a few dozen
+// values each), float64 across threads.
 __global__ void density_sums_kernel(const float *rho, long long N, double *sums) {
-    double s = 0.0, sp = 0.0;
+    float s = 0.f, sc = 0.f, sp = 0.f, spc = 0.f;  // Neumaier running compensations
+    auto add = [](float &acc, float &c, float v) {
+        const float t = acc + v;
+        c += (fabsf(acc) >= fabsf(v)) ? (acc - t) + v : (v - t) + acc;
+        acc = t;
+    };
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
-        const double v = rho[p];
-        s += v;
-        sp += v > 0 ? v : 0.0;
+        const float v = rho[p];
+        add(s, sc, v);
+        add(sp, spc, v > 0.f ? v : 0.f);
     }
-    block_sum_to(s, sums);
+    block_sum_to((double)s + (double)sc, sums);
     __syncthreads();
-    block_sum_to(sp, sums + 1);
+    block_sum_to((double)sp + (double)spc, sums + 1);
 }
 
-__global__ void density_power_kernel(float *rho, long long N, const double *sums, int fix_negative, double B) {
-    const double f = fix_negative ? sums[0] / sums[1] : 1.0;
+__global__ void density_power_kernel(float *rho, long long N, const double *sums, int fix_negative, float B) {
+    const float f = fix_negative ? (float)(sums[0] / sums[1]) : 1.f;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
-        double v = rho[p];
-        if (fix_negative) v = (v < 0 ? 0.0 : v) * f;
-        if (B != 1.0) v = pow(v, B);
-        rho[p] = (float)v;
+        float v = rho[p];
+        if (fix_negative) v = (v < 0.f ? 0.f : v) * f;
+        if (B != 1.f) v = powf(v, B);
+        rho[p] = v;
     }
 }
 
@@ -235,19 +251,19 @@ __device__ __forceinline__ double freq(int i, int n) { return (double)(i <= (n -
 
 template <typename C>
 __global__ void poisson_kernel(C *Rk, long long Nh, PoissonPrm P) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Nh; q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % P.nh2);
-        const int j = (int)((q / P.nh2) % P.n1);
-        const int i = (int)(q / ((long long)P.nh2 * P.n1));
-        const double m0 = freq(i, P.n0), m1 = freq(j, P.n1), m2 = freq(k, P.n2);
-        const double gx = m0 * P.b[0] + m1 * P.b[3] + m2 * P.b[6];
-        const double gy = m0 * P.b[1] + m1 * P.b[4] + m2 * P.b[7];
-        const double gz = m0 * P.b[2] + m1 * P.b[5] + m2 * P.b[8];
-        const double g2 = gx * gx + gy * gy + gz * gz;
-        const C r = Rk[q];
-        const double f = (q == 0) ? 0.0 : P.s / g2;
-        Rk[q] = Cx<C>::make(r.x * f, r.y * f);
-    }
+    using R = typename Cx<C>::real;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.nh2) return;
+    const int j = blockIdx.y, i = blockIdx.z;
+    const long long q = ((long long)i * P.n1 + j) * P.nh2 + k;
+    const R m0 = (R)freq(i, P.n0), m1 = (R)freq(j, P.n1), m2 = (R)freq(k, P.n2);
+    const R gx = m0 * (R)P.b[0] + m1 * (R)P.b[3] + m2 * (R)P.b[6];
+    const R gy = m0 * (R)P.b[1] + m1 * (R)P.b[4] + m2 * (R)P.b[7];
+    const R gz = m0 * (R)P.b[2] + m1 * (R)P.b[5] + m2 * (R)P.b[8];
+    const R g2 = gx * gx + gy * gy + gz * gz;
+    const C r = Rk[q];
+    const R f = (q == 0) ? (R)0 : (R)P.s / g2;
+    Rk[q] = Cx<C>::make(r.x * f, r.y * f);
 }
 
 // ------------------------------------------------------------- Gaussian densities
@@ -320,6 +336,7 @@ extern "C" int ppgpu_fft_create(const int *n, int flags, void **handle) {
     if (!n || !handle) return set_error(PPGPU_ERR_ARG, "fft_create: null argument");
     for (int k = 0; k < 3; k++)
         if (n[k] <= 0) return set_error(PPGPU_ERR_ARG, "fft_create: sizes must be positive");
+    if (n[0] > 65535 || n[1] > 65535) return set_error(PPGPU_ERR_ARG, "fft_create: n0, n1 must be at most 65535");
     if (flags & ~PPGPU_FFT_F64) return set_error(PPGPU_ERR_ARG, "fft_create: unknown flags %d", flags);
     FFTPlan *P = new FFTPlan();
     for (int k = 0; k < 3; k++) P->n[k] = n[k];
@@ -414,14 +431,14 @@ extern "C" int ppgpu_fft_potential2forces(void *handle, const float *V, const fl
     sp.sF = 2 * M_PI * dV / detLinv / (double)P->N;
     const int with_e = (flags & PPGPU_FF_WITH_E) ? 1 : 0, acc = (flags & PPGPU_FF_ACCUMULATE) ? 1 : 0;
     if (P->f64) {
-        spectra_kernel<cufftDoubleComplex><<<blocks_for(P->Nh), FFT_THREADS, 0, st>>>(
+        spectra_kernel<cufftDoubleComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>(
             (const cufftDoubleComplex *)P->Vk, (const cufftDoubleComplex *)P->Rk, (cufftDoubleComplex *)P->S4, P->Nh, sp);
         PPGPU_CHECK_LAUNCH("spectra_kernel");
         PPGPU_CUFFT(cufftExecZ2D(P->c2r4, (cufftDoubleComplex *)P->S4, (double *)P->planar), "inverse x4");
         pack_fe_kernel<double><<<blocks_for(P->N), FFT_THREADS, 0, st>>>((float4 *)FE, (const double *)P->planar, P->N,
                                                                           scale, with_e, acc);
     } else {
-        spectra_kernel<cufftComplex><<<blocks_for(P->Nh), FFT_THREADS, 0, st>>>(
+        spectra_kernel<cufftComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>(
             (const cufftComplex *)P->Vk, (const cufftComplex *)P->Rk, (cufftComplex *)P->S4, P->Nh, sp);
         PPGPU_CHECK_LAUNCH("spectra_kernel");
         PPGPU_CUFFT(cufftExecC2R(P->c2r4, (cufftComplex *)P->S4, (cufftReal *)P->planar), "inverse x4");
@@ -470,7 +487,7 @@ extern "C" int ppgpu_fft_density_power(void *handle, float *rho, double B, int f
         PPGPU_CHECK_LAUNCH("density_sums_kernel");
     }
     if (!fix_negative && B == 1.0) return set_ok();
-    density_power_kernel<<<blocks_for(P->N), FFT_THREADS, 0, st>>>(rho, P->N, P->sums, fix_negative, B);
+    density_power_kernel<<<blocks_for(P->N), FFT_THREADS, 0, st>>>(rho, P->N, P->sums, fix_negative, (float)B);
     PPGPU_CHECK_LAUNCH("density_power_kernel");
     return set_ok();
 }
@@ -498,13 +515,13 @@ extern "C" int ppgpu_fft_poisson(void *handle, const float *rho_charge, const do
         for (int c = 0; c < 3; c++) pp.b[3 * r + c] = 2 * M_PI * ci[3 * c + r];
     pp.s = 4 * M_PI * 14.399645 / (double)P->N;
     if (P->f64) {
-        poisson_kernel<cufftDoubleComplex><<<blocks_for(P->Nh), FFT_THREADS, 0, st>>>((cufftDoubleComplex *)P->Rk, P->Nh, pp);
+        poisson_kernel<cufftDoubleComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>((cufftDoubleComplex *)P->Rk, P->Nh, pp);
         PPGPU_CHECK_LAUNCH("poisson_kernel");
         PPGPU_CUFFT(cufftExecZ2D(P->c2r1, (cufftDoubleComplex *)P->Rk, stage), "inverse V");
         f64_to_f32_kernel<<<blocks_for(P->N), FFT_THREADS, 0, st>>>(V, stage, P->N);
         PPGPU_CHECK_LAUNCH("f64_to_f32_kernel");
     } else {
-        poisson_kernel<cufftComplex><<<blocks_for(P->Nh), FFT_THREADS, 0, st>>>((cufftComplex *)P->Rk, P->Nh, pp);
+        poisson_kernel<cufftComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>((cufftComplex *)P->Rk, P->Nh, pp);
         PPGPU_CHECK_LAUNCH("poisson_kernel");
         PPGPU_CUFFT(cufftExecC2R(P->c2r1, (cufftComplex *)P->Rk, (cufftReal *)V), "inverse V");
     }
