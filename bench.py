@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap", "molecule_batch"])
     ap.add_argument("--nmol", type=int, default=256)
+    ap.add_argument("--tuning", default=None, help="molecule_batch launch shape 'ctas_per_sm,tile_w,tile_h,chunk' (default: autotuned)")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0)
@@ -252,13 +253,16 @@ class BatchBench:
     molecule) replayed from a CUDA graph, launch shape from the autotuner.  Also times the
     plain GPU form (one HighLevel.Pipeline per molecule) for comparison."""
 
-    def __init__(self, systems, relax, HL, torch):
+    def __init__(self, systems, relax, HL, torch, tuning=None):
         from ppafm_gb300 import batch as BT
 
         self.w = systems[0]
         self.systems = systems
         self.torch = torch
-        self.tuning, self.tune_ms = BT.autotune(systems, self.w, relax, reps=2)
+        if tuning is None:
+            self.tuning, self.tune_ms = BT.autotune(systems, self.w, relax, reps=2)
+        else:
+            self.tuning, self.tune_ms = tuple(tuning), None
         self.pl = BT.BatchPipeline(systems, self.w, relax=relax, want_ppos=True, tuning=self.tuning)
         self.pl.capture()
         self.units = self.pl.pixel_z
@@ -330,7 +334,8 @@ def run_batch(args, rank, world, local):
     systems = workloads.molecule_batch(seed=args.seed + rank, nmol=args.nmol, scale=args.scale)
     w = systems[0]
     relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
-    job = BatchBench(systems, relax, HL, torch)
+    tuning = [int(x) for x in args.tuning.split(",")] if args.tuning else None
+    job = BatchBench(systems, relax, HL, torch, tuning=tuning)
     job.HL = HL
     st = torch.cuda.current_stream()
 

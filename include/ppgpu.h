@@ -225,6 +225,12 @@ int ppgpu_batch_info(void *handle, long long *out4);
 int ppgpu_batch_iterations(void *handle, unsigned long long *out, void *stream);
 int ppgpu_batch_destroy(void *handle);
 
+/* ------------------------------------------------------------ tensor-core self test
+ * D[128][N] (float32) = A[128][K] . B[N][K]^T with bf16 A, B (device, row-major), one tile
+ * on the tcgen05 tensor cores (K multiple of 16 up to 128, N multiple of 16 up to 256).
+ * No reference counterpart: checks the MMA building block of the warm-start network. */
+int ppgpu_tc_selftest(const void *A, const void *B, int K, int N, float *D, void *stream);
+
 /* -------------------------------------------------------------- grid utilities */
 /* Fz -> df along the last axis: out[c][j] = scale * sum_i F[c][j+i] * W[nw-1-i]. */
 int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const double *W, double scale, float *out,

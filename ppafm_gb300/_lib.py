@@ -76,6 +76,7 @@ SIGNATURES = {
     "ppgpu_batch_info": ([c_void_p, POINTER(c_longlong)], c_int),
     "ppgpu_batch_iterations": ([c_void_p, POINTER(c_ulonglong), c_void_p], c_int),
     "ppgpu_batch_destroy": ([c_void_p], c_int),
+    "ppgpu_tc_selftest": ([c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p], c_int),
 }
 
 
