@@ -231,6 +231,22 @@ int ppgpu_batch_destroy(void *handle);
  * No reference counterpart: checks the MMA building block of the warm-start network. */
 int ppgpu_tc_selftest(const void *A, const void *B, int K, int N, float *D, void *stream);
 
+/* ------------------------------------------------------------ warm-start network
+ * No reference counterpart.  A 96 -> 128 -> 128 -> 16 SiLU MLP (bf16 weights and activations,
+ * float32 accumulation) on the tcgen05 tensor cores; float32 master parameters (layout:
+ * W1 [96][128] | W2 [128][128] | W3 [128][16] | b1 [128] | b2 [128] | b3 [16]) with Adam.
+ * X rows: 96 bf16 (84 features + 12 zeros); T rows: 4 f32 (3 targets); Y rows: 16 f32. */
+int ppgpu_mlp_create(unsigned long long seed, void **handle);
+int ppgpu_mlp_destroy(void *handle);
+int ppgpu_mlp_nparams(void);
+int ppgpu_mlp_get(void *handle, int which, float *host); /* 0 params, 1 grads, 2/3 Adam moments */
+int ppgpu_mlp_set(void *handle, const float *host);
+int ppgpu_mlp_forward(void *handle, const void *X, int n, float *Y, void *stream);
+int ppgpu_mlp_backward(void *handle, const void *X, const float *T, const int *idx, int nbatch, void *stream);
+int ppgpu_mlp_adam(void *handle, double lr, int step, void *stream);
+int ppgpu_mlp_take_loss(void *handle, double *out, void *stream);
+int ppgpu_mlp_views(void *handle, void **out8);
+
 /* -------------------------------------------------------------- grid utilities */
 /* Fz -> df along the last axis: out[c][j] = scale * sum_i F[c][j+i] * W[nw-1-i]. */
 int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const double *W, double scale, float *out,

@@ -77,6 +77,16 @@ SIGNATURES = {
     "ppgpu_batch_iterations": ([c_void_p, POINTER(c_ulonglong), c_void_p], c_int),
     "ppgpu_batch_destroy": ([c_void_p], c_int),
     "ppgpu_tc_selftest": ([c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p], c_int),
+    "ppgpu_mlp_create": ([c_ulonglong, POINTER(c_void_p)], c_int),
+    "ppgpu_mlp_destroy": ([c_void_p], c_int),
+    "ppgpu_mlp_nparams": ([], c_int),
+    "ppgpu_mlp_get": ([c_void_p, c_int, POINTER(c_float)], c_int),
+    "ppgpu_mlp_set": ([c_void_p, POINTER(c_float)], c_int),
+    "ppgpu_mlp_forward": ([c_void_p, c_void_p, c_int, c_void_p, c_void_p], c_int),
+    "ppgpu_mlp_backward": ([c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p], c_int),
+    "ppgpu_mlp_adam": ([c_void_p, c_double, c_int, c_void_p], c_int),
+    "ppgpu_mlp_take_loss": ([c_void_p, POINTER(c_double), c_void_p], c_int),
+    "ppgpu_mlp_views": ([c_void_p, POINTER(c_void_p)], c_int),
 }
 
 

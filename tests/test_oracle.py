@@ -208,3 +208,20 @@ def test_gaussian_density_kat(oracle):
     assert np.isclose(rho[0, 0, k], w / ((2 * np.pi) ** 1.5 * s**3), rtol=1e-12)
     assert np.isclose(rho.sum() * (L / n) ** 3, w, rtol=1e-6)
     assert np.isclose(rho[1, 0, k], rho[-1, 0, k], rtol=1e-12)  # minimum image across x = 0
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    """The float64 restatement's backward against central differences of its loss."""
+    from oracle import mlp_oracle as MO
+
+    rng = np.random.default_rng(0)
+    P = rng.normal(0, 0.2, MO.NPARAM)
+    X = rng.normal(0, 1, (5, 96))
+    X[:, 84:] = 0
+    T = rng.normal(0, 1, (5, 4))
+    _, G = MO.loss_and_grad(P, X, T, bf=False)
+    for i in rng.choice(MO.NPARAM, 40, replace=False):
+        d = np.zeros_like(P)
+        d[i] = 1e-6
+        fd = (MO.loss_and_grad(P + d, X, T, False)[0] - MO.loss_and_grad(P - d, X, T, False)[0]) / 2e-6
+        assert abs(fd - G[i]) <= 1e-5 * (abs(G[i]) + 1e-3)
