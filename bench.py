@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap", "molecule_batch"])
     ap.add_argument("--nmol", type=int, default=256)
+    ap.add_argument("--no-learned", action="store_true", help="molecule_batch: skip the learned warm start")
     ap.add_argument("--tuning", default=None, help="molecule_batch launch shape 'ctas_per_sm,tile_w,tile_h,chunk' (default: autotuned)")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -300,6 +301,66 @@ class BatchBench:
         self.torch.cuda.current_stream().synchronize()
         return h2d, d2h
 
+    def learned(self, args, plain_loop_ms, steps=3000):
+        """Config-4 line: train the warm-start network on plain-FIRE pairs of a held-out batch
+        (every 4th stroke of 256 other molecules: ~21M pairs; Adam, lr 1e-3, batch 8192), then
+        time the height-synchronous batched run with it (CUDA graph) against plain FIRE."""
+        import torch
+
+        from ppafm_gb300 import workloads
+        from ppafm_gb300.warmstart import WarmStartNet, generate_pairs
+
+        held = workloads.molecule_batch(seed=args.seed + 1000, nmol=args.nmol, scale=args.scale)
+        t0 = time.perf_counter()
+        X, T = generate_pairs(held, self.w, self.relax, stride=4, tuning=self.tuning)
+        torch.cuda.synchronize()
+        t_gen = time.perf_counter() - t0
+        net = WarmStartNet(seed=0)
+        t0 = time.perf_counter()
+        log = net.train(X, T, steps=steps, batch=8192, lr=1e-3, log_every=steps // 3)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        npairs = int(X.shape[0])
+        del X, T, held
+        pl = self.BT.BatchPipeline(self.systems, self.w, relax=self.relax, want_ppos=False, want_iters=True, tuning=self.tuning)
+
+        def its():
+            return np.concatenate([pl.outputs(j)["iters"].cpu().numpy().ravel() for j in range(len(self.systems))])
+
+        def dfs():
+            return [pl.outputs(j)["df"].cpu().numpy().copy() for j in range(len(self.systems))]
+
+        pl.run()
+        torch.cuda.synchronize()
+        it_plain, df_plain = its(), dfs()
+        ms = {}
+        for name, fn in (("learned", lambda: pl.run_layered(net)), ("layered_plain", lambda: pl.run_layered(None))):
+            g = pl.capture(fn)
+            g.replay()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(args.steps):
+                g.replay()
+            b.record()
+            b.synchronize()
+            ms[name] = a.elapsed_time(b) / args.steps
+            if name == "learned":
+                it_l, df_l = its(), dfs()
+        dd = np.concatenate([np.abs(x - y).ravel() for x, y in zip(df_l, df_plain)])
+        net.close()
+        pl.close()
+        return {
+            "ms_per_step": ms["learned"],
+            "value": self.units / (ms["learned"] * 1e-3),
+            "speedup_vs_plain_gpu_loop": plain_loop_ms / ms["learned"],
+            "layered_plain_ms_per_step": ms["layered_plain"],
+            "fire_iters_per_pixel_z": {"plain_mean": float(it_plain.mean()), "plain_p99": float(np.percentile(it_plain, 99)), "learned_mean": float(it_l.mean()), "learned_p99": float(np.percentile(it_l, 99))},
+            "df_vs_plain_fire": {"frac_over_0.1Hz": float((dd > 0.1).mean()), "p99.9_Hz": float(np.quantile(dd, 0.999)), "max_Hz": float(dd.max())},
+            "training": {"pairs": npairs, "steps": steps, "batch": 8192, "lr": 1e-3, "generate_s": t_gen, "train_s": t_train, "loss": log},
+        }
+
     def plain_ms(self, reps=2):
         pls = self.BT.plain_loop(self.systems, self.w, self.relax)
         torch = self.torch
@@ -384,6 +445,9 @@ def run_batch(args, rank, world, local):
             torch.distributed.destroy_process_group()
         return None
     plain = job.plain_ms()
+    learned = None
+    if not args.no_learned:
+        learned = job.learned(args, plain)
     peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
     flops = job.pairs * FLOPS_LJC_PAIR
     line = {
@@ -412,6 +476,7 @@ def run_batch(args, rank, world, local):
             "parallelism": f"replicas x{world}",
         },
         "plain_gpu_loop": {"ms_per_step": plain, "value": job.units / (plain * 1e-3), "speedup_of_batched": plain / (1e3 * t_step_max / K)},
+        "learned_warm_start": learned,
         "fire_iters_per_pixel_z": iters / job.units,
         "e2e": {"value": job.units * world * K / t_e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": job.launches_per_step * K,

@@ -224,6 +224,15 @@ int ppgpu_batch_info(void *handle, long long *out4);
 /* FIRE iterations of the last run (synchronises the stream). */
 int ppgpu_batch_iterations(void *handle, unsigned long long *out, void *stream);
 int ppgpu_batch_destroy(void *handle);
+/* Height-synchronous run with an optional warm-start network (ppgpu_mlp_*; NULL = plain FIRE
+ * from the height above): for each height the network proposes every stroke's starting
+ * displacement and FIRE starts from the proposal unless its force residual exceeds the plain
+ * start's.  rec_stride > 0 records training pairs of strokes gs % rec_stride == 0 at sample
+ * (gs / rec_stride) * nz_max + iz: rec_x [.][96] bf16 features, rec_t [.][4] f32 targets.
+ * Allocates its state buffers on the first call only; no host synchronisation. */
+int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, void *rec_x, void *rec_t, void *stream);
+/* out2 = (strokes including tile padding, largest nz). */
+int ppgpu_batch_layer_info(void *handle, long long *out2);
 
 /* ------------------------------------------------------------ tensor-core self test
  * D[128][N] (float32) = A[128][K] . B[N][K]^T with bf16 A, B (device, row-major), one tile

@@ -110,18 +110,27 @@ class BatchPipeline:
     def run(self, stream=None):
         check(lib().ppgpu_batch_run(self.handle, stream_handle(stream)))
 
-    def capture(self):
-        """Records one run in a CUDA graph; replay() launches it."""
+    def run_layered(self, net=None, record=None, stream=None):
+        """Height-synchronous run: with a WarmStartNet the learned warm start, without it plain
+        FIRE (same results as run()).  record = (stride, X, T) stores training pairs."""
+        mlp = net.handle if net is not None else None
+        stride, X, T = record if record is not None else (0, None, None)
+        check(lib().ppgpu_batch_run_layered(self.handle, mlp, int(stride), None if X is None else ctypes.c_void_p(X.data_ptr()), None if T is None else ctypes.c_void_p(T.data_ptr()), stream_handle(stream)))
+
+    def capture(self, fn=None):
+        """Records one run (or fn(), e.g. lambda: self.run_layered(net)) in a CUDA graph;
+        replay() launches it."""
+        fn = fn or self.run
         torch.cuda.synchronize()
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
-            self.run(s)  # warm-up outside the capture (lazy module loading)
+            fn()  # warm-up outside the capture (lazy module loading, first-use buffers)
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
-            self.run()
+            fn()
         return self.graph
 
     def replay(self):

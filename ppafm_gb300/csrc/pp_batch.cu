@@ -34,6 +34,7 @@
 #include "pp_common.cuh"
 #include "pp_df.cuh"
 #include "pp_ff_dev.cuh"
+#include "pp_mlp_dev.cuh"
 #include "pp_relax_dev.cuh"
 
 namespace ppgpu {
@@ -349,16 +350,310 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const BatchPrm 
     relax_phase(B);
 }
 
+// ------------------------------------------------------------ height-synchronous mode
+//
+// The learned warm start needs every stroke of a height at once (its network runs on 128-row
+// tiles), so this mode walks the heights in lockstep: for each height iz, the proposal kernel
+// computes the network's starting displacement of every stroke, then the height kernel runs
+// FIRE for every stroke from the better of the two starts (plain: the displacement converged
+// at the height above; learned: that plus the proposal) -- better = smaller initial force
+// residual, so a bad proposal falls back to the plain start.  With no network the height
+// kernel starts plain and reproduces the flattened kernel's result stroke for stroke.
+
+struct LayerPrm {
+    int iz, nz_max;
+    dfl *state;                // [nstrokes][3] displacement after the last finished height
+    float4 *prop;              // [nstrokes] proposed change of the displacement (NULL: plain)
+    unsigned char *rec_x;      // training features [samples][96] bf16 (NULL: not recorded)
+    float4 *rec_t;             // training targets [samples]: OUT_SCALE * (d_converged - d_start_plain)
+    int rec_stride;            // strokes gs % rec_stride == 0 are recorded, sample (gs / stride) * nz_max + iz
+    unsigned long long *pool;  // this height's stroke counter
+    int *tile_ctr;             // this height's proposal tile counter
+};
+
+// Tip, grid cell and fraction of global stroke gs at height iz; false for tile padding and for
+// heights beyond the system's scan.
+struct StrokeAt {
+    int job, ix, iy, nz;
+    dfl tip[3];
+    int base[3];
+    dfl tf[3];
+};
+__device__ __forceinline__ bool stroke_at(const BatchPrm &B, long long gs, int iz, StrokeAt &A) {
+    const int j = find_job_stroke(B, gs);
+    const BatchJob &J = B.jobs[j];
+    const long long s = gs - J.stroke0;
+    const int tsz = J.tw * J.th;
+    const long long tile = s / tsz;
+    const int r = (int)(s - tile * tsz);
+    const int tx = (int)(tile / J.nty), ty = (int)(tile - (long long)tx * J.nty);
+    A.ix = tx * J.tw + r / J.th;
+    A.iy = ty * J.th + r % J.th;
+    if (A.ix >= J.nx || A.iy >= J.ny || iz >= J.nz) return false;
+    A.job = j;
+    A.nz = J.nz;
+    A.tip[0] = J.xs[A.ix];
+    A.tip[1] = J.ys[A.iy];
+    A.tip[2] = J.zs[iz];
+    const dfl g[3] = {df_mul(J.dic[0], A.tip[0]), df_mul(J.dic[1], A.tip[1]), df_mul(J.dic[2], A.tip[2])};
+    tip_cell(g, A.base, A.tf);
+    return true;
+}
+
+__device__ __forceinline__ void load_prev(const BatchPrm &B, const LayerPrm &L, long long gs, dfl d[3]) {
+    if (L.iz == 0) {
+        d[0] = B.R.r0[0];
+        d[1] = B.R.r0[1];
+        d[2] = B.R.r0[2];
+    } else {
+        d[0] = L.state[3 * gs];
+        d[1] = L.state[3 * gs + 1];
+        d[2] = L.state[3 * gs + 2];
+    }
+}
+
+// Proposal kernel: features of every stroke at height iz (recorded for training when asked)
+// and, with a network, its proposed displacement change.  Persistent CTAs of 128 threads
+// take tiles of 128 strokes; the weights stay in shared memory.
+template <bool NET>
+__global__ void __launch_bounds__(128, 2) propose_kernel(const BatchPrm B, const LayerPrm L, const MLPTiles W) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tbase;
+    __shared__ long long s_tile;
+    unsigned char *sW1t = sm, *sW2t = sW1t + TILE_W1T, *sW3t = sW2t + TILE_W2T, *act = NET ? sW3t + TILE_W3T : sm;
+    const int tid = threadIdx.x;
+    if (NET) {
+        copy_tile(sW1t, W.W1t, TILE_W1T);
+        copy_tile(sW2t, W.W2t, TILE_W2T);
+        copy_tile(sW3t, W.W3t, TILE_W3T);
+        if (tid == 0) tc_mbar_init(&bar);
+        if (tid < 32) tmem_alloc(&tbase, 128);
+    }
+    cta_handoff();
+    uint32_t ph = 0;
+    bool ok = true;
+    const long long ntiles = (B.nstrokes + 127) / 128;
+    while (true) {
+        if (tid == 0) s_tile = atomicAdd(L.tile_ctr, 1);
+        __syncthreads();
+        const long long tile = s_tile;
+        __syncthreads();
+        if (tile >= ntiles) break;
+        const long long gs = tile * 128 + tid;
+        StrokeAt A;
+        dfl d[3];
+        const bool valid = gs < B.nstrokes && stroke_at(B, gs, L.iz, A);
+        if (valid) {
+            load_prev(B, L, gs, d);
+            const BatchJob &J = B.jobs[A.job];
+            dfl u[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(J.dic[k], d[k]));
+            const float3 dr = make_float3(df_round(df_add(d[0], B.R.nr0[0])), df_round(df_add(d[1], B.R.nr0[1])),
+                                          df_round(df_add(d[2], B.R.nr0[2])));
+            warm_features<false>(J.FE, J.n0, J.n1, J.n2, A.base, u, dr, act, tid);
+            if (L.rec_x && gs % L.rec_stride == 0) {
+                const long long slot = (gs / L.rec_stride) * L.nz_max + L.iz;
+                int4 *dst = reinterpret_cast<int4 *>(L.rec_x + slot * (MLP_IN * 2));
+#pragma unroll
+                for (int g = 0; g < MLP_IN / 8; g++) dst[g] = *reinterpret_cast<const int4 *>(act + tile_off(tid, 8 * g, MLP_IN));
+            }
+        } else if (NET) {
+            const float z[16] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k0 = 0; k0 < MLP_IN; k0 += 16) store16_bf16(act, tid, k0, z, MLP_IN);
+        }
+        if (NET) {
+            cta_handoff();
+            float y[16];
+            ok &= mlp_forward(act, sW1t, sW2t, sW3t, W.b1, W.b2, W.b3, tbase, &bar, ph, y);
+            if (valid)
+                L.prop[gs] = make_float4(y[0] * (1.f / OUT_SCALE), y[1] * (1.f / OUT_SCALE), y[2] * (1.f / OUT_SCALE), 0.f);
+        }
+    }
+    if (NET) {
+        if (!ok && tid == 0) raise_device_error(B.err, PPGPU_ERR_DEVICE_TIMEOUT);
+        tc_fence_before();
+        __syncthreads();
+        if (tid < 32) tmem_dealloc(tbase, 128);
+    }
+}
+
+// |f|^2 of the probe-particle force at displacement d (the residual FIRE starts from); the
+// grid force there is returned in F for FIRE's first step.
+__device__ __forceinline__ float residual2(const BatchPrm &B, const BatchJob &J, const StrokeAt &A, const dfl d[3],
+                                           dfl F[3]) {
+    dfl u[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(J.dic[k], d[k]));
+    interp_force_df<false>(J.FE, J.n0, J.n1, J.n2, A.base, u, F);
+    const float3 f = pp_force_df(B.R, F, d);
+    return f.x * f.x + f.y * f.y + f.z * f.z;
+}
+
+// Height kernel: FIRE at height iz for every stroke of the pool, lanes refilled as in the
+// flattened kernel.  Writes the height's outputs and the converged displacement (state).
+__global__ void __launch_bounds__(BATCH_THREADS) layer_relax_kernel(const BatchPrm B, const LayerPrm L) {
+    const int lane = threadIdx.x & 31;
+    const RelaxPrm &P = B.R;
+    StrokeAt A;
+    long long gs = -1;
+    bool has = false;
+    // Every trip does one gather.  phase 0: the learned start dm is evaluated (its residual
+    // and probe-particle force kept); phase 1: the plain start d0 is evaluated, the better
+    // one chosen and FIRE's first move made from it in the same trip; phase 2: FIRE.
+    int phase = 2;
+    dfl d[3], d0[3], dm[3];
+    float3 fm = make_float3(0.f, 0.f, 0.f);
+    float rm = 0.f;
+    float3 v = make_float3(0.f, 0.f, 0.f);
+    float dt = 0.f, acoef = 0.f;
+    int it = 0, itcount = 0;
+    bool fin = false;
+    long long pool_next = 0, pool_end = 0;
+    bool drained = false;
+    unsigned long long mine = 0;
+    const int chunk = B.chunk;
+    while (true) {
+        unsigned need = __ballot_sync(FULL, !has);
+        while (need && !drained) {
+            if (pool_next >= pool_end) {
+                unsigned long long g = 0;
+                if (lane == 0) g = atomicAdd(L.pool, (unsigned long long)chunk);
+                g = __shfl_sync(FULL, g, 0);
+                if ((long long)g >= B.nstrokes) {
+                    drained = true;
+                    break;
+                }
+                pool_next = (long long)g;
+                pool_end = min(pool_next + (long long)chunk, B.nstrokes);
+            }
+            const int rank = __popc(need & ((1u << lane) - 1u));
+            const int take = (int)min((long long)__popc(need), pool_end - pool_next);
+            if (((need >> lane) & 1u) && rank < take) {
+                gs = pool_next + rank;
+                if (stroke_at(B, gs, L.iz, A)) {
+                    load_prev(B, L, gs, d0);
+#pragma unroll
+                    for (int k = 0; k < 3; k++) d[k] = d0[k];
+                    phase = 2;
+                    if (L.prop && P.maxIters > 0) {
+                        const float4 q = L.prop[gs];
+                        dm[0] = df_add_f(d0[0], q.x);
+                        dm[1] = df_add_f(d0[1], q.y);
+                        dm[2] = df_add_f(d0[2], q.z);
+                        phase = 0;
+                    }
+                    v = make_float3(0.f, 0.f, 0.f);
+                    dt = P.dtmaxf;
+                    acoef = P.acoef0f;
+                    it = 0;
+                    itcount = 0;
+                    fin = P.maxIters <= 0;
+                    has = true;
+                }
+            }
+            pool_next += take;
+            need = __ballot_sync(FULL, !has);
+        }
+        if (!__any_sync(FULL, has)) break;
+        if (has) {
+            const BatchJob &J = B.jobs[A.job];
+            dfl de[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) de[k] = (phase == 0) ? dm[k] : d[k];
+            dfl u[3], F[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(J.dic[k], de[k]));
+            interp_force_df<false>(J.FE, J.n0, J.n1, J.n2, A.base, u, F);
+            if (fin) {
+                const long long pix = (long long)A.ix * J.ny + A.iy;
+                const long long o = pix * A.nz + (A.nz - 1 - L.iz);
+                if (J.fzs) J.fzs[o] = df_round(F[2]);
+                if (J.ppos) {
+#pragma unroll
+                    for (int k = 0; k < 3; k++) J.ppos[3 * o + k] = df_round(df_add(df_add(A.tip[k], d[k]), J.offd[k]));
+                }
+                if (J.iters) J.iters[o] = itcount;
+                L.state[3 * gs] = d[0];
+                L.state[3 * gs + 1] = d[1];
+                L.state[3 * gs + 2] = d[2];
+                if (L.rec_t && gs % L.rec_stride == 0) {
+                    const long long slot = (gs / L.rec_stride) * L.nz_max + L.iz;
+                    L.rec_t[slot] = make_float4(OUT_SCALE * df_round(df_add(d[0], df_neg(d0[0]))),
+                                                OUT_SCALE * df_round(df_add(d[1], df_neg(d0[1]))),
+                                                OUT_SCALE * df_round(df_add(d[2], df_neg(d0[2]))), 0.f);
+                }
+                has = false;
+            } else {
+                float3 f = pp_force_df(P, F, de);
+                const float r = f.x * f.x + f.y * f.y + f.z * f.z;
+                if (phase == 0) {  // learned start evaluated; the plain one next trip
+                    fm = f;
+                    rm = r;
+                    phase = 1;
+                } else {
+                    if (phase == 1) {  // learned start unless its residual is larger
+                        if (rm <= r) {
+#pragma unroll
+                            for (int k = 0; k < 3; k++) d[k] = dm[k];
+                            f = fm;
+                        }
+                        phase = 2;
+                    }
+                    const float ff = relax_move_df(P, f, d, v, dt, acoef);
+                    mine++;
+                    if (ff < P.convF2f) {
+                        itcount = it;
+                        fin = true;
+                    } else if (++it >= P.maxIters) {
+                        itcount = P.maxIters;
+                        fin = true;
+                    }
+                }
+            }
+        }
+    }
+    add_iterations(B.iter_total, mine);
+}
+
+// Fz -> df along each stroke after the last height (np.convolve 'valid', Fz2df).
+__global__ void batch_df_kernel(const BatchPrm B) {
+    for (long long gs = blockIdx.x * (long long)blockDim.x + threadIdx.x; gs < B.nstrokes;
+         gs += (long long)gridDim.x * blockDim.x) {
+        StrokeAt A;
+        if (!stroke_at(B, gs, 0, A)) continue;
+        const BatchJob &J = B.jobs[A.job];
+        if (!J.df || !J.fzs || B.nw <= 0) continue;
+        const long long pix = (long long)A.ix * J.ny + A.iy;
+        const float *f = J.fzs + pix * A.nz;
+        const int nout = A.nz - B.nw + 1;
+        float *out = J.df + pix * nout;
+        for (int jj = 0; jj < nout; jj++) {
+            float acc = 0.f;
+            for (int i = 0; i < B.nw; i++) acc = fmaf(f[jj + i], B.W[B.nw - 1 - i], acc);
+            out[jj] = acc;
+        }
+    }
+}
+
 // --------------------------------------------------------------------------- host
 
 struct BatchHandle {
     int dev = 0;
     int njobs = 0;
     int ctas = 0;
+    int nz_max = 0;
     BatchPrm prm;
     void *dmem = nullptr;  // job table + coordinate tables + counters
     size_t ctr_bytes = 0;
     void *ctr_base = nullptr;
+    // height-synchronous mode (allocated on first use)
+    dfl *state = nullptr;
+    float4 *prop = nullptr;
+    unsigned long long *pools = nullptr;  // [nz_max] stroke counters
+    int *tiles = nullptr;                 // [nz_max] proposal tile counters
 };
 
 }  // namespace ppgpu
@@ -457,7 +752,10 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
     }
     B.nff_items = ff0;
     B.nstrokes = s0;
+    int nz_max = 0;
+    for (int j = 0; j < njobs; j++) nz_max = std::max(nz_max, jobs[j].nz);
     BatchHandle *H = new BatchHandle();
+    H->nz_max = nz_max;
     cudaGetDevice(&H->dev);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->dev);
@@ -531,6 +829,96 @@ extern "C" int ppgpu_batch_destroy(void *handle) {
     BatchHandle *H = (BatchHandle *)handle;
     if (!H) return set_ok();
     cudaFree(H->dmem);
+    cudaFree(H->state);
     delete H;
+    return set_ok();
+}
+
+/* Height-synchronous run (see layer_relax_kernel): force fields, then for each height the
+ * proposal kernel (with the network `mlp`, or features only when recording) and the height
+ * kernel, then df.  mlp NULL: plain FIRE from the height above (same results as
+ * ppgpu_batch_run).  rec_stride > 0: strokes gs % rec_stride == 0 record training pairs,
+ * sample (gs / rec_stride) * nz_max + iz: rec_x [.][96] bf16 features, rec_t [.][4] f32 targets
+ * OUT_SCALE (10/A) * (converged - plain start).  No host synchronisation (graph-capturable). */
+extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, void *rec_x, void *rec_t, void *stream) {
+    BatchHandle *H = (BatchHandle *)handle;
+    if (!H) return set_error(PPGPU_ERR_ARG, "batch_run_layered: null handle");
+    if (rec_stride < 0 || (rec_stride > 0 && (!rec_x || !rec_t)))
+        return set_error(PPGPU_ERR_ARG, "batch_run_layered: recording needs rec_x and rec_t");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long ns = H->prm.nstrokes;
+    const int nz = H->nz_max;
+    if (!H->state) {
+        const size_t b_state = sizeof(dfl) * 3 * (size_t)std::max(ns, 1LL), b_prop = sizeof(float4) * (size_t)std::max(ns, 1LL);
+        const size_t b_ctr = (sizeof(unsigned long long) + sizeof(int)) * (size_t)std::max(nz, 1);
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, b_state + b_prop + b_ctr + 64);
+        if (e != cudaSuccess) return cuda_fail(e, "batch layered buffers");
+        H->state = (dfl *)p;
+        H->prop = (float4 *)((char *)p + ((b_state + 15) / 16) * 16);
+        H->pools = (unsigned long long *)((char *)H->prop + b_prop);
+        H->tiles = (int *)(H->pools + std::max(nz, 1));
+    }
+    MLPTiles W;
+    memset(&W, 0, sizeof(W));
+    if (mlp) {
+        void *v[8];
+        int rc = ppgpu_mlp_views(mlp, v);
+        if (rc) return rc;
+        W.W1t = (const unsigned char *)v[0];
+        W.W2t = (const unsigned char *)v[1];
+        W.W3t = (const unsigned char *)v[2];
+        W.W3 = (const unsigned char *)v[3];
+        W.W2 = (const unsigned char *)v[4];
+        W.b1 = (const float *)v[5];
+        W.b2 = (const float *)v[6];
+        W.b3 = (const float *)v[7];
+    }
+    PPGPU_CUDA(cudaMemsetAsync(H->ctr_base, 0, H->ctr_bytes, st), "batch counters");
+    PPGPU_CUDA(cudaMemsetAsync(H->pools, 0, (sizeof(unsigned long long) + sizeof(int)) * (size_t)std::max(nz, 1), st),
+               "batch layer counters");
+    // force fields only (an empty stroke pool ends the relaxation phase at once)
+    BatchPrm Bff = H->prm;
+    Bff.nstrokes = 0;
+    batch_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(Bff);
+    PPGPU_CHECK_LAUNCH("batch_kernel (force fields)");
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->dev);
+    const int smem_net = TILE_W1T + TILE_W2T + TILE_W3T + TILE_ACT, smem_feat = 128 * MLP_IN * 2;
+    if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(propose_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_net), "propose smem");
+    const bool propose = mlp || rec_stride > 0;
+    for (int iz = 0; iz < nz; iz++) {
+        LayerPrm L;
+        memset(&L, 0, sizeof(L));
+        L.iz = iz;
+        L.nz_max = nz;
+        L.state = H->state;
+        L.prop = mlp ? H->prop : nullptr;
+        L.rec_x = rec_stride > 0 ? (unsigned char *)rec_x : nullptr;
+        L.rec_t = rec_stride > 0 ? (float4 *)rec_t : nullptr;
+        L.rec_stride = rec_stride > 0 ? rec_stride : 1;
+        L.pool = H->pools + iz;
+        L.tile_ctr = H->tiles + iz;
+        if (propose) {
+            if (mlp)
+                propose_kernel<true><<<2 * sms, 128, smem_net, st>>>(H->prm, L, W);
+            else
+                propose_kernel<false><<<2 * sms, 128, smem_feat, st>>>(H->prm, L, W);
+            PPGPU_CHECK_LAUNCH("propose_kernel");
+        }
+        layer_relax_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm, L);
+        PPGPU_CHECK_LAUNCH("layer_relax_kernel");
+    }
+    batch_df_kernel<<<2 * sms, 256, 0, st>>>(H->prm);
+    PPGPU_CHECK_LAUNCH("batch_df_kernel");
+    return set_ok();
+}
+
+/* out2 = (strokes incl. tile padding, largest nz): recorded samples = ceil(strokes/stride) * nz. */
+extern "C" int ppgpu_batch_layer_info(void *handle, long long *out2) {
+    BatchHandle *H = (BatchHandle *)handle;
+    if (!H || !out2) return set_error(PPGPU_ERR_ARG, "batch_layer_info: null argument");
+    out2[0] = H->prm.nstrokes;
+    out2[1] = H->nz_max;
     return set_ok();
 }

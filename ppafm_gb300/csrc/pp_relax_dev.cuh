@@ -149,41 +149,42 @@ __device__ __forceinline__ float3 pp_force_df(const RelaxPrm &P, const dfl F[3],
 // Returns |f|^2.
 __device__ __forceinline__ float relax_move_df(const RelaxPrm &P, float3 f, dfl d[3], float3 &v, float &dt,
                                                float &acoef) {
-    const float ff = f.x * f.x + f.y * f.y + f.z * f.z;
+    // explicitly rounded operations: the same bits in every kernel that inlines this
+    const float ff = __fmaf_rn(f.z, f.z, __fmaf_rn(f.y, f.y, __fmul_rn(f.x, f.x)));
     float h;
     if (P.relaxAlg == 1) {
-        const float vv = v.x * v.x + v.y * v.y + v.z * v.z;
-        const float vf = f.x * v.x + f.y * v.y + f.z * v.z;
+        const float vv = __fmaf_rn(v.z, v.z, __fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x)));
+        const float vf = __fmaf_rn(f.z, v.z, __fmaf_rn(f.y, v.y, __fmul_rn(f.x, v.x)));
         if (vf < 0.f) {
             v = make_float3(0.f, 0.f, 0.f);
-            dt = dt * P.fdecf;
+            dt = __fmul_rn(dt, P.fdecf);
             acoef = P.acoef0f;
         } else {
             // cf f has length acoef |v|; vv ff below 1e-30 gives cf = 0 instead of an
             // overflow (the reference divides by zero at ff == 0, and cf = 0 at vv == 0)
-            const float vf2 = vv * ff;  // sqrt(vv/ff) = vv / sqrt(vv ff)
-            const float cf = (vf2 > 1e-30f) ? acoef * vv * rsqrt_approx(vf2) : 0.f;
-            const float cv = 1.f - acoef;
-            v.x = fmaf(f.x, cf, v.x * cv);
-            v.y = fmaf(f.y, cf, v.y * cv);
-            v.z = fmaf(f.z, cf, v.z * cv);
-            dt = fminf(dt * P.fincf, P.dtmaxf);
-            acoef = acoef * P.falphaf;
+            const float vf2 = __fmul_rn(vv, ff);  // sqrt(vv/ff) = vv / sqrt(vv ff)
+            const float cf = (vf2 > 1e-30f) ? __fmul_rn(__fmul_rn(acoef, vv), rsqrt_approx(vf2)) : 0.f;
+            const float cv = __fsub_rn(1.f, acoef);
+            v.x = __fmaf_rn(f.x, cf, __fmul_rn(v.x, cv));
+            v.y = __fmaf_rn(f.y, cf, __fmul_rn(v.y, cv));
+            v.z = __fmaf_rn(f.z, cf, __fmul_rn(v.z, cv));
+            dt = fminf(__fmul_rn(dt, P.fincf), P.dtmaxf);
+            acoef = __fmul_rn(acoef, P.falphaf);
         }
         h = dt;
     } else {
-        const float c = 1.f - P.acoef0f;
-        v.x *= c;
-        v.y *= c;
-        v.z *= c;
+        const float c = __fsub_rn(1.f, P.acoef0f);
+        v.x = __fmul_rn(v.x, c);
+        v.y = __fmul_rn(v.y, c);
+        v.z = __fmul_rn(v.z, c);
         h = P.dtmaxf;
     }
-    v.x = fmaf(f.x, h, v.x);
-    v.y = fmaf(f.y, h, v.y);
-    v.z = fmaf(f.z, h, v.z);
-    d[0] = df_add_f(d[0], v.x * h);
-    d[1] = df_add_f(d[1], v.y * h);
-    d[2] = df_add_f(d[2], v.z * h);
+    v.x = __fmaf_rn(f.x, h, v.x);
+    v.y = __fmaf_rn(f.y, h, v.y);
+    v.z = __fmaf_rn(f.z, h, v.z);
+    d[0] = df_add_f(d[0], __fmul_rn(v.x, h));
+    d[1] = df_add_f(d[1], __fmul_rn(v.y, h));
+    d[2] = df_add_f(d[2], __fmul_rn(v.z, h));
     return ff;
 }
 
