@@ -255,6 +255,8 @@ int ppgpu_mlp_backward(void *handle, const void *X, const float *T, const int *i
 int ppgpu_mlp_adam(void *handle, double lr, int step, void *stream);
 int ppgpu_mlp_take_loss(void *handle, double *out, void *stream);
 int ppgpu_mlp_views(void *handle, void **out8);
+/* Loss weights of the three outputs (default 1): loss = mean over samples of sum_o w_o (y_o - t_o)^2. */
+int ppgpu_mlp_set_loss_weights(void *handle, const double *w3);
 
 /* -------------------------------------------------------------- grid utilities */
 /* Fz -> df along the last axis: out[c][j] = scale * sum_i F[c][j+i] * W[nw-1-i]. */

@@ -89,6 +89,7 @@ SIGNATURES = {
     "ppgpu_mlp_adam": ([c_void_p, c_double, c_int, c_void_p], c_int),
     "ppgpu_mlp_take_loss": ([c_void_p, POINTER(c_double), c_void_p], c_int),
     "ppgpu_mlp_views": ([c_void_p, POINTER(c_void_p)], c_int),
+    "ppgpu_mlp_set_loss_weights": ([c_void_p, _dp], c_int),
 }
 
 

@@ -75,6 +75,7 @@ struct BatchCtr {  // reset before every run
 
 struct BatchPrm {
     const BatchJob *jobs;
+    const int2 *stab;  // [nstrokes] (system, ix << 16 | iy); system -1 for tile padding
     int njobs;
     long long nff_items;
     long long nstrokes;
@@ -101,17 +102,6 @@ __device__ __forceinline__ int find_job_ff(const BatchPrm &B, long long item) {
     return lo;
 }
 
-__device__ __forceinline__ int find_job_stroke(const BatchPrm &B, long long s) {
-    int lo = 0, hi = B.njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (B.jobs[mid].stroke0 <= s)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    return lo;
-}
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
     int v;
@@ -178,16 +168,13 @@ __device__ __forceinline__ void stroke_height(Stroke &S, const BatchJob &J) {
 
 // Starts global stroke gs; false if it is tile padding outside the scan (no work).
 __device__ __forceinline__ bool stroke_start(Stroke &S, const BatchPrm &B, long long gs) {
-    const int j = find_job_stroke(B, gs);
+    const int2 e = B.stab[gs];
+    if (e.x < 0) return false;
+    const int j = e.x;
     const BatchJob &J = B.jobs[j];
-    const long long s = gs - J.stroke0;
-    const int tsz = J.tw * J.th;
-    const long long tile = s / tsz;
-    const int r = (int)(s - tile * tsz);
-    const int tx = (int)(tile / J.nty), ty = (int)(tile - (long long)tx * J.nty);
-    S.ix = tx * J.tw + r / J.th;
-    S.iy = ty * J.th + r % J.th;
-    if (S.ix >= J.nx || S.iy >= J.ny || J.nz <= 0) return false;
+    S.ix = e.y >> 16;
+    S.iy = e.y & 0xFFFF;
+    if (J.nz <= 0) return false;
     S.job = j;
     S.FE = J.FE;
     S.n0 = J.n0;
@@ -375,23 +362,30 @@ struct LayerPrm {
 // heights beyond the system's scan.
 struct StrokeAt {
     int job, ix, iy, nz;
+    const float4 *FE;  // the system's grid, size and metric (kept in registers)
+    int n0, n1, n2;
+    dfl dic[3];
     dfl tip[3];
     int base[3];
     dfl tf[3];
 };
 __device__ __forceinline__ bool stroke_at(const BatchPrm &B, long long gs, int iz, StrokeAt &A) {
-    const int j = find_job_stroke(B, gs);
+    const int2 e = B.stab[gs];
+    if (e.x < 0) return false;
+    const int j = e.x;
     const BatchJob &J = B.jobs[j];
-    const long long s = gs - J.stroke0;
-    const int tsz = J.tw * J.th;
-    const long long tile = s / tsz;
-    const int r = (int)(s - tile * tsz);
-    const int tx = (int)(tile / J.nty), ty = (int)(tile - (long long)tx * J.nty);
-    A.ix = tx * J.tw + r / J.th;
-    A.iy = ty * J.th + r % J.th;
-    if (A.ix >= J.nx || A.iy >= J.ny || iz >= J.nz) return false;
+    A.ix = e.y >> 16;
+    A.iy = e.y & 0xFFFF;
+    if (iz >= J.nz) return false;
     A.job = j;
     A.nz = J.nz;
+    A.FE = J.FE;
+    A.n0 = J.n0;
+    A.n1 = J.n1;
+    A.n2 = J.n2;
+    A.dic[0] = J.dic[0];
+    A.dic[1] = J.dic[1];
+    A.dic[2] = J.dic[2];
     A.tip[0] = J.xs[A.ix];
     A.tip[1] = J.ys[A.iy];
     A.tip[2] = J.zs[iz];
@@ -412,84 +406,130 @@ __device__ __forceinline__ void load_prev(const BatchPrm &B, const LayerPrm &L, 
     }
 }
 
-// Proposal kernel: features of every stroke at height iz (recorded for training when asked)
-// and, with a network, its proposed displacement change.  Persistent CTAs of 128 threads
-// take tiles of 128 strokes; the weights stay in shared memory.
-template <bool NET>
-__global__ void __launch_bounds__(128, 2) propose_kernel(const BatchPrm B, const LayerPrm L, const MLPTiles W) {
-    extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t bar;
-    __shared__ uint32_t tbase;
-    __shared__ long long s_tile;
-    unsigned char *sW1t = sm, *sW2t = sW1t + TILE_W1T, *sW3t = sW2t + TILE_W2T, *act = NET ? sW3t + TILE_W3T : sm;
-    const int tid = threadIdx.x;
-    if (NET) {
-        copy_tile(sW1t, W.W1t, TILE_W1T);
-        copy_tile(sW2t, W.W2t, TILE_W2T);
-        copy_tile(sW3t, W.W3t, TILE_W3T);
-        if (tid == 0) tc_mbar_init(&bar);
-        if (tid < 32) tmem_alloc(&tbase, 128);
+// Feature kernel: the network inputs of every stroke at height iz, 16 threads per stroke (one
+// per x-y node column of the 4x4x4 neighbourhood of the probe's cell, so the gathers of a
+// stroke are all in flight at once).  Rows go into input tiles of 128 strokes in the tensor
+// cores' K-major layout (tile gs / 128, row gs % 128); recorded training rows are copied
+// row-major.  Padding strokes get zero rows.
+constexpr int FEAT_STROKES = 16;  // strokes per 256-thread block
+__global__ void __launch_bounds__(256) feature_kernel(const BatchPrm B, const LayerPrm L, unsigned char *Xtiles) {
+    __shared__ float S[FEAT_STROKES][16][9];  // z-interpolated samples per column: [c][cz*3+comp]
+    const int g = threadIdx.x >> 4, c = threadIdx.x & 15;
+    const long long gs = (long long)blockIdx.x * FEAT_STROKES + g;
+    StrokeAt A;
+    dfl d[3];
+    float t[3] = {0.f, 0.f, 0.f};
+    const bool valid = gs < B.nstrokes && stroke_at(B, gs, L.iz, A);
+    if (valid) {
+        load_prev(B, L, gs, d);
+        const BatchJob &J = B.jobs[A.job];
+        int ci[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const dfl u = df_add(A.tf[k], df_mul(J.dic[k], d[k]));
+            const dfl tk = split_cell(u, ci[k]);
+            ci[k] += A.base[k];
+            t[k] = __fadd_rn(tk.h, tk.l);
+        }
+        const int px = c >> 2, py = c & 3;
+        const int ix = wrap_index(ci[0] - 1 + px, J.n0), iy = wrap_index(ci[1] - 1 + py, J.n1);
+        const float4 *col = J.FE + ((long long)ix * J.n1 + iy) * J.n2;
+        float4 q[4];
+#pragma unroll
+        for (int pz = 0; pz < 4; pz++) q[pz] = col[wrap_index(ci[2] - 1 + pz, J.n2)];
+#pragma unroll
+        for (int cz = 0; cz < 3; cz++) {
+            S[g][c][3 * cz + 0] = fmaf(t[2], q[cz + 1].x - q[cz].x, q[cz].x);
+            S[g][c][3 * cz + 1] = fmaf(t[2], q[cz + 1].y - q[cz].y, q[cz].y);
+            S[g][c][3 * cz + 2] = fmaf(t[2], q[cz + 1].z - q[cz].z, q[cz].z);
+        }
     }
-    cta_handoff();
-    uint32_t ph = 0;
-    bool ok = true;
-    const long long ntiles = (B.nstrokes + 127) / 128;
-    while (true) {
-        if (tid == 0) s_tile = atomicAdd(L.tile_ctr, 1);
-        __syncthreads();
-        const long long tile = s_tile;
-        __syncthreads();
-        if (tile >= ntiles) break;
-        const long long gs = tile * 128 + tid;
-        StrokeAt A;
-        dfl d[3];
-        const bool valid = gs < B.nstrokes && stroke_at(B, gs, L.iz, A);
+    __syncthreads();
+    __shared__ __align__(16) __nv_bfloat16 R[FEAT_STROKES][MLP_IN];  // the block's rows, stored as 16-byte chunks
+    float dr0 = 0.f, dr1 = 0.f, dr2 = 0.f;
+    if (valid) {
+        dr0 = FEAT_DSCALE * df_round(df_add(d[0], B.R.nr0[0]));
+        dr1 = FEAT_DSCALE * df_round(df_add(d[1], B.R.nr0[1]));
+        dr2 = FEAT_DSCALE * df_round(df_add(d[2], B.R.nr0[2]));
+    }
+#pragma unroll
+    for (int m = 0; m < MLP_IN / 16; m++) {
+        const int k = c + 16 * m;
+        float x = 0.f;
         if (valid) {
-            load_prev(B, L, gs, d);
-            const BatchJob &J = B.jobs[A.job];
-            dfl u[3];
+            if (k < 81) {
+                const int s = k / 3, comp = k - 3 * s;
+                const int a = s / 9, b = (s / 3) % 3, cz = s % 3;
+                float F = 0.f;
 #pragma unroll
-            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(J.dic[k], d[k]));
-            const float3 dr = make_float3(df_round(df_add(d[0], B.R.nr0[0])), df_round(df_add(d[1], B.R.nr0[1])),
-                                          df_round(df_add(d[2], B.R.nr0[2])));
-            warm_features<false>(J.FE, J.n0, J.n1, J.n2, A.base, u, dr, act, tid);
-            if (L.rec_x && gs % L.rec_stride == 0) {
-                const long long slot = (gs / L.rec_stride) * L.nz_max + L.iz;
-                int4 *dst = reinterpret_cast<int4 *>(L.rec_x + slot * (MLP_IN * 2));
+                for (int dx = 0; dx < 2; dx++)
 #pragma unroll
-                for (int g = 0; g < MLP_IN / 8; g++) dst[g] = *reinterpret_cast<const int4 *>(act + tile_off(tid, 8 * g, MLP_IN));
+                    for (int dy = 0; dy < 2; dy++) {
+                        const float w = (dx ? t[0] : 1.f - t[0]) * (dy ? t[1] : 1.f - t[1]);
+                        F = fmaf(w, S[g][4 * (a + dx) + (b + dy)][3 * cz + comp], F);
+                    }
+                x = tanh_fast(FEAT_FSCALE * F);
+            } else if (k < MLP_FEAT) {
+                x = (k == 81) ? dr0 : ((k == 82) ? dr1 : dr2);
             }
-        } else if (NET) {
-            const float z[16] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int k0 = 0; k0 < MLP_IN; k0 += 16) store16_bf16(act, tid, k0, z, MLP_IN);
         }
-        if (NET) {
-            cta_handoff();
-            float y[16];
-            ok &= mlp_forward(act, sW1t, sW2t, sW3t, W.b1, W.b2, W.b3, tbase, &bar, ph, y);
-            if (valid)
-                L.prop[gs] = make_float4(y[0] * (1.f / OUT_SCALE), y[1] * (1.f / OUT_SCALE), y[2] * (1.f / OUT_SCALE), 0.f);
-        }
+        R[g][k] = __float2bfloat16_rn(x);
     }
-    if (NET) {
-        if (!ok && tid == 0) raise_device_error(B.err, PPGPU_ERR_DEVICE_TIMEOUT);
-        tc_fence_before();
-        __syncthreads();
-        if (tid < 32) tmem_dealloc(tbase, 128);
+    __syncthreads();
+    // 16 strokes x 12 chunks of 8 values: one 16-byte store each (tile layout; row-major copy
+    // of the recorded training rows)
+    const long long npad = (B.nstrokes + 127) / 128 * 128;
+    for (int q = threadIdx.x; q < FEAT_STROKES * (MLP_IN / 8); q += blockDim.x) {
+        const int gg = q / (MLP_IN / 8), ch = q - gg * (MLP_IN / 8);
+        const long long gq = (long long)blockIdx.x * FEAT_STROKES + gg;
+        if (gq >= npad) continue;
+        const int4 v = *reinterpret_cast<const int4 *>(&R[gg][8 * ch]);
+        *reinterpret_cast<int4 *>(Xtiles + (gq >> 7) * (long long)(128 * MLP_IN * 2) + tile_off((int)(gq & 127), 8 * ch, MLP_IN)) = v;
+        if (L.rec_x && gq < B.nstrokes && gq % L.rec_stride == 0 && B.stab[gq].x >= 0 && L.iz < B.jobs[B.stab[gq].x].nz)
+            reinterpret_cast<int4 *>(L.rec_x + ((gq / L.rec_stride) * L.nz_max + L.iz) * (MLP_IN * 2))[ch] = v;
     }
 }
 
-// |f|^2 of the probe-particle force at displacement d (the residual FIRE starts from); the
-// grid force there is returned in F for FIRE's first step.
-__device__ __forceinline__ float residual2(const BatchPrm &B, const BatchJob &J, const StrokeAt &A, const dfl d[3],
-                                           dfl F[3]) {
-    dfl u[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(J.dic[k], d[k]));
-    interp_force_df<false>(J.FE, J.n0, J.n1, J.n2, A.base, u, F);
-    const float3 f = pp_force_df(B.R, F, d);
-    return f.x * f.x + f.y * f.y + f.z * f.z;
+// Inference kernel: persistent CTAs keep the weights in shared memory and run the network on
+// input tiles fetched by bulk copies; the proposal of stroke gs is OUT_SCALE^-1 * y[0..2].
+__global__ void __launch_bounds__(128, 2) infer_kernel(const BatchPrm B, const LayerPrm L, const MLPTiles W,
+                                                       const unsigned char *Xtiles) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint64_t bar_mma, bar_copy;
+    __shared__ uint32_t tbase;
+    unsigned char *sW1t = sm, *sW2t = sW1t + TILE_W1T, *sW3t = sW2t + TILE_W2T, *act = sW3t + TILE_W3T;
+    const int tid = threadIdx.x;
+    copy_tile(sW1t, W.W1t, TILE_W1T);
+    copy_tile(sW2t, W.W2t, TILE_W2T);
+    copy_tile(sW3t, W.W3t, TILE_W3T);
+    if (tid == 0) {
+        tc_mbar_init(&bar_mma);
+        tc_mbar_init(&bar_copy);
+    }
+    if (tid < 32) tmem_alloc(&tbase, 128);
+    cta_handoff();
+    uint32_t ph = 0, phc = 0;
+    bool ok = true;
+    const long long ntiles = (B.nstrokes + 127) / 128;
+    constexpr uint32_t XBYTES = 128 * MLP_IN * 2;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (tid == 0) {
+            fence_async_smem();  // earlier generic writes of act ordered before the async copy
+            mbar_expect_tx(&bar_copy, XBYTES);
+            bulk_g2s(act, Xtiles + tile * XBYTES, XBYTES, &bar_copy);
+        }
+        ok &= tc_mbar_wait(&bar_copy, phc);
+        phc ^= 1u;
+        float y[16];
+        ok &= mlp_forward(act, sW1t, sW2t, sW3t, W.b1, W.b2, W.b3, tbase, &bar_mma, ph, y);
+        const long long gs = tile * 128 + tid;
+        if (gs < B.nstrokes)
+            L.prop[gs] = make_float4(y[0] * (1.f / OUT_SCALE), y[1] * (1.f / OUT_SCALE), y[2] * (1.f / OUT_SCALE), 0.f);
+    }
+    if (!ok && tid == 0) raise_device_error(B.err, PPGPU_ERR_DEVICE_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (tid < 32) tmem_dealloc(tbase, 128);
 }
 
 // Height kernel: FIRE at height iz for every stroke of the pool, lanes refilled as in the
@@ -559,15 +599,15 @@ __global__ void __launch_bounds__(BATCH_THREADS) layer_relax_kernel(const BatchP
         }
         if (!__any_sync(FULL, has)) break;
         if (has) {
-            const BatchJob &J = B.jobs[A.job];
             dfl de[3];
 #pragma unroll
             for (int k = 0; k < 3; k++) de[k] = (phase == 0) ? dm[k] : d[k];
             dfl u[3], F[3];
 #pragma unroll
-            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(J.dic[k], de[k]));
-            interp_force_df<false>(J.FE, J.n0, J.n1, J.n2, A.base, u, F);
+            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(A.dic[k], de[k]));
+            interp_force_df<false>(A.FE, A.n0, A.n1, A.n2, A.base, u, F);
             if (fin) {
+                const BatchJob &J = B.jobs[A.job];
                 const long long pix = (long long)A.ix * J.ny + A.iy;
                 const long long o = pix * A.nz + (A.nz - 1 - L.iz);
                 if (J.fzs) J.fzs[o] = df_round(F[2]);
@@ -650,6 +690,7 @@ struct BatchHandle {
     size_t ctr_bytes = 0;
     void *ctr_base = nullptr;
     // height-synchronous mode (allocated on first use)
+    unsigned char *xtiles = nullptr;  // network input tiles of one height (allocation base)
     dfl *state = nullptr;
     float4 *prop = nullptr;
     unsigned long long *pools = nullptr;  // [nz_max] stroke counters
@@ -702,8 +743,9 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
         const double *c = h.cell;
         if (c[1] != 0.0 || c[2] != 0.0 || c[3] != 0.0 || c[5] != 0.0 || c[6] != 0.0 || c[7] != 0.0)
             return set_error(PPGPU_ERR_ARG, "batch job %d: the batched path needs an orthogonal (diagonal) cell", j);
-        if (h.nx < 0 || h.ny < 0 || h.nz < 0 || (h.nx * (long long)h.ny * h.nz > 0 && (!h.xs || !h.ys || !h.zs)))
-            return set_error(PPGPU_ERR_ARG, "batch job %d: bad scan", j);
+        if (h.nx < 0 || h.ny < 0 || h.nz < 0 || h.nx > 65535 || h.ny > 65535 ||
+            (h.nx * (long long)h.ny * h.nz > 0 && (!h.xs || !h.ys || !h.zs)))
+            return set_error(PPGPU_ERR_ARG, "batch job %d: bad scan (at most 65535 pixels per axis)", j);
         if (h.df && (nw <= 0 || nw > h.nz || !h.fzs))
             return set_error(PPGPU_ERR_ARG, "batch job %d: df needs 1 <= nw <= nz and fzs", j);
         GridGeom g;
@@ -762,10 +804,24 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
     H->ctas = sms * ctas_per_sm;
     H->njobs = njobs;
     // device memory: [jobs][tables][counters: BatchCtr | iter total | ff_done[njobs]]
+    // stroke table: the system and pixel of every stroke of the pool (tile order of each system)
+    std::vector<int2> stab((size_t)s0);
+    for (int j = 0; j < njobs; j++) {
+        const BatchJob &b = J[j];
+        const int tsz = b.tw * b.th;
+        for (long long s = 0; s < b.nstrokes; s++) {
+            const long long tile = s / tsz;
+            const int r = (int)(s - tile * tsz);
+            const int tx = (int)(tile / b.nty), ty = (int)(tile - (long long)tx * b.nty);
+            const int ix = tx * b.tw + r / b.th, iy = ty * b.th + r % b.th;
+            stab[b.stroke0 + s] = (ix < b.nx && iy < b.ny) ? make_int2(j, (ix << 16) | iy) : make_int2(-1, 0);
+        }
+    }
     const size_t jobs_b = ((sizeof(BatchJob) * njobs + 255) / 256) * 256;
     const size_t tabs_b = ((sizeof(dfl) * tabs.size() + 255) / 256) * 256;
+    const size_t stab_b = ((sizeof(int2) * stab.size() + 255) / 256) * 256;
     H->ctr_bytes = sizeof(BatchCtr) + sizeof(unsigned long long) + sizeof(int) * njobs;
-    cudaError_t e = cudaMalloc(&H->dmem, jobs_b + tabs_b + H->ctr_bytes);
+    cudaError_t e = cudaMalloc(&H->dmem, jobs_b + tabs_b + stab_b + H->ctr_bytes);
     if (e != cudaSuccess) {
         delete H;
         return cuda_fail(e, "batch tables");
@@ -779,13 +835,16 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
     }
     e = cudaMemcpy(base, J.data(), sizeof(BatchJob) * njobs, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !tabs.empty()) e = cudaMemcpy(dtabs, tabs.data(), sizeof(dfl) * tabs.size(), cudaMemcpyHostToDevice);
+    int2 *dstab = (int2 *)(base + jobs_b + tabs_b);
+    if (e == cudaSuccess && !stab.empty()) e = cudaMemcpy(dstab, stab.data(), sizeof(int2) * stab.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(H->dmem);
         delete H;
         return cuda_fail(e, "batch tables upload");
     }
-    H->ctr_base = base + jobs_b + tabs_b;
+    H->ctr_base = base + jobs_b + tabs_b + stab_b;
     B.jobs = (const BatchJob *)base;
+    B.stab = dstab;
     B.ctr = (BatchCtr *)H->ctr_base;
     B.iter_total = (unsigned long long *)((char *)H->ctr_base + sizeof(BatchCtr));
     B.ff_done = (int *)((char *)H->ctr_base + sizeof(BatchCtr) + sizeof(unsigned long long));
@@ -829,7 +888,7 @@ extern "C" int ppgpu_batch_destroy(void *handle) {
     BatchHandle *H = (BatchHandle *)handle;
     if (!H) return set_ok();
     cudaFree(H->dmem);
-    cudaFree(H->state);
+    cudaFree(H->xtiles);
     delete H;
     return set_ok();
 }
@@ -851,11 +910,13 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     if (!H->state) {
         const size_t b_state = sizeof(dfl) * 3 * (size_t)std::max(ns, 1LL), b_prop = sizeof(float4) * (size_t)std::max(ns, 1LL);
         const size_t b_ctr = (sizeof(unsigned long long) + sizeof(int)) * (size_t)std::max(nz, 1);
+        const size_t b_x = (size_t)((ns + 127) / 128) * 128 * MLP_IN * 2;
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, b_state + b_prop + b_ctr + 64);
+        cudaError_t e = cudaMalloc(&p, b_x + b_state + b_prop + b_ctr + 256);
         if (e != cudaSuccess) return cuda_fail(e, "batch layered buffers");
-        H->state = (dfl *)p;
-        H->prop = (float4 *)((char *)p + ((b_state + 15) / 16) * 16);
+        H->xtiles = (unsigned char *)p;
+        H->state = (dfl *)((char *)p + b_x);
+        H->prop = (float4 *)((char *)H->state + ((b_state + 15) / 16) * 16);
         H->pools = (unsigned long long *)((char *)H->prop + b_prop);
         H->tiles = (int *)(H->pools + std::max(nz, 1));
     }
@@ -884,9 +945,10 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     PPGPU_CHECK_LAUNCH("batch_kernel (force fields)");
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->dev);
-    const int smem_net = TILE_W1T + TILE_W2T + TILE_W3T + TILE_ACT, smem_feat = 128 * MLP_IN * 2;
-    if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(propose_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_net), "propose smem");
+    const int smem_net = TILE_W1T + TILE_W2T + TILE_W3T + TILE_ACT;
+    if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_net), "infer smem");
     const bool propose = mlp || rec_stride > 0;
+    const unsigned feat_blocks = (unsigned)((((ns + 127) / 128) * 128 + FEAT_STROKES - 1) / FEAT_STROKES);
     for (int iz = 0; iz < nz; iz++) {
         LayerPrm L;
         memset(&L, 0, sizeof(L));
@@ -899,12 +961,13 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
         L.rec_stride = rec_stride > 0 ? rec_stride : 1;
         L.pool = H->pools + iz;
         L.tile_ctr = H->tiles + iz;
-        if (propose) {
-            if (mlp)
-                propose_kernel<true><<<2 * sms, 128, smem_net, st>>>(H->prm, L, W);
-            else
-                propose_kernel<false><<<2 * sms, 128, smem_feat, st>>>(H->prm, L, W);
-            PPGPU_CHECK_LAUNCH("propose_kernel");
+        if (propose && ns > 0) {
+            feature_kernel<<<feat_blocks, 256, 0, st>>>(H->prm, L, H->xtiles);
+            PPGPU_CHECK_LAUNCH("feature_kernel");
+            if (mlp) {
+                infer_kernel<<<2 * sms, 128, smem_net, st>>>(H->prm, L, W, H->xtiles);
+                PPGPU_CHECK_LAUNCH("infer_kernel");
+            }
         }
         layer_relax_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm, L);
         PPGPU_CHECK_LAUNCH("layer_relax_kernel");

@@ -36,6 +36,7 @@ struct MLP {
     float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;  // params, grads, Adam moments
     unsigned char *tiles = nullptr;  // W1t | W2t | W3t | W3 | W2
     float *loss = nullptr;           // device scalar
+    float lw[3] = {1.f, 1.f, 1.f};   // per-output loss weights
     // per-batch transposed activation tiles for the weight gradients
     unsigned char *xt = nullptr, *h1t = nullptr, *h2t = nullptr, *dyt = nullptr, *dz2t = nullptr, *dz1t = nullptr;
     int cap_tiles = 0;  // CTAs (of 128 samples) the transposed buffers hold
@@ -107,7 +108,7 @@ constexpr int FB_SMEM = TILE_W1T + TILE_W2T + TILE_W3T + TILE_W3 + TILE_W2 + 128
 // bias gradients and the loss.  TMEM columns: Z1 [0,128), Z2 [128,256), Y [256,272),
 // dH2 [384,512), dH1 [128,256) (over Z2 once it is consumed).
 __global__ void __launch_bounds__(128, 1) mlp_fwd_bwd_kernel(MLPTiles W, const __nv_bfloat16 *X, const float4 *T,
-                                                             const int *idx, int nbatch, float *G, float *loss,
+                                                             const int *idx, int nbatch, float3 lw, float *G, float *loss,
                                                              unsigned char *xt, unsigned char *h1t, unsigned char *h2t,
                                                              unsigned char *dyt, unsigned char *dz2t, unsigned char *dz1t,
                                                              int *err) {
@@ -184,10 +185,12 @@ __global__ void __launch_bounds__(128, 1) mlp_fwd_bwd_kernel(MLPTiles W, const _
         tmem_ld16(lane_addr(tm, 256), y);
         const float t3[3] = {tg.x, tg.y, tg.z};
         float l = 0.f;
+        const float w3[3] = {lw.x, lw.y, lw.z};
         for (int o = 0; o < MLP_OUT; o++) {
             const float e = (o < MLP_NOUT) ? (y[o] + W.b3[o] - t3[o]) : 0.f;
-            l += e * e;
-            dy[o] = 2.f * e * inv;
+            const float wo = (o < MLP_NOUT) ? w3[o] : 0.f;
+            l += wo * e * e;
+            dy[o] = 2.f * wo * e * inv;
             store_t(dyt + (size_t)c * 128 * MLP_OUT * 2, o, tid, dy[o]);
             col_sum_add(dy[o], G + OFF_B3 + o);
         }
@@ -516,7 +519,7 @@ extern "C" int ppgpu_mlp_backward(void *handle, const void *X, const float *T, c
     cudaStream_t s = (cudaStream_t)stream;
     PPGPU_CUDA(cudaFuncSetAttribute(mlp_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FB_SMEM), "mlp smem");
     mlp_fwd_bwd_kernel<<<ntiles, 128, FB_SMEM, s>>>(M->view(), (const __nv_bfloat16 *)X, (const float4 *)T, idx, nbatch,
-                                                    M->G, M->loss, M->xt, M->h1t, M->h2t, M->dyt, M->dz2t, M->dz1t,
+                                                    make_float3(M->lw[0], M->lw[1], M->lw[2]), M->G, M->loss, M->xt, M->h1t, M->h2t, M->dyt, M->dz2t, M->dz1t,
                                                     device_error_word());
     PPGPU_CHECK_LAUNCH("mlp_fwd_bwd_kernel");
     const int per = 8;
@@ -565,5 +568,16 @@ extern "C" int ppgpu_mlp_views(void *handle, void **out8) {
     out8[5] = (void *)t.b1;
     out8[6] = (void *)t.b2;
     out8[7] = (void *)t.b3;
+    return set_ok();
+}
+
+/* Loss weights of the three outputs (default 1, 1, 1): the loss is mean(sum_o w_o (y_o - t_o)^2). */
+extern "C" int ppgpu_mlp_set_loss_weights(void *handle, const double *w3) {
+    MLP *M = (MLP *)handle;
+    if (!M || !w3) return set_error(PPGPU_ERR_ARG, "mlp_set_loss_weights: bad arguments");
+    for (int k = 0; k < 3; k++) {
+        if (!(w3[k] >= 0.0)) return set_error(PPGPU_ERR_ARG, "mlp_set_loss_weights: weights must be >= 0");
+        M->lw[k] = (float)w3[k];
+    }
     return set_ok();
 }

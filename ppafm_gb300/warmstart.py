@@ -10,7 +10,7 @@ many iterations a height takes.  Its training pairs come from plain FIRE itself
 
     net = WarmStartNet(seed=0)
     X, T = generate_pairs(heldout_systems, params, relax, stride=4)
-    net.train(X, T, steps=3000, batch=8192, lr=1e-3)
+    net.train(X, T, steps=30000, batch=8192, lr=5e-4)
     bp = BatchPipeline(systems, params, relax)
     bp.run_layered(net)            # or bp.run_layered() for plain FIRE in the same schedule
 """
@@ -28,11 +28,18 @@ NIN, NOUT_ROW = 96, 16
 class WarmStartNet:
     """The network's parameters (float32 master copy + Adam state) on the device."""
 
-    def __init__(self, seed=0):
+    def __init__(self, seed=0, loss_weights=(1.0, 1.0, 10.0)):
         self.handle = ctypes.c_void_p()
         check(lib().ppgpu_mlp_create(int(seed), ctypes.byref(self.handle)))
         self.nparams = lib().ppgpu_mlp_nparams()
         self.steps = 0
+        self.set_loss_weights(loss_weights)
+
+    def set_loss_weights(self, w):
+        """Per-output weights of the squared error (x, y, z of the displacement change); the
+        default weights z 10x: an error along the stiff radial spring costs the most iterations."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        check(lib().ppgpu_mlp_set_loss_weights(self.handle, w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
 
     def _get(self, which):
         out = np.zeros(self.nparams, dtype=np.float32)

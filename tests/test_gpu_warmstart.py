@@ -118,7 +118,7 @@ def test_learned_warm_start_gain(gpulib):
     X, T = generate_pairs(train_sys, params, relax, stride=1)
     assert X.shape[0] > 100000
     net = WarmStartNet(seed=0)
-    log = net.train(X, T, steps=1500, batch=8192, lr=1e-3, log_every=500)
+    log = net.train(X, T, steps=4000, batch=8192, lr=1e-3, log_every=1000)
     assert log[-1][1] < 0.5 * log[0][1], log
     test_sys, _, _ = _batch(8, 2000, 0.35)
     plain = BatchPipeline(test_sys, params, relax=relax, want_iters=True)
@@ -130,7 +130,7 @@ def test_learned_warm_start_gain(gpulib):
     it_l = np.concatenate([learned.outputs(j)["iters"].cpu().numpy().ravel() for j in range(len(test_sys))])
     # every height converged (no height hit the iteration cap that plain FIRE did not hit)
     assert (it_l >= relax["maxIters"]).sum() <= (it_p >= relax["maxIters"]).sum() + 2
-    assert it_l.mean() < 0.9 * it_p.mean(), (it_l.mean(), it_p.mean())
+    assert it_l.mean() < 0.75 * it_p.mean(), (it_l.mean(), it_p.mean())
     for j in range(len(test_sys)):
         a, b = plain.outputs(j), learned.outputs(j)
         dpos = np.linalg.norm(a["ppos"].cpu().numpy() - b["ppos"].cpu().numpy(), axis=-1)
