@@ -244,7 +244,7 @@ int ppgpu_tc_selftest(const void *A, const void *B, int K, int N, float *D, void
  * No reference counterpart.  A 96 -> 128 -> 128 -> 16 SiLU MLP (bf16 weights and activations,
  * float32 accumulation) on the tcgen05 tensor cores; float32 master parameters (layout:
  * W1 [96][128] | W2 [128][128] | W3 [128][16] | b1 [128] | b2 [128] | b3 [16]) with Adam.
- * X rows: 96 bf16 (84 features + 12 zeros); T rows: 4 f32 (3 targets); Y rows: 16 f32. */
+ * X rows: 96 bf16 (90 features + 6 zeros); T rows: 4 f32 (3 targets); Y rows: 16 f32. */
 int ppgpu_mlp_create(unsigned long long seed, void **handle);
 int ppgpu_mlp_destroy(void *handle);
 int ppgpu_mlp_nparams(void);

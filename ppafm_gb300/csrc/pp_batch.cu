@@ -340,18 +340,21 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const BatchPrm 
 // ------------------------------------------------------------ height-synchronous mode
 //
 // The learned warm start needs every stroke of a height at once (its network runs on 128-row
-// tiles), so this mode walks the heights in lockstep: for each height iz, the proposal kernel
-// computes the network's starting displacement of every stroke, then the height kernel runs
-// FIRE for every stroke from the better of the two starts (plain: the displacement converged
-// at the height above; learned: that plus the proposal) -- better = smaller initial force
-// residual, so a bad proposal falls back to the plain start.  With no network the height
-// kernel starts plain and reproduces the flattened kernel's result stroke for stroke.
+// tiles), so this mode walks the heights in lockstep: for each height iz, the inference
+// kernel computes the network's starting displacement of every stroke, then the height kernel
+// runs FIRE for every stroke from the better of the two starts (plain: the displacement
+// converged at the height above; learned: that plus the proposal) -- better = smaller initial
+// force residual, so a bad proposal falls back to the plain start.  The lane that finishes a
+// stroke at height iz writes the stroke's network inputs for height iz + 1 at once, while the
+// grid cells around the probe are still in L1.  With no network the height kernel starts
+// plain and reproduces the flattened kernel's result stroke for stroke.
 
 struct LayerPrm {
     int iz, nz_max;
     dfl *state;                // [nstrokes][3] displacement after the last finished height
     float4 *prop;              // [nstrokes] proposed change of the displacement (NULL: plain)
-    unsigned char *rec_x;      // training features [samples][96] bf16 (NULL: not recorded)
+    unsigned char *xtiles;     // network input tiles of the next height (NULL: no network)
+    unsigned char *rec_x;      // training features [samples][MLP_IN] bf16 (NULL: not recorded)
     float4 *rec_t;             // training targets [samples]: OUT_SCALE * (d_converged - d_start_plain)
     int rec_stride;            // strokes gs % rec_stride == 0 are recorded, sample (gs / stride) * nz_max + iz
     unsigned long long *pool;  // this height's stroke counter
@@ -406,87 +409,38 @@ __device__ __forceinline__ void load_prev(const BatchPrm &B, const LayerPrm &L, 
     }
 }
 
-// Feature kernel: the network inputs of every stroke at height iz, 16 threads per stroke (one
-// per x-y node column of the 4x4x4 neighbourhood of the probe's cell, so the gathers of a
-// stroke are all in flight at once).  Rows go into input tiles of 128 strokes in the tensor
-// cores' K-major layout (tile gs / 128, row gs % 128); recorded training rows are copied
-// row-major.  Padding strokes get zero rows.
-constexpr int FEAT_STROKES = 16;  // strokes per 256-thread block
-__global__ void __launch_bounds__(256) feature_kernel(const BatchPrm B, const LayerPrm L, unsigned char *Xtiles) {
-    __shared__ float S[FEAT_STROKES][16][9];  // z-interpolated samples per column: [c][cz*3+comp]
-    const int g = threadIdx.x >> 4, c = threadIdx.x & 15;
-    const long long gs = (long long)blockIdx.x * FEAT_STROKES + g;
-    StrokeAt A;
-    dfl d[3];
-    float t[3] = {0.f, 0.f, 0.f};
-    const bool valid = gs < B.nstrokes && stroke_at(B, gs, L.iz, A);
-    if (valid) {
+// Network inputs of stroke gs at height iz (A = stroke_at(gs, iz)) from the displacement d
+// converged at the height above and dd, the change of the converged displacement there:
+// row gs % 128 of input tile gs / 128 in the tensor cores' K-major layout, and the
+// row-major training copy when this stroke is recorded.
+constexpr long long XTILE_BYTES = 128LL * MLP_IN * 2;
+__device__ __forceinline__ void write_features(const BatchPrm &B, const LayerPrm &L, long long gs, int iz,
+                                               const StrokeAt &A, const dfl d[3], float3 dd) {
+    const bool rec = L.rec_x && gs % L.rec_stride == 0;
+    if (!L.xtiles && !rec) return;
+    dfl u[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(A.dic[k], d[k]));
+    const float3 dr = make_float3(df_round(df_add(d[0], B.R.nr0[0])), df_round(df_add(d[1], B.R.nr0[1])),
+                                  df_round(df_add(d[2], B.R.nr0[2])));
+    unsigned char *tile = L.xtiles ? L.xtiles + (gs >> 7) * XTILE_BYTES : nullptr;
+    const int row = (int)(gs & 127);
+    int4 *rrow = rec ? reinterpret_cast<int4 *>(L.rec_x + ((gs / L.rec_stride) * L.nz_max + iz) * (MLP_IN * 2)) : nullptr;
+    stencil_features(A.FE, A.n0, A.n1, A.n2, A.base, u, dr, dd, [&](int c, int4 v) {
+        if (tile) *reinterpret_cast<int4 *>(tile + tile_off(row, 8 * c, MLP_IN)) = v;
+        if (rrow) rrow[c] = v;
+    });
+}
+
+// Network inputs of every stroke at the first height (start: the probe's rest displacement).
+__global__ void __launch_bounds__(256) feature0_kernel(const BatchPrm B, const LayerPrm L) {
+    for (long long gs = blockIdx.x * (long long)blockDim.x + threadIdx.x; gs < B.nstrokes;
+         gs += (long long)gridDim.x * blockDim.x) {
+        StrokeAt A;
+        if (!stroke_at(B, gs, 0, A)) continue;
+        dfl d[3];
         load_prev(B, L, gs, d);
-        const BatchJob &J = B.jobs[A.job];
-        int ci[3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const dfl u = df_add(A.tf[k], df_mul(J.dic[k], d[k]));
-            const dfl tk = split_cell(u, ci[k]);
-            ci[k] += A.base[k];
-            t[k] = __fadd_rn(tk.h, tk.l);
-        }
-        const int px = c >> 2, py = c & 3;
-        const int ix = wrap_index(ci[0] - 1 + px, J.n0), iy = wrap_index(ci[1] - 1 + py, J.n1);
-        const float4 *col = J.FE + ((long long)ix * J.n1 + iy) * J.n2;
-        float4 q[4];
-#pragma unroll
-        for (int pz = 0; pz < 4; pz++) q[pz] = col[wrap_index(ci[2] - 1 + pz, J.n2)];
-#pragma unroll
-        for (int cz = 0; cz < 3; cz++) {
-            S[g][c][3 * cz + 0] = fmaf(t[2], q[cz + 1].x - q[cz].x, q[cz].x);
-            S[g][c][3 * cz + 1] = fmaf(t[2], q[cz + 1].y - q[cz].y, q[cz].y);
-            S[g][c][3 * cz + 2] = fmaf(t[2], q[cz + 1].z - q[cz].z, q[cz].z);
-        }
-    }
-    __syncthreads();
-    __shared__ __align__(16) __nv_bfloat16 R[FEAT_STROKES][MLP_IN];  // the block's rows, stored as 16-byte chunks
-    float dr0 = 0.f, dr1 = 0.f, dr2 = 0.f;
-    if (valid) {
-        dr0 = FEAT_DSCALE * df_round(df_add(d[0], B.R.nr0[0]));
-        dr1 = FEAT_DSCALE * df_round(df_add(d[1], B.R.nr0[1]));
-        dr2 = FEAT_DSCALE * df_round(df_add(d[2], B.R.nr0[2]));
-    }
-#pragma unroll
-    for (int m = 0; m < MLP_IN / 16; m++) {
-        const int k = c + 16 * m;
-        float x = 0.f;
-        if (valid) {
-            if (k < 81) {
-                const int s = k / 3, comp = k - 3 * s;
-                const int a = s / 9, b = (s / 3) % 3, cz = s % 3;
-                float F = 0.f;
-#pragma unroll
-                for (int dx = 0; dx < 2; dx++)
-#pragma unroll
-                    for (int dy = 0; dy < 2; dy++) {
-                        const float w = (dx ? t[0] : 1.f - t[0]) * (dy ? t[1] : 1.f - t[1]);
-                        F = fmaf(w, S[g][4 * (a + dx) + (b + dy)][3 * cz + comp], F);
-                    }
-                x = tanh_fast(FEAT_FSCALE * F);
-            } else if (k < MLP_FEAT) {
-                x = (k == 81) ? dr0 : ((k == 82) ? dr1 : dr2);
-            }
-        }
-        R[g][k] = __float2bfloat16_rn(x);
-    }
-    __syncthreads();
-    // 16 strokes x 12 chunks of 8 values: one 16-byte store each (tile layout; row-major copy
-    // of the recorded training rows)
-    const long long npad = (B.nstrokes + 127) / 128 * 128;
-    for (int q = threadIdx.x; q < FEAT_STROKES * (MLP_IN / 8); q += blockDim.x) {
-        const int gg = q / (MLP_IN / 8), ch = q - gg * (MLP_IN / 8);
-        const long long gq = (long long)blockIdx.x * FEAT_STROKES + gg;
-        if (gq >= npad) continue;
-        const int4 v = *reinterpret_cast<const int4 *>(&R[gg][8 * ch]);
-        *reinterpret_cast<int4 *>(Xtiles + (gq >> 7) * (long long)(128 * MLP_IN * 2) + tile_off((int)(gq & 127), 8 * ch, MLP_IN)) = v;
-        if (L.rec_x && gq < B.nstrokes && gq % L.rec_stride == 0 && B.stab[gq].x >= 0 && L.iz < B.jobs[B.stab[gq].x].nz)
-            reinterpret_cast<int4 *>(L.rec_x + ((gq / L.rec_stride) * L.nz_max + L.iz) * (MLP_IN * 2))[ch] = v;
+        write_features(B, L, gs, 0, A, d, make_float3(0.f, 0.f, 0.f));
     }
 }
 
@@ -511,7 +465,7 @@ __global__ void __launch_bounds__(128, 2) infer_kernel(const BatchPrm B, const L
     uint32_t ph = 0, phc = 0;
     bool ok = true;
     const long long ntiles = (B.nstrokes + 127) / 128;
-    constexpr uint32_t XBYTES = 128 * MLP_IN * 2;
+    constexpr uint32_t XBYTES = (uint32_t)XTILE_BYTES;
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         if (tid == 0) {
             fence_async_smem();  // earlier generic writes of act ordered before the async copy
@@ -534,7 +488,7 @@ __global__ void __launch_bounds__(128, 2) infer_kernel(const BatchPrm B, const L
 
 // Height kernel: FIRE at height iz for every stroke of the pool, lanes refilled as in the
 // flattened kernel.  Writes the height's outputs and the converged displacement (state).
-__global__ void __launch_bounds__(BATCH_THREADS) layer_relax_kernel(const BatchPrm B, const LayerPrm L) {
+__global__ void __launch_bounds__(BATCH_THREADS, 2) layer_relax_kernel(const BatchPrm B, const LayerPrm L) {
     const int lane = threadIdx.x & 31;
     const RelaxPrm &P = B.R;
     StrokeAt A;
@@ -619,6 +573,13 @@ __global__ void __launch_bounds__(BATCH_THREADS) layer_relax_kernel(const BatchP
                 L.state[3 * gs] = d[0];
                 L.state[3 * gs + 1] = d[1];
                 L.state[3 * gs + 2] = d[2];
+                if (L.iz + 1 < A.nz && (L.xtiles || L.rec_x)) {
+                    StrokeAt An;
+                    if (stroke_at(B, gs, L.iz + 1, An))
+                        write_features(B, L, gs, L.iz + 1, An, d,
+                                       make_float3(df_round(df_add(d[0], df_neg(d0[0]))), df_round(df_add(d[1], df_neg(d0[1]))),
+                                                   df_round(df_add(d[2], df_neg(d0[2])))));
+                }
                 if (L.rec_t && gs % L.rec_stride == 0) {
                     const long long slot = (gs / L.rec_stride) * L.nz_max + L.iz;
                     L.rec_t[slot] = make_float4(OUT_SCALE * df_round(df_add(d[0], df_neg(d0[0]))),
@@ -897,7 +858,7 @@ extern "C" int ppgpu_batch_destroy(void *handle) {
  * proposal kernel (with the network `mlp`, or features only when recording) and the height
  * kernel, then df.  mlp NULL: plain FIRE from the height above (same results as
  * ppgpu_batch_run).  rec_stride > 0: strokes gs % rec_stride == 0 record training pairs,
- * sample (gs / rec_stride) * nz_max + iz: rec_x [.][96] bf16 features, rec_t [.][4] f32 targets
+ * sample (gs / rec_stride) * nz_max + iz: rec_x [.][MLP_IN = 96] bf16 features, rec_t [.][4] f32 targets
  * OUT_SCALE (10/A) * (converged - plain start).  No host synchronisation (graph-capturable). */
 extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, void *rec_x, void *rec_t, void *stream) {
     BatchHandle *H = (BatchHandle *)handle;
@@ -919,6 +880,9 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
         H->prop = (float4 *)((char *)H->state + ((b_state + 15) / 16) * 16);
         H->pools = (unsigned long long *)((char *)H->prop + b_prop);
         H->tiles = (int *)(H->pools + std::max(nz, 1));
+        // input rows of padding strokes are never written: keep them zero (finite)
+        e = cudaMemset(H->xtiles, 0, b_x);
+        if (e != cudaSuccess) return cuda_fail(e, "batch layered buffers");
     }
     MLPTiles W;
     memset(&W, 0, sizeof(W));
@@ -948,7 +912,6 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     const int smem_net = TILE_W1T + TILE_W2T + TILE_W3T + TILE_ACT;
     if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_net), "infer smem");
     const bool propose = mlp || rec_stride > 0;
-    const unsigned feat_blocks = (unsigned)((((ns + 127) / 128) * 128 + FEAT_STROKES - 1) / FEAT_STROKES);
     for (int iz = 0; iz < nz; iz++) {
         LayerPrm L;
         memset(&L, 0, sizeof(L));
@@ -956,14 +919,17 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
         L.nz_max = nz;
         L.state = H->state;
         L.prop = mlp ? H->prop : nullptr;
+        L.xtiles = mlp ? H->xtiles : nullptr;
         L.rec_x = rec_stride > 0 ? (unsigned char *)rec_x : nullptr;
         L.rec_t = rec_stride > 0 ? (float4 *)rec_t : nullptr;
         L.rec_stride = rec_stride > 0 ? rec_stride : 1;
         L.pool = H->pools + iz;
         L.tile_ctr = H->tiles + iz;
         if (propose && ns > 0) {
-            feature_kernel<<<feat_blocks, 256, 0, st>>>(H->prm, L, H->xtiles);
-            PPGPU_CHECK_LAUNCH("feature_kernel");
+            if (iz == 0) {  // later heights: written by the height kernel above
+                feature0_kernel<<<2 * sms, 256, 0, st>>>(H->prm, L);
+                PPGPU_CHECK_LAUNCH("feature0_kernel");
+            }
             if (mlp) {
                 infer_kernel<<<2 * sms, 128, smem_net, st>>>(H->prm, L, W, H->xtiles);
                 PPGPU_CHECK_LAUNCH("infer_kernel");

@@ -60,17 +60,16 @@ static unsigned blocks_for(long long n) {
     return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
-// One thread per half-spectrum element: x over the last axis, y and z over the rows.
-static dim3 spec_grid(const FFTPlan *P) {
-    const int nh2 = P->n[2] / 2 + 1;
-    return dim3((unsigned)((nh2 + FFT_THREADS - 1) / FFT_THREADS), (unsigned)P->n[1], (unsigned)P->n[0]);
-}
+// One thread per half-spectrum element over a 1-D grid.
+static unsigned spec_blocks(const FFTPlan *P) { return (unsigned)((P->Nh + FFT_THREADS - 1) / FFT_THREADS); }
 
 // Rolled coordinate index of getMGrid (fieldFFT.py:32-49): i for i < n/2, i - n above.
 __device__ __forceinline__ double rolled(int i, int n) { return (double)(i < n / 2 ? i : i - n); }
-__device__ __forceinline__ double rolled_odd(int i, int n) {
+// Twice the odd part of the rolled index, rolled(i) - rolled(-i mod n): an integer, so the
+// spectra kernel needs no float64 arithmetic in its float32 form.
+__device__ __forceinline__ int rolled_odd2(int i, int n) {
     const int j = (i == 0) ? 0 : n - i;
-    return 0.5 * (rolled(i, n) - rolled(j, n));
+    return (i < n / 2 ? i : i - n) - (j < n / 2 ? j : j - n);
 }
 
 struct GaussCell {
@@ -79,16 +78,31 @@ struct GaussCell {
 
 struct SpecPrm {
     int n0, n1, n2, nh2;
-    double z[9];   // zeta_a = sum_j z[3a+j] * Xodd_j   (Linv[a][j] * dzeta_j * d_j)
+    long long Nh;   // elements of one half spectrum
+    double z[9];    // zeta_a = sum_j z[3a+j] * Xodd_j   (Linv[a][j] * dzeta_j * d_j)
     double sE, sF;  // dV/detLinv/N and 2 pi dV/detLinv/N
+    float zf[9], sEf, sFf;  // the same rounded to float32 (the float32 kernel's copies)
 };
+
+// The coefficients in the kernel's precision (no float64 -> float32 conversions per thread).
+template <typename R>
+__device__ __forceinline__ R spec_z(const SpecPrm &P, int i);
+template <>
+__device__ __forceinline__ float spec_z<float>(const SpecPrm &P, int i) { return P.zf[i]; }
+template <>
+__device__ __forceinline__ double spec_z<double>(const SpecPrm &P, int i) { return P.z[i]; }
+template <typename R>
+__device__ __forceinline__ R spec_s(const SpecPrm &P, bool force) {
+    if constexpr (sizeof(R) == 4) return force ? P.sFf : P.sEf;
+    else return force ? P.sF : P.sE;
+}
 
 template <typename C>
 struct Cx;
 template <>
 struct Cx<cufftComplex> {
     using real = float;
-    static __device__ __forceinline__ cufftComplex make(double x, double y) { return make_cuComplex((float)x, (float)y); }
+    static __device__ __forceinline__ cufftComplex make(float x, float y) { return make_cuComplex(x, y); }
 };
 template <>
 struct Cx<cufftDoubleComplex> {
@@ -96,29 +110,30 @@ struct Cx<cufftDoubleComplex> {
     static __device__ __forceinline__ cufftDoubleComplex make(double x, double y) { return make_cuDoubleComplex(x, y); }
 };
 
-// Four output spectra from FFT(V) and FFT(rho).  Grid (ceil(nh2/FFT_THREADS), n1, n0): one
-// thread per half-spectrum element of row (i, j).  The arithmetic is done in the precision
-// of the transforms (float32 spectra: float; float64 spectra: double).
+// Four output spectra from FFT(V) and FFT(rho).  One thread per half-spectrum element, the
+// elements numbered q = (i * n1 + j) * nh2 + k over a 1-D grid.  The arithmetic is done in
+// the precision of the transforms (float32 spectra: float; float64 spectra: double).
 template <typename C>
-__global__ void spectra_kernel(const C *__restrict__ Vk, const C *__restrict__ Rk, C *__restrict__ S4, long long Nh,
-                               SpecPrm P) {
+__global__ void spectra_kernel(const C *__restrict__ Vk, const C *__restrict__ Rk, C *__restrict__ S4, SpecPrm P) {
     using R = typename Cx<C>::real;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= P.nh2) return;
-    const int j = blockIdx.y, i = blockIdx.z;
-    const long long q = ((long long)i * P.n1 + j) * P.nh2 + k;
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= P.Nh) return;
+    const long long row = q / P.nh2;
+    const int k = (int)(q - row * P.nh2);
+    const int i = (int)(row / P.n1), j = (int)(row - (long long)i * P.n1);
     const C a = Vk[q], b = Rk[q];
     // C = a conj(b)
     const R cr = a.x * b.x + a.y * b.y;
     const R ci = a.y * b.x - a.x * b.y;
-    const R xo = (R)rolled_odd(i, P.n0), yo = (R)rolled_odd(j, P.n1), zo = (R)rolled_odd(k, P.n2);
-    const R sE = (R)P.sE, sF = (R)P.sF;
+    const R xo = (R)0.5 * (R)rolled_odd2(i, P.n0), yo = (R)0.5 * (R)rolled_odd2(j, P.n1),
+            zo = (R)0.5 * (R)rolled_odd2(k, P.n2);
+    const R sE = spec_s<R>(P, false), sF = spec_s<R>(P, true);
     S4[q] = Cx<C>::make(cr * sE, ci * sE);
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
-        const R zeta = ((R)P.z[3 * ax] * xo + (R)P.z[3 * ax + 1] * yo + (R)P.z[3 * ax + 2] * zo) * sF;
+        const R zeta = (spec_z<R>(P, 3 * ax) * xo + spec_z<R>(P, 3 * ax + 1) * yo + spec_z<R>(P, 3 * ax + 2) * zo) * sF;
         // zeta C (-2 pi i) = zeta (2 pi ci, -2 pi cr)
-        S4[(ax + 1) * Nh + q] = Cx<C>::make(zeta * ci, -zeta * cr);
+        S4[(ax + 1) * P.Nh + q] = Cx<C>::make(zeta * ci, -zeta * cr);
     }
 }
 
@@ -242,27 +257,37 @@ __global__ void density_power_kernel(float *rho, long long N, const double *sums
 
 struct PoissonPrm {
     int n0, n1, n2, nh2;
+    long long Nh;
     double b[9];  // reciprocal basis rows b_j (2 pi included): G = sum_j m_j b_j
     double s;     // 4 pi k_e / N
+    float bf[9], sf;  // the same rounded to float32
 };
 
 // numpy fftfreq index: 0..(n-1)/2 then negative.
-__device__ __forceinline__ double freq(int i, int n) { return (double)(i <= (n - 1) / 2 ? i : i - n); }
+__device__ __forceinline__ int freq(int i, int n) { return i <= (n - 1) / 2 ? i : i - n; }
+
+template <typename R>
+__device__ __forceinline__ R pois_b(const PoissonPrm &P, int i) {
+    if constexpr (sizeof(R) == 4) return P.bf[i];
+    else return P.b[i];
+}
 
 template <typename C>
-__global__ void poisson_kernel(C *Rk, long long Nh, PoissonPrm P) {
+__global__ void poisson_kernel(C *Rk, PoissonPrm P) {
     using R = typename Cx<C>::real;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= P.nh2) return;
-    const int j = blockIdx.y, i = blockIdx.z;
-    const long long q = ((long long)i * P.n1 + j) * P.nh2 + k;
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= P.Nh) return;
+    const long long row = q / P.nh2;
+    const int k = (int)(q - row * P.nh2);
+    const int i = (int)(row / P.n1), j = (int)(row - (long long)i * P.n1);
     const R m0 = (R)freq(i, P.n0), m1 = (R)freq(j, P.n1), m2 = (R)freq(k, P.n2);
-    const R gx = m0 * (R)P.b[0] + m1 * (R)P.b[3] + m2 * (R)P.b[6];
-    const R gy = m0 * (R)P.b[1] + m1 * (R)P.b[4] + m2 * (R)P.b[7];
-    const R gz = m0 * (R)P.b[2] + m1 * (R)P.b[5] + m2 * (R)P.b[8];
+    const R gx = m0 * pois_b<R>(P, 0) + m1 * pois_b<R>(P, 3) + m2 * pois_b<R>(P, 6);
+    const R gy = m0 * pois_b<R>(P, 1) + m1 * pois_b<R>(P, 4) + m2 * pois_b<R>(P, 7);
+    const R gz = m0 * pois_b<R>(P, 2) + m1 * pois_b<R>(P, 5) + m2 * pois_b<R>(P, 8);
     const R g2 = gx * gx + gy * gy + gz * gz;
     const C r = Rk[q];
-    const R f = (q == 0) ? (R)0 : (R)P.s / g2;
+    const R sc = (sizeof(R) == 4) ? (R)P.sf : (R)P.s;
+    const R f = (q == 0) ? (R)0 : sc / g2;
     Rk[q] = Cx<C>::make(r.x * f, r.y * f);
 }
 
@@ -429,17 +454,21 @@ extern "C" int ppgpu_fft_potential2forces(void *handle, const float *V, const fl
     const double dV = dd[0] * dd[1] * dd[2];
     sp.sE = dV / detLinv / (double)P->N;
     sp.sF = 2 * M_PI * dV / detLinv / (double)P->N;
+    sp.Nh = P->Nh;
+    for (int a = 0; a < 9; a++) sp.zf[a] = (float)sp.z[a];
+    sp.sEf = (float)sp.sE;
+    sp.sFf = (float)sp.sF;
     const int with_e = (flags & PPGPU_FF_WITH_E) ? 1 : 0, acc = (flags & PPGPU_FF_ACCUMULATE) ? 1 : 0;
     if (P->f64) {
-        spectra_kernel<cufftDoubleComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>(
-            (const cufftDoubleComplex *)P->Vk, (const cufftDoubleComplex *)P->Rk, (cufftDoubleComplex *)P->S4, P->Nh, sp);
+        spectra_kernel<cufftDoubleComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>(
+            (const cufftDoubleComplex *)P->Vk, (const cufftDoubleComplex *)P->Rk, (cufftDoubleComplex *)P->S4, sp);
         PPGPU_CHECK_LAUNCH("spectra_kernel");
         PPGPU_CUFFT(cufftExecZ2D(P->c2r4, (cufftDoubleComplex *)P->S4, (double *)P->planar), "inverse x4");
         pack_fe_kernel<double><<<blocks_for(P->N), FFT_THREADS, 0, st>>>((float4 *)FE, (const double *)P->planar, P->N,
                                                                           scale, with_e, acc);
     } else {
-        spectra_kernel<cufftComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>(
-            (const cufftComplex *)P->Vk, (const cufftComplex *)P->Rk, (cufftComplex *)P->S4, P->Nh, sp);
+        spectra_kernel<cufftComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>(
+            (const cufftComplex *)P->Vk, (const cufftComplex *)P->Rk, (cufftComplex *)P->S4, sp);
         PPGPU_CHECK_LAUNCH("spectra_kernel");
         PPGPU_CUFFT(cufftExecC2R(P->c2r4, (cufftComplex *)P->S4, (cufftReal *)P->planar), "inverse x4");
         pack_fe_kernel<float><<<blocks_for(P->N), FFT_THREADS, 0, st>>>((float4 *)FE, (const float *)P->planar, P->N,
@@ -514,14 +543,17 @@ extern "C" int ppgpu_fft_poisson(void *handle, const float *rho_charge, const do
     for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) pp.b[3 * r + c] = 2 * M_PI * ci[3 * c + r];
     pp.s = 4 * M_PI * 14.399645 / (double)P->N;
+    pp.Nh = P->Nh;
+    for (int a = 0; a < 9; a++) pp.bf[a] = (float)pp.b[a];
+    pp.sf = (float)pp.s;
     if (P->f64) {
-        poisson_kernel<cufftDoubleComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>((cufftDoubleComplex *)P->Rk, P->Nh, pp);
+        poisson_kernel<cufftDoubleComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>((cufftDoubleComplex *)P->Rk, pp);
         PPGPU_CHECK_LAUNCH("poisson_kernel");
         PPGPU_CUFFT(cufftExecZ2D(P->c2r1, (cufftDoubleComplex *)P->Rk, stage), "inverse V");
         f64_to_f32_kernel<<<blocks_for(P->N), FFT_THREADS, 0, st>>>(V, stage, P->N);
         PPGPU_CHECK_LAUNCH("f64_to_f32_kernel");
     } else {
-        poisson_kernel<cufftComplex><<<spec_grid(P), FFT_THREADS, 0, st>>>((cufftComplex *)P->Rk, P->Nh, pp);
+        poisson_kernel<cufftComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>((cufftComplex *)P->Rk, pp);
         PPGPU_CHECK_LAUNCH("poisson_kernel");
         PPGPU_CUFFT(cufftExecC2R(P->c2r1, (cufftComplex *)P->Rk, (cufftReal *)V), "inverse V");
     }

@@ -5,7 +5,7 @@
 // converged displacement of the height above; plain FIRE then always runs to the same
 // convergence criterion, so the network can only save iterations.
 //
-// Network: 96 (84 features + 12 zero pad) -> 128 -> 128 -> 16 (3 used), SiLU, bf16 weights
+// Network: 96 (90 features + 6 zero pad) -> 128 -> 128 -> 16 (3 used), SiLU, bf16 weights
 // and activations, float32 accumulation in tensor memory.  Every GEMM is a 128-row tile
 // issued by one thread with tcgen05.mma (pp_tc.cuh); epilogues (bias, SiLU, its derivative,
 // conversions) run on all threads from tcgen05.ld.
@@ -23,7 +23,7 @@ namespace ppgpu {
 
 // ------------------------------------------------------------- parameters
 // Master parameters (float32, one array): W1 [96 in][128 out], W2 [128][128], W3 [128][16],
-// b1 [128], b2 [128], b3 [16].  Rows 84..95 of W1 multiply zero padding.
+// b1 [128], b2 [128], b3 [16].  Rows 90..95 of W1 multiply zero padding.
 constexpr int OFF_W1 = 0;
 constexpr int OFF_W2 = OFF_W1 + MLP_IN * MLP_H;
 constexpr int OFF_W3 = OFF_W2 + MLP_H * MLP_H;

@@ -1,14 +1,18 @@
 // pp_mlp_dev.cuh -- device side of the warm-start network (shared by the proposal kernel of
 // pp_batch.cu and the training kernels of pp_mlp.cu).
 //
-// Network: x[96] (84 features, 12 zeros) -> 128 -> 128 -> y[16] (3 used), SiLU, bf16 weights and
+// Network: x[96] (90 features, 6 zeros) -> 128 -> 128 -> y[16] (3 used), SiLU, bf16 weights and
 // activations, float32 accumulation in tensor memory (tcgen05, pp_tc.cuh).  One CTA of 128
 // threads runs 128 samples; thread t owns sample t (TMEM lane t).
 //
-// Features of a probe at grid coordinate base + u with previous converged displacement d:
-//   f[9*(3*(a+1)+(b+1))+3*(c+1)+comp] = tanh(FEAT_FSCALE * F_comp(u + (a, b, c)))
-//       for a, b, c in {-1, 0, 1}: the trilinear force one grid step around the probe;
-//   f[81..83] = FEAT_DSCALE * (d - rPP0);   f[84..95] = 0.
+// Features of a probe whose start point (tip + previous converged displacement d) has grid
+// coordinate m + s (m the nearest grid node, s in [-1/2, 1/2)^3), with F the force at the
+// 3 x 3 x 3 grid nodes around m:
+//   f[3 (9 (a+1) + 3 (b+1) + (c+1)) + comp] = tanh(FEAT_FSCALE * F_comp(m + (a, b, c)))   0..80
+//   f[81 + k] = 2 s_k                                                                 81..83
+//   f[84 + k] = FEAT_DSCALE * (d - rPP0)_k                                            84..86
+//   f[87 + k] = OUT_SCALE * (change of the converged displacement at the height above) 87..89
+//   f[90..95] = 0.
 // Output: y[0..2] = OUT_SCALE * (d_converged - d).
 #pragma once
 
@@ -21,7 +25,7 @@
 namespace ppgpu {
 
 constexpr int MLP_IN = 96;
-constexpr int MLP_FEAT = 84;
+constexpr int MLP_FEAT = 90;
 constexpr int MLP_H = 128;
 constexpr int MLP_OUT = 16;
 constexpr int MLP_NOUT = 3;
@@ -121,7 +125,7 @@ __device__ __forceinline__ void silu_epilogue(unsigned char *act, uint32_t tmem,
     }
 }
 
-// Forward pass of the 128 samples whose inputs are in `act` (K = 96 layout).  Leaves the
+// Forward pass of the 128 samples whose inputs are in `act` (K = MLP_IN layout).  Leaves the
 // output row (16 floats, bias added) in y.  act is overwritten by the hidden activations.
 // Returns false if an MMA never completed (bounded wait).
 __device__ __forceinline__ bool mlp_forward(unsigned char *act, const unsigned char *W1t, const unsigned char *W2t,
@@ -160,88 +164,65 @@ __device__ __forceinline__ bool mlp_forward(unsigned char *act, const unsigned c
     return ok;
 }
 
-// Features of one probe (see the header comment) written as row `row` of the K = 96 input
-// tile.  FE: float4 grid, n: its size, base + u: the probe's grid coordinate (u
-// double-float), dr = d - rPP0.
-template <bool NC>
-__device__ __forceinline__ void warm_features(const float4 *FE, int n0, int n1, int n2, const int base[3],
-                                              const dfl u[3], float3 dr, unsigned char *tile, int row) {
-    int ci[3];
-    float t[3];
+// Features of one probe (see the header comment): grid (FE, n0..n2), the probe's start point
+// at grid coordinate base + u (u double-float), dr = d - rPP0, dd = the change of the
+// converged displacement at the height above (A).  Chunk c (values 8c .. 8c+7, packed to
+// bf16) is handed to emit(c, int4) as soon as it is complete.
+template <typename Emit>
+__device__ __forceinline__ void stencil_features(const float4 *FE, int n0, int n1, int n2, const int base[3],
+                                                 const dfl u[3], float3 dr, float3 dd, Emit emit) {
+    int m[3];
+    float sx[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const dfl tk = split_cell(u[k], ci[k]);
-        ci[k] += base[k];
-        t[k] = __fadd_rn(tk.h, tk.l);
+        const dfl tk = split_cell(u[k], m[k]);
+        m[k] += base[k];
+        const float t = __fadd_rn(tk.h, tk.l);
+        const bool up = t >= 0.5f;  // nearest node
+        m[k] += up ? 1 : 0;
+        sx[k] = up ? t - 1.f : t;
     }
-    float acc[27][3];
+    __align__(16) __nv_bfloat162 pk[4];
+    float lo = 0.f;
+    // value i (a compile-time index once unrolled) into the pending chunk
+    auto push = [&](int i, float x) {
+        if (i & 1) pk[(i & 7) >> 1] = __floats2bfloat162_rn(lo, x);
+        else lo = x;
+        if ((i & 7) == 7) emit(i >> 3, *reinterpret_cast<const int4 *>(pk));
+    };
+    int iy[3], iz[3];
 #pragma unroll
-    for (int s = 0; s < 27; s++) acc[s][0] = acc[s][1] = acc[s][2] = 0.f;
-    // the 4x4 node columns around the cell (x, y offsets -1..2), each 4 nodes along z
+    for (int o = 0; o < 3; o++) {
+        iy[o] = wrap_index(m[1] - 1 + o, n1);
+        iz[o] = wrap_index(m[2] - 1 + o, n2);
+    }
 #pragma unroll
-    for (int px = 0; px < 4; px++) {
-        const int ix = wrap_index(ci[0] - 1 + px, n0);
+    for (int a = 0; a < 3; a++) {
+        const long long xrow = (long long)wrap_index(m[0] - 1 + a, n0) * n1;
+        float4 q[9];
 #pragma unroll
-        for (int py = 0; py < 4; py++) {
-            const int iy = wrap_index(ci[1] - 1 + py, n1);
-            const long long col = ((long long)ix * n1 + iy) * n2;
-            float3 node[4];
+        for (int b = 0; b < 3; b++)
 #pragma unroll
-            for (int pz = 0; pz < 4; pz++) {
-                const int iz = wrap_index(ci[2] - 1 + pz, n2);
-                const float4 q = NC ? __ldg(FE + col + iz) : FE[col + iz];
-                node[pz] = make_float3(q.x, q.y, q.z);
-            }
-            // z interpolation for the sample offsets -1, 0, 1 (c = 0, 1, 2): nodes c, c+1
-            float3 vz[3];
+            for (int c = 0; c < 3; c++) q[3 * b + c] = FE[(xrow + iy[b]) * n2 + iz[c]];
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                vz[c].x = fmaf(t[2], node[c + 1].x - node[c].x, node[c].x);
-                vz[c].y = fmaf(t[2], node[c + 1].y - node[c].y, node[c].y);
-                vz[c].z = fmaf(t[2], node[c + 1].z - node[c].z, node[c].z);
-            }
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                // sample a uses x nodes a (weight 1-tx) and a+1 (weight tx)
-                const float wx = (px == a) ? 1.f - t[0] : ((px == a + 1) ? t[0] : 0.f);
-                if (px != a && px != a + 1) continue;
-#pragma unroll
-                for (int b = 0; b < 3; b++) {
-                    if (py != b && py != b + 1) continue;
-                    const float w = wx * ((py == b) ? 1.f - t[1] : t[1]);
-#pragma unroll
-                    for (int c = 0; c < 3; c++) {
-                        const int s = 9 * a + 3 * b + c;
-                        acc[s][0] = fmaf(w, vz[c].x, acc[s][0]);
-                        acc[s][1] = fmaf(w, vz[c].y, acc[s][1]);
-                        acc[s][2] = fmaf(w, vz[c].z, acc[s][2]);
-                    }
-                }
-            }
+        for (int bc = 0; bc < 9; bc++) {
+            const int i = 3 * (9 * a + bc);
+            push(i, tanh_fast(FEAT_FSCALE * q[bc].x));
+            push(i + 1, tanh_fast(FEAT_FSCALE * q[bc].y));
+            push(i + 2, tanh_fast(FEAT_FSCALE * q[bc].z));
         }
     }
-    // tanh-compressed forces, the scaled displacement and zero padding: 96 values
-    float v[16];
+    push(81, 2.f * sx[0]);
+    push(82, 2.f * sx[1]);
+    push(83, 2.f * sx[2]);
+    push(84, FEAT_DSCALE * dr.x);
+    push(85, FEAT_DSCALE * dr.y);
+    push(86, FEAT_DSCALE * dr.z);
+    push(87, OUT_SCALE * dd.x);
+    push(88, OUT_SCALE * dd.y);
+    push(89, OUT_SCALE * dd.z);
 #pragma unroll
-    for (int g = 0; g < MLP_IN / 16; g++) {
-#pragma unroll
-        for (int i = 0; i < 16; i++) {
-            const int k = 16 * g + i;
-            float x;
-            if (k < 81)
-                x = tanh_fast(FEAT_FSCALE * acc[k / 3][k % 3]);
-            else if (k == 81)
-                x = FEAT_DSCALE * dr.x;
-            else if (k == 82)
-                x = FEAT_DSCALE * dr.y;
-            else if (k == 83)
-                x = FEAT_DSCALE * dr.z;
-            else
-                x = 0.f;
-            v[i] = x;
-        }
-        store16_bf16(tile, row, 16 * g, v, MLP_IN);
-    }
+    for (int i = 90; i < MLP_IN; i++) push(i, 0.f);
 }
 
 }  // namespace ppgpu

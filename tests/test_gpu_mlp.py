@@ -4,6 +4,8 @@ network's forward/backward against the numpy float64 oracle and the trained netw
 import numpy as np
 import pytest
 
+from oracle.mlp_oracle import IN as NIN
+
 pytestmark = pytest.mark.gpu
 
 
@@ -48,9 +50,9 @@ def _data(n, seed):
     import torch
 
     rng = np.random.default_rng(seed)
-    X = rng.normal(0, 1, (n, 96)).astype(np.float32)
-    X[:, 81:] *= 0.5
-    X[:, 84:] = 0.0
+    X = rng.normal(0, 1, (n, NIN)).astype(np.float32)
+    X[:, 81:90] *= 0.5
+    X[:, 90:] = 0.0
     T = rng.normal(0, 0.5, (n, 4)).astype(np.float32)
     Xd = torch.tensor(X, dtype=torch.bfloat16, device="cuda")
     Td = torch.tensor(T, device="cuda")
@@ -144,11 +146,11 @@ def test_mlp_training_reduces_loss(gpulib):
     L, h = _net(11)
     n = 8192
     rng = np.random.default_rng(4)
-    X = rng.normal(0, 1, (n, 96)).astype(np.float32)
-    X[:, 84:] = 0
-    Wt = rng.normal(0, 0.3, (84, 3))
+    X = rng.normal(0, 1, (n, NIN)).astype(np.float32)
+    X[:, 90:] = 0
+    Wt = rng.normal(0, 0.3, (90, 3))
     T = np.zeros((n, 4), np.float32)
-    T[:, :3] = np.tanh(X[:, :84] @ Wt)
+    T[:, :3] = np.tanh(X[:, :90] @ Wt)
     Xd = torch.tensor(X, dtype=torch.bfloat16, device="cuda")
     Td = torch.tensor(T, device="cuda")
     losses = []

@@ -216,8 +216,8 @@ def test_mlp_oracle_gradient_finite_differences():
 
     rng = np.random.default_rng(0)
     P = rng.normal(0, 0.2, MO.NPARAM)
-    X = rng.normal(0, 1, (5, 96))
-    X[:, 84:] = 0
+    X = rng.normal(0, 1, (5, MO.IN))
+    X[:, MO.IN - 6 :] = 0
     T = rng.normal(0, 1, (5, 4))
     _, G = MO.loss_and_grad(P, X, T, bf=False)
     for i in rng.choice(MO.NPARAM, 40, replace=False):
