@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "pp_common.cuh"
@@ -358,7 +359,24 @@ struct LayerPrm {
     float4 *rec_t;             // training targets [samples]: OUT_SCALE * (d_converged - d_start_plain)
     int rec_stride;            // strokes gs % rec_stride == 0 are recorded, sample (gs / stride) * nz_max + iz
     unsigned long long *pool;  // this height's stroke counter
-    int *tile_ctr;             // this height's proposal tile counter
+    float4 *dd;                // [nstrokes] change of the converged displacement at this height
+                               // (written by the height kernel, read by the next feature kernel)
+    float accept_f2;           // a proposal is taken when its |F|^2 is at most this
+    // long strokes first: strokes that took at least hard_it iterations at the height above
+    // are listed (hard_in, *hard_n_in of them) and dispensed before the tile-ordered pool,
+    // which skips them (prev_it_in).  This height fills the lists of the next one.
+    int hard_it;
+    const int *hard_in;
+    const unsigned *hard_n_in;
+    unsigned long long *hard_ctr;
+    int *hard_out;
+    unsigned *hard_n_out;
+    const unsigned short *prev_it_in;
+    unsigned short *prev_it_out;
+};
+
+struct DfVec3 {  // a double-float displacement
+    dfl c[3];
 };
 
 // Tip, grid cell and fraction of global stroke gs at height iz; false for tile padding and for
@@ -409,38 +427,128 @@ __device__ __forceinline__ void load_prev(const BatchPrm &B, const LayerPrm &L, 
     }
 }
 
-// Network inputs of stroke gs at height iz (A = stroke_at(gs, iz)) from the displacement d
-// converged at the height above and dd, the change of the converged displacement there:
-// row gs % 128 of input tile gs / 128 in the tensor cores' K-major layout, and the
-// row-major training copy when this stroke is recorded.
+// Network inputs of stroke gs at height iz: row gs % 128 of input tile gs / 128 in the
+// tensor cores' K-major layout, and the row-major training copy when the stroke is recorded.
 constexpr long long XTILE_BYTES = 128LL * MLP_IN * 2;
-__device__ __forceinline__ void write_features(const BatchPrm &B, const LayerPrm &L, long long gs, int iz,
-                                               const StrokeAt &A, const dfl d[3], float3 dd) {
-    const bool rec = L.rec_x && gs % L.rec_stride == 0;
-    if (!L.xtiles && !rec) return;
-    dfl u[3];
+
+// What the 3x3x3 stencil row of one stroke needs (the feature layout of pp_mlp_dev.cuh).
+struct FeatTask {
+    const float4 *FE;
+    int n0, n1, n2;
+    int gs;     // -1: nothing to write
+    int m[3];   // nearest grid node of the start point (unwrapped)
+    float e[9];  // features 81..89: 2 s, FEAT_DSCALE (d - rPP0), OUT_SCALE dd
+};
+
+// Task of stroke gs at height iz (A = stroke_at(gs, iz)), from the displacement d converged at
+// the height above and dd, the change of the converged displacement there.
+__device__ __forceinline__ void make_task(const BatchPrm &B, long long gs, const StrokeAt &A, const dfl d[3], float3 dd,
+                                          FeatTask &T) {
+    T.FE = A.FE;
+    T.n0 = A.n0;
+    T.n1 = A.n1;
+    T.n2 = A.n2;
+    T.gs = (int)gs;
 #pragma unroll
-    for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(A.dic[k], d[k]));
-    const float3 dr = make_float3(df_round(df_add(d[0], B.R.nr0[0])), df_round(df_add(d[1], B.R.nr0[1])),
-                                  df_round(df_add(d[2], B.R.nr0[2])));
-    unsigned char *tile = L.xtiles ? L.xtiles + (gs >> 7) * XTILE_BYTES : nullptr;
-    const int row = (int)(gs & 127);
-    int4 *rrow = rec ? reinterpret_cast<int4 *>(L.rec_x + ((gs / L.rec_stride) * L.nz_max + iz) * (MLP_IN * 2)) : nullptr;
-    stencil_features(A.FE, A.n0, A.n1, A.n2, A.base, u, dr, dd, [&](int c, int4 v) {
-        if (tile) *reinterpret_cast<int4 *>(tile + tile_off(row, 8 * c, MLP_IN)) = v;
-        if (rrow) rrow[c] = v;
-    });
+    for (int k = 0; k < 3; k++) {
+        const dfl u = df_add(A.tf[k], df_mul(A.dic[k], d[k]));
+        int ci;
+        const dfl tk = split_cell(u, ci);
+        const float t = __fadd_rn(tk.h, tk.l);
+        const bool up = t >= 0.5f;  // nearest node
+        T.m[k] = ci + A.base[k] + (up ? 1 : 0);
+        T.e[k] = 2.f * (up ? t - 1.f : t);
+        T.e[3 + k] = FEAT_DSCALE * df_round(df_add(d[k], B.R.nr0[k]));
+    }
+    T.e[6] = OUT_SCALE * dd.x;
+    T.e[7] = OUT_SCALE * dd.y;
+    T.e[8] = OUT_SCALE * dd.z;
 }
 
-// Network inputs of every stroke at the first height (start: the probe's rest displacement).
-__global__ void __launch_bounds__(256) feature0_kernel(const BatchPrm B, const LayerPrm L) {
-    for (long long gs = blockIdx.x * (long long)blockDim.x + threadIdx.x; gs < B.nstrokes;
-         gs += (long long)gridDim.x * blockDim.x) {
-        StrokeAt A;
-        if (!stroke_at(B, gs, 0, A)) continue;
-        dfl d[3];
-        load_prev(B, L, gs, d);
-        write_features(B, L, gs, 0, A, d, make_float3(0.f, 0.f, 0.f));
+// One warp writes the rows of ntask (1..FEAT_TPC) tasks: FEAT_LPT lanes per task, stencil nodes
+// j, j + FEAT_LPT, ... for lane j (all its gathers in flight at once), values staged in the
+// warp's row buffers, then one 16-byte store per chunk (the feature layout of pp_mlp_dev.cuh).
+constexpr int FEAT_TPC = 4;              // tasks per warp call
+constexpr int FEAT_LPT = 32 / FEAT_TPC;  // lanes per task
+constexpr int FEAT_NPL = (27 + FEAT_LPT - 1) / FEAT_LPT;  // stencil nodes per lane
+__device__ __forceinline__ void warp_features(const FeatTask *tk, int ntask, __nv_bfloat16 (*row)[MLP_IN],
+                                              const LayerPrm &L, int iz) {
+    const int lane = threadIdx.x & 31, tsk = lane / FEAT_LPT, j = lane % FEAT_LPT;
+    const bool act = tsk < ntask && tk[tsk].gs >= 0;
+    if (act) {
+        const FeatTask &T = tk[tsk];
+        float4 q[FEAT_NPL];
+#pragma unroll
+        for (int r = 0; r < FEAT_NPL; r++) {
+            const int node = j + FEAT_LPT * r;
+            if (node < 27) {
+                const int a = node / 9, b = (node / 3) % 3, c = node % 3;
+                const int ix = wrap_index(T.m[0] - 1 + a, T.n0), iy = wrap_index(T.m[1] - 1 + b, T.n1),
+                          iz3 = wrap_index(T.m[2] - 1 + c, T.n2);
+                q[r] = T.FE[((long long)ix * T.n1 + iy) * T.n2 + iz3];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < FEAT_NPL; r++) {
+            const int node = j + FEAT_LPT * r;
+            if (node < 27) {
+                row[tsk][3 * node] = __float2bfloat16_rn(tanh_fast(FEAT_FSCALE * q[r].x));
+                row[tsk][3 * node + 1] = __float2bfloat16_rn(tanh_fast(FEAT_FSCALE * q[r].y));
+                row[tsk][3 * node + 2] = __float2bfloat16_rn(tanh_fast(FEAT_FSCALE * q[r].z));
+            }
+        }
+        if (j == FEAT_LPT - 1) {  // a lane with one node fewer
+#pragma unroll
+            for (int i = 0; i < 9; i++) row[tsk][81 + i] = __float2bfloat16_rn(T.e[i]);
+#pragma unroll
+            for (int i = 90; i < MLP_IN; i++) row[tsk][i] = __float2bfloat16_rn(0.f);
+        }
+    }
+    __syncwarp();
+    constexpr int CH = MLP_IN / 8;  // 16-byte chunks per row
+#pragma unroll
+    for (int r = 0; r < (FEAT_TPC * CH + 31) / 32; r++) {
+        const int qi = lane + 32 * r, t = qi / CH, ch = qi - t * CH;
+        if (t < ntask && tk[t].gs >= 0) {
+            const long long gs = tk[t].gs;
+            const int4 v = reinterpret_cast<const int4 *>(row[t])[ch];
+            if (L.xtiles)
+                *reinterpret_cast<int4 *>(L.xtiles + (gs >> 7) * XTILE_BYTES + tile_off((int)(gs & 127), 8 * ch, MLP_IN)) = v;
+            if (L.rec_x && gs % L.rec_stride == 0)
+                reinterpret_cast<int4 *>(L.rec_x + ((gs / L.rec_stride) * L.nz_max + iz) * (MLP_IN * 2))[ch] = v;
+        }
+    }
+    __syncwarp();
+}
+
+// Feature kernel: the network inputs of every stroke at height iz (start: the displacement
+// converged at the height above, state, and its change there, dd; the rest displacement at
+// the first height).  Each warp takes FEAT_TPC strokes at a time: FEAT_TPC lanes build their
+// tasks, then the warp writes the rows (warp_features).
+__global__ void __launch_bounds__(256) feature_kernel(const BatchPrm B, const LayerPrm L) {
+    __shared__ FeatTask fq[8][FEAT_TPC];
+    __shared__ __align__(16) __nv_bfloat16 frow[8][FEAT_TPC][MLP_IN];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long step = (long long)gridDim.x * 8 * FEAT_TPC;
+    for (long long g0 = ((long long)blockIdx.x * 8 + w) * FEAT_TPC; g0 < B.nstrokes; g0 += step) {
+        if (lane < FEAT_TPC) {
+            const long long gs = g0 + lane;
+            FeatTask &T = fq[w][lane];
+            T.gs = -1;
+            StrokeAt A;
+            if (gs < B.nstrokes && (L.xtiles || gs % L.rec_stride == 0) && stroke_at(B, gs, L.iz, A)) {
+                dfl d[3];
+                load_prev(B, L, gs, d);
+                float3 dd = make_float3(0.f, 0.f, 0.f);
+                if (L.iz > 0) {
+                    const float4 q = L.dd[gs];
+                    dd = make_float3(q.x, q.y, q.z);
+                }
+                make_task(B, gs, A, d, dd, T);
+            }
+        }
+        __syncwarp();
+        warp_features(fq[w], FEAT_TPC, frow[w], L, L.iz);
     }
 }
 
@@ -486,26 +594,120 @@ __global__ void __launch_bounds__(128, 2) infer_kernel(const BatchPrm B, const L
     if (tid < 32) tmem_dealloc(tbase, 128);
 }
 
+constexpr float LAYER_ACCEPT_F2 = 1.0f;  // (eV/A)^2: proposals with a larger residual fall back
+constexpr int LAYER_HARD_ITERS = 40;     // strokes this long at the height above go first
+
+// ---- float32 FIRE of the learned mode.  A warm-started stroke stops at a different point of
+// the |F|^2 < convF2 ball than plain FIRE from the height above, so the double-float
+// arithmetic that makes the plain path stop where the reference stops buys nothing there;
+// float32 keeps the residual's error (~1e-7 eV/A) far below the criterion (1e-4 eV/A).
+
+// Periodic trilinear interpolation (Grid.h:93-111) at grid coordinate base + u, float32.
+__device__ __forceinline__ float3 interp_force_f32(const float4 *FE, int n0, int n1, int n2, const int base[3],
+                                                   const float u[3]) {
+    int ci[3];
+    float t[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float fl = floorf(u[k]);
+        t[k] = u[k] - fl;
+        ci[k] = (int)fl + base[k];
+    }
+    const int ix0 = wrap_index(ci[0], n0), iy0 = wrap_index(ci[1], n1), iz0 = wrap_index(ci[2], n2);
+    const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
+    const int iy1 = (iy0 + 1 == n1) ? 0 : iy0 + 1;
+    const int iz1 = (iz0 + 1 == n2) ? 0 : iz0 + 1;
+    const long long r00 = ((long long)ix0 * n1 + iy0) * n2, r01 = ((long long)ix0 * n1 + iy1) * n2;
+    const long long r10 = ((long long)ix1 * n1 + iy0) * n2, r11 = ((long long)ix1 * n1 + iy1) * n2;
+    const float4 c[8] = {FE[r00 + iz0], FE[r00 + iz1], FE[r01 + iz0], FE[r01 + iz1],
+                         FE[r10 + iz0], FE[r10 + iz1], FE[r11 + iz0], FE[r11 + iz1]};
+    auto lerp = [](float a, float b, float w) { return fmaf(w, b - a, a); };
+    auto comp = [&](int k) {
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = k == 0 ? c[i].x : (k == 1 ? c[i].y : c[i].z);
+        const float a00 = lerp(v[0], v[1], t[2]), a01 = lerp(v[2], v[3], t[2]);
+        const float a10 = lerp(v[4], v[5], t[2]), a11 = lerp(v[6], v[7], t[2]);
+        return lerp(lerp(a00, a01, t[1]), lerp(a10, a11, t[1]), t[0]);
+    };
+    return make_float3(comp(0), comp(1), comp(2));
+}
+
+// Probe-particle force (getPPforce, ProbeParticle.cpp:282-294; forceRSpring, Forces.h:85-89):
+// grid force + radial spring kRad (l - l0)/l d + lateral spring kSpring (d - rPP0).
+__device__ __forceinline__ float3 pp_force_f32(const RelaxPrm &P, float3 F, float3 d) {
+    const float l2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+    const float rs = rsqrt_approx(l2);
+    const float l = l2 * rs;
+    const float sr = P.kRadf.h * ((l + P.nl0.h) * rs);
+    return make_float3(fmaf(d.x + P.nr0[0].h, P.kSf[0].h, fmaf(d.x, sr, F.x)),
+                       fmaf(d.y + P.nr0[1].h, P.kSf[1].h, fmaf(d.y, sr, F.y)),
+                       fmaf(d.z + P.nr0[2].h, P.kSf[2].h, fmaf(d.z, sr, F.z)));
+}
+
+// relax_move_df with a float32 displacement.
+__device__ __forceinline__ float relax_move_f32(const RelaxPrm &P, float3 f, float3 &d, float3 &v, float &dt,
+                                                float &acoef) {
+    const float ff = fmaf(f.z, f.z, fmaf(f.y, f.y, f.x * f.x));
+    float h;
+    if (P.relaxAlg == 1) {
+        const float vv = fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x));
+        const float vf = fmaf(f.z, v.z, fmaf(f.y, v.y, f.x * v.x));
+        if (vf < 0.f) {
+            v = make_float3(0.f, 0.f, 0.f);
+            dt = dt * P.fdecf;
+            acoef = P.acoef0f;
+        } else {
+            const float vf2 = vv * ff;
+            const float cf = (vf2 > 1e-30f) ? acoef * vv * rsqrt_approx(vf2) : 0.f;
+            const float cv = 1.f - acoef;
+            v.x = fmaf(f.x, cf, v.x * cv);
+            v.y = fmaf(f.y, cf, v.y * cv);
+            v.z = fmaf(f.z, cf, v.z * cv);
+            dt = fminf(dt * P.fincf, P.dtmaxf);
+            acoef = acoef * P.falphaf;
+        }
+        h = dt;
+    } else {
+        const float c = 1.f - P.acoef0f;
+        v.x *= c;
+        v.y *= c;
+        v.z *= c;
+        h = P.dtmaxf;
+    }
+    v.x = fmaf(f.x, h, v.x);
+    v.y = fmaf(f.y, h, v.y);
+    v.z = fmaf(f.z, h, v.z);
+    d.x = fmaf(v.x, h, d.x);
+    d.y = fmaf(v.y, h, d.y);
+    d.z = fmaf(v.z, h, d.z);
+    return ff;
+}
+
 // Height kernel: FIRE at height iz for every stroke of the pool, lanes refilled as in the
-// flattened kernel.  Writes the height's outputs and the converged displacement (state).
+// flattened kernel; the strokes listed as long by the height above are dispensed first.
+// Writes the height's outputs, the converged displacement (state) and its change (dd).
+// LEARNED = false: plain FIRE from the height above in the double-float arithmetic of the
+// flattened kernel (the same result stroke for stroke).  LEARNED = true: the start is the
+// proposal when its |F|^2 is at most accept_f2 (FIRE's first move made from it in the same
+// trip), else the plain start; FIRE in float32.
+template <bool LEARNED>
 __global__ void __launch_bounds__(BATCH_THREADS, 2) layer_relax_kernel(const BatchPrm B, const LayerPrm L) {
+    using Disp = typename std::conditional<LEARNED, float3, DfVec3>::type;
     const int lane = threadIdx.x & 31;
     const RelaxPrm &P = B.R;
     StrokeAt A;
     long long gs = -1;
     bool has = false;
-    // Every trip does one gather.  phase 0: the learned start dm is evaluated (its residual
-    // and probe-particle force kept); phase 1: the plain start d0 is evaluated, the better
-    // one chosen and FIRE's first move made from it in the same trip; phase 2: FIRE.
-    int phase = 2;
-    dfl d[3], d0[3], dm[3];
-    float3 fm = make_float3(0.f, 0.f, 0.f);
-    float rm = 0.f;
+    bool proposal = false;  // learned: this trip evaluates the proposal
+    Disp d, d0, dm;
     float3 v = make_float3(0.f, 0.f, 0.f);
     float dt = 0.f, acoef = 0.f;
     int it = 0, itcount = 0;
     bool fin = false;
     long long pool_next = 0, pool_end = 0;
+    int src = (L.hard_in && L.hard_n_in) ? 0 : 1;  // 0: the list of long strokes, 1: the pool
+    const long long nhard = src == 0 ? (long long)*L.hard_n_in : 0;
     bool drained = false;
     unsigned long long mine = 0;
     const int chunk = B.chunk;
@@ -513,31 +715,53 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) layer_relax_kernel(const Bat
         unsigned need = __ballot_sync(FULL, !has);
         while (need && !drained) {
             if (pool_next >= pool_end) {
-                unsigned long long g = 0;
-                if (lane == 0) g = atomicAdd(L.pool, (unsigned long long)chunk);
-                g = __shfl_sync(FULL, g, 0);
-                if ((long long)g >= B.nstrokes) {
+                long long g = 0, lim = 0;
+                if (src == 0) {
+                    unsigned long long x = 0;
+                    if (lane == 0) x = atomicAdd(L.hard_ctr, (unsigned long long)chunk);
+                    x = __shfl_sync(FULL, x, 0);
+                    if ((long long)x < nhard) {
+                        g = (long long)x;
+                        lim = nhard;
+                    } else {
+                        src = 1;
+                    }
+                }
+                if (src == 1) {
+                    unsigned long long x = 0;
+                    if (lane == 0) x = atomicAdd(L.pool, (unsigned long long)chunk);
+                    x = __shfl_sync(FULL, x, 0);
+                    g = (long long)x;
+                    lim = B.nstrokes;
+                }
+                if (g >= lim) {
                     drained = true;
                     break;
                 }
-                pool_next = (long long)g;
-                pool_end = min(pool_next + (long long)chunk, B.nstrokes);
+                pool_next = g;
+                pool_end = min(pool_next + (long long)chunk, lim);
             }
             const int rank = __popc(need & ((1u << lane) - 1u));
             const int take = (int)min((long long)__popc(need), pool_end - pool_next);
             if (((need >> lane) & 1u) && rank < take) {
-                gs = pool_next + rank;
-                if (stroke_at(B, gs, L.iz, A)) {
-                    load_prev(B, L, gs, d0);
+                const long long idx = pool_next + rank;
+                gs = (src == 0) ? (long long)L.hard_in[idx] : idx;
+                bool ok = stroke_at(B, gs, L.iz, A);
+                if (ok && src == 1 && L.prev_it_in && (int)L.prev_it_in[gs] >= L.hard_it) ok = false;  // listed
+                if (ok) {
+                    dfl p[3];
+                    load_prev(B, L, gs, p);
+                    if constexpr (LEARNED) {
+                        d0 = make_float3(df_round(p[0]), df_round(p[1]), df_round(p[2]));
+                        d = d0;
+                        proposal = L.prop && P.maxIters > 0;
+                        if (proposal) {
+                            const float4 q = L.prop[gs];
+                            dm = make_float3(d0.x + q.x, d0.y + q.y, d0.z + q.z);
+                        }
+                    } else {
 #pragma unroll
-                    for (int k = 0; k < 3; k++) d[k] = d0[k];
-                    phase = 2;
-                    if (L.prop && P.maxIters > 0) {
-                        const float4 q = L.prop[gs];
-                        dm[0] = df_add_f(d0[0], q.x);
-                        dm[1] = df_add_f(d0[1], q.y);
-                        dm[2] = df_add_f(d0[2], q.z);
-                        phase = 0;
+                        for (int k = 0; k < 3; k++) d0.c[k] = d.c[k] = p[k];
                     }
                     v = make_float3(0.f, 0.f, 0.f);
                     dt = P.dtmaxf;
@@ -552,68 +776,78 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) layer_relax_kernel(const Bat
             need = __ballot_sync(FULL, !has);
         }
         if (!__any_sync(FULL, has)) break;
-        if (has) {
-            dfl de[3];
+        if (!has) continue;
+        // one trip: the force at the current displacement, then either the outputs (fin) or a move
+        float3 Fg;       // learned: grid force
+        dfl F[3];        // plain: grid force
+        if constexpr (LEARNED) {
+            const float3 de = proposal ? dm : d;
+            const float u[3] = {fmaf(A.dic[0].h, de.x, df_round(A.tf[0])), fmaf(A.dic[1].h, de.y, df_round(A.tf[1])),
+                                fmaf(A.dic[2].h, de.z, df_round(A.tf[2]))};
+            Fg = interp_force_f32(A.FE, A.n0, A.n1, A.n2, A.base, u);
+        } else {
+            dfl u[3];
 #pragma unroll
-            for (int k = 0; k < 3; k++) de[k] = (phase == 0) ? dm[k] : d[k];
-            dfl u[3], F[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(A.dic[k], de[k]));
+            for (int k = 0; k < 3; k++) u[k] = df_add(A.tf[k], df_mul(A.dic[k], d.c[k]));
             interp_force_df<false>(A.FE, A.n0, A.n1, A.n2, A.base, u, F);
-            if (fin) {
-                const BatchJob &J = B.jobs[A.job];
-                const long long pix = (long long)A.ix * J.ny + A.iy;
-                const long long o = pix * A.nz + (A.nz - 1 - L.iz);
-                if (J.fzs) J.fzs[o] = df_round(F[2]);
-                if (J.ppos) {
-#pragma unroll
-                    for (int k = 0; k < 3; k++) J.ppos[3 * o + k] = df_round(df_add(df_add(A.tip[k], d[k]), J.offd[k]));
-                }
-                if (J.iters) J.iters[o] = itcount;
-                L.state[3 * gs] = d[0];
-                L.state[3 * gs + 1] = d[1];
-                L.state[3 * gs + 2] = d[2];
-                if (L.iz + 1 < A.nz && (L.xtiles || L.rec_x)) {
-                    StrokeAt An;
-                    if (stroke_at(B, gs, L.iz + 1, An))
-                        write_features(B, L, gs, L.iz + 1, An, d,
-                                       make_float3(df_round(df_add(d[0], df_neg(d0[0]))), df_round(df_add(d[1], df_neg(d0[1]))),
-                                                   df_round(df_add(d[2], df_neg(d0[2])))));
-                }
-                if (L.rec_t && gs % L.rec_stride == 0) {
-                    const long long slot = (gs / L.rec_stride) * L.nz_max + L.iz;
-                    L.rec_t[slot] = make_float4(OUT_SCALE * df_round(df_add(d[0], df_neg(d0[0]))),
-                                                OUT_SCALE * df_round(df_add(d[1], df_neg(d0[1]))),
-                                                OUT_SCALE * df_round(df_add(d[2], df_neg(d0[2]))), 0.f);
-                }
-                has = false;
+        }
+        if (fin) {
+            const BatchJob &J = B.jobs[A.job];
+            const long long pix = (long long)A.ix * J.ny + A.iy;
+            const long long o = pix * A.nz + (A.nz - 1 - L.iz);
+            dfl dc[3];  // converged displacement
+            float3 dd;  // its change from the height above
+            if constexpr (LEARNED) {
+                dc[0] = {d.x, 0.f};
+                dc[1] = {d.y, 0.f};
+                dc[2] = {d.z, 0.f};
+                dd = make_float3(d.x - d0.x, d.y - d0.y, d.z - d0.z);
+                if (J.fzs) J.fzs[o] = Fg.z;
             } else {
-                float3 f = pp_force_df(P, F, de);
-                const float r = f.x * f.x + f.y * f.y + f.z * f.z;
-                if (phase == 0) {  // learned start evaluated; the plain one next trip
-                    fm = f;
-                    rm = r;
-                    phase = 1;
-                } else {
-                    if (phase == 1) {  // learned start unless its residual is larger
-                        if (rm <= r) {
 #pragma unroll
-                            for (int k = 0; k < 3; k++) d[k] = dm[k];
-                            f = fm;
-                        }
-                        phase = 2;
-                    }
-                    const float ff = relax_move_df(P, f, d, v, dt, acoef);
-                    mine++;
-                    if (ff < P.convF2f) {
-                        itcount = it;
-                        fin = true;
-                    } else if (++it >= P.maxIters) {
-                        itcount = P.maxIters;
-                        fin = true;
-                    }
-                }
+                for (int k = 0; k < 3; k++) dc[k] = d.c[k];
+                dd = make_float3(df_round(df_add(d.c[0], df_neg(d0.c[0]))), df_round(df_add(d.c[1], df_neg(d0.c[1]))),
+                                 df_round(df_add(d.c[2], df_neg(d0.c[2]))));
+                if (J.fzs) J.fzs[o] = df_round(F[2]);
             }
+            if (J.ppos) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) J.ppos[3 * o + k] = df_round(df_add(df_add(A.tip[k], dc[k]), J.offd[k]));
+            }
+            if (J.iters) J.iters[o] = itcount;
+            L.state[3 * gs] = dc[0];
+            L.state[3 * gs + 1] = dc[1];
+            L.state[3 * gs + 2] = dc[2];
+            if (L.dd) L.dd[gs] = make_float4(dd.x, dd.y, dd.z, 0.f);
+            if (L.prev_it_out) L.prev_it_out[gs] = (unsigned short)min(itcount, 65535);
+            if (L.hard_out && itcount >= L.hard_it && L.iz + 1 < A.nz) L.hard_out[atomicAdd(L.hard_n_out, 1u)] = (int)gs;
+            if (L.rec_t && gs % L.rec_stride == 0) {
+                const long long slot = (gs / L.rec_stride) * L.nz_max + L.iz;
+                L.rec_t[slot] = make_float4(OUT_SCALE * dd.x, OUT_SCALE * dd.y, OUT_SCALE * dd.z, 0.f);
+            }
+            has = false;
+            continue;
+        }
+        float ff;
+        if constexpr (LEARNED) {
+            float3 f = pp_force_f32(P, Fg, proposal ? dm : d);
+            if (proposal) {  // taken unless its residual is too large
+                proposal = false;
+                if (fmaf(f.z, f.z, fmaf(f.y, f.y, f.x * f.x)) > L.accept_f2) continue;  // plain start next trip
+                d = dm;
+            }
+            ff = relax_move_f32(P, f, d, v, dt, acoef);
+        } else {
+            const float3 f = pp_force_df(P, F, d.c);
+            ff = relax_move_df(P, f, d.c, v, dt, acoef);
+        }
+        mine++;
+        if (ff < P.convF2f) {
+            itcount = it;
+            fin = true;
+        } else if (++it >= P.maxIters) {
+            itcount = P.maxIters;
+            fin = true;
         }
     }
     add_iterations(B.iter_total, mine);
@@ -654,8 +888,11 @@ struct BatchHandle {
     unsigned char *xtiles = nullptr;  // network input tiles of one height (allocation base)
     dfl *state = nullptr;
     float4 *prop = nullptr;
-    unsigned long long *pools = nullptr;  // [nz_max] stroke counters
-    int *tiles = nullptr;                 // [nz_max] proposal tile counters
+    unsigned long long *pools = nullptr;  // [nz_max] stroke counters, then [nz_max] long-list counters
+    unsigned *hard_n = nullptr;           // [nz_max] long strokes listed for each height
+    int *hard = nullptr;                  // [2][nstrokes] lists of long strokes (by height parity)
+    unsigned short *prev_it = nullptr;    // [2][nstrokes] iterations at the last two heights
+    float4 *dd = nullptr;                 // [nstrokes] change of the converged displacement
 };
 
 }  // namespace ppgpu
@@ -868,18 +1105,23 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     cudaStream_t st = (cudaStream_t)stream;
     const long long ns = H->prm.nstrokes;
     const int nz = H->nz_max;
+    const size_t b_ctr = (2 * sizeof(unsigned long long) + sizeof(unsigned)) * (size_t)std::max(nz, 1);
     if (!H->state) {
-        const size_t b_state = sizeof(dfl) * 3 * (size_t)std::max(ns, 1LL), b_prop = sizeof(float4) * (size_t)std::max(ns, 1LL);
-        const size_t b_ctr = (sizeof(unsigned long long) + sizeof(int)) * (size_t)std::max(nz, 1);
+        const size_t nsx = (size_t)std::max(ns, 1LL);
+        const size_t b_state = sizeof(dfl) * 3 * nsx, b_prop = sizeof(float4) * nsx;
         const size_t b_x = (size_t)((ns + 127) / 128) * 128 * MLP_IN * 2;
+        const size_t b_hard = sizeof(int) * 2 * nsx, b_it = sizeof(unsigned short) * 2 * nsx, b_dd = sizeof(float4) * nsx;
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, b_x + b_state + b_prop + b_ctr + 256);
+        cudaError_t e = cudaMalloc(&p, b_x + b_state + b_prop + b_ctr + b_hard + b_it + b_dd + 512);
         if (e != cudaSuccess) return cuda_fail(e, "batch layered buffers");
         H->xtiles = (unsigned char *)p;
         H->state = (dfl *)((char *)p + b_x);
         H->prop = (float4 *)((char *)H->state + ((b_state + 15) / 16) * 16);
         H->pools = (unsigned long long *)((char *)H->prop + b_prop);
-        H->tiles = (int *)(H->pools + std::max(nz, 1));
+        H->hard_n = (unsigned *)(H->pools + 2 * std::max(nz, 1));
+        H->hard = (int *)((char *)H->pools + ((b_ctr + 15) / 16) * 16);
+        H->prev_it = (unsigned short *)(H->hard + 2 * nsx);
+        H->dd = (float4 *)((char *)H->prev_it + ((b_it + 255) / 256) * 256);
         // input rows of padding strokes are never written: keep them zero (finite)
         e = cudaMemset(H->xtiles, 0, b_x);
         if (e != cudaSuccess) return cuda_fail(e, "batch layered buffers");
@@ -900,8 +1142,7 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
         W.b3 = (const float *)v[7];
     }
     PPGPU_CUDA(cudaMemsetAsync(H->ctr_base, 0, H->ctr_bytes, st), "batch counters");
-    PPGPU_CUDA(cudaMemsetAsync(H->pools, 0, (sizeof(unsigned long long) + sizeof(int)) * (size_t)std::max(nz, 1), st),
-               "batch layer counters");
+    PPGPU_CUDA(cudaMemsetAsync(H->pools, 0, b_ctr, st), "batch layer counters");
     // force fields only (an empty stroke pool ends the relaxation phase at once)
     BatchPrm Bff = H->prm;
     Bff.nstrokes = 0;
@@ -924,18 +1165,33 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
         L.rec_t = rec_stride > 0 ? (float4 *)rec_t : nullptr;
         L.rec_stride = rec_stride > 0 ? rec_stride : 1;
         L.pool = H->pools + iz;
-        L.tile_ctr = H->tiles + iz;
+        L.accept_f2 = LAYER_ACCEPT_F2;
+        L.hard_it = LAYER_HARD_ITERS;
+        const size_t nsx = (size_t)std::max(ns, 1LL);
+        if (iz > 0) {
+            L.hard_in = H->hard + (size_t)(iz & 1) * nsx;
+            L.hard_n_in = H->hard_n + iz;
+            L.prev_it_in = H->prev_it + (size_t)((iz - 1) & 1) * nsx;
+        }
+        L.hard_ctr = H->pools + nz + iz;
+        if (iz + 1 < nz) {
+            L.hard_out = H->hard + (size_t)((iz + 1) & 1) * nsx;
+            L.hard_n_out = H->hard_n + iz + 1;
+        }
+        L.prev_it_out = H->prev_it + (size_t)(iz & 1) * nsx;
+        L.dd = H->dd;
         if (propose && ns > 0) {
-            if (iz == 0) {  // later heights: written by the height kernel above
-                feature0_kernel<<<2 * sms, 256, 0, st>>>(H->prm, L);
-                PPGPU_CHECK_LAUNCH("feature0_kernel");
-            }
+            feature_kernel<<<4 * sms, 256, 0, st>>>(H->prm, L);
+            PPGPU_CHECK_LAUNCH("feature_kernel");
             if (mlp) {
                 infer_kernel<<<2 * sms, 128, smem_net, st>>>(H->prm, L, W, H->xtiles);
                 PPGPU_CHECK_LAUNCH("infer_kernel");
             }
         }
-        layer_relax_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm, L);
+        if (mlp)
+            layer_relax_kernel<true><<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm, L);
+        else
+            layer_relax_kernel<false><<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm, L);
         PPGPU_CHECK_LAUNCH("layer_relax_kernel");
     }
     batch_df_kernel<<<2 * sms, 256, 0, st>>>(H->prm);

@@ -164,65 +164,4 @@ __device__ __forceinline__ bool mlp_forward(unsigned char *act, const unsigned c
     return ok;
 }
 
-// Features of one probe (see the header comment): grid (FE, n0..n2), the probe's start point
-// at grid coordinate base + u (u double-float), dr = d - rPP0, dd = the change of the
-// converged displacement at the height above (A).  Chunk c (values 8c .. 8c+7, packed to
-// bf16) is handed to emit(c, int4) as soon as it is complete.
-template <typename Emit>
-__device__ __forceinline__ void stencil_features(const float4 *FE, int n0, int n1, int n2, const int base[3],
-                                                 const dfl u[3], float3 dr, float3 dd, Emit emit) {
-    int m[3];
-    float sx[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const dfl tk = split_cell(u[k], m[k]);
-        m[k] += base[k];
-        const float t = __fadd_rn(tk.h, tk.l);
-        const bool up = t >= 0.5f;  // nearest node
-        m[k] += up ? 1 : 0;
-        sx[k] = up ? t - 1.f : t;
-    }
-    __align__(16) __nv_bfloat162 pk[4];
-    float lo = 0.f;
-    // value i (a compile-time index once unrolled) into the pending chunk
-    auto push = [&](int i, float x) {
-        if (i & 1) pk[(i & 7) >> 1] = __floats2bfloat162_rn(lo, x);
-        else lo = x;
-        if ((i & 7) == 7) emit(i >> 3, *reinterpret_cast<const int4 *>(pk));
-    };
-    int iy[3], iz[3];
-#pragma unroll
-    for (int o = 0; o < 3; o++) {
-        iy[o] = wrap_index(m[1] - 1 + o, n1);
-        iz[o] = wrap_index(m[2] - 1 + o, n2);
-    }
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const long long xrow = (long long)wrap_index(m[0] - 1 + a, n0) * n1;
-        float4 q[9];
-#pragma unroll
-        for (int b = 0; b < 3; b++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) q[3 * b + c] = FE[(xrow + iy[b]) * n2 + iz[c]];
-#pragma unroll
-        for (int bc = 0; bc < 9; bc++) {
-            const int i = 3 * (9 * a + bc);
-            push(i, tanh_fast(FEAT_FSCALE * q[bc].x));
-            push(i + 1, tanh_fast(FEAT_FSCALE * q[bc].y));
-            push(i + 2, tanh_fast(FEAT_FSCALE * q[bc].z));
-        }
-    }
-    push(81, 2.f * sx[0]);
-    push(82, 2.f * sx[1]);
-    push(83, 2.f * sx[2]);
-    push(84, FEAT_DSCALE * dr.x);
-    push(85, FEAT_DSCALE * dr.y);
-    push(86, FEAT_DSCALE * dr.z);
-    push(87, OUT_SCALE * dd.x);
-    push(88, OUT_SCALE * dd.y);
-    push(89, OUT_SCALE * dd.z);
-#pragma unroll
-    for (int i = 90; i < MLP_IN; i++) push(i, 0.f);
-}
-
 }  // namespace ppgpu
