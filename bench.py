@@ -301,10 +301,10 @@ class BatchBench:
         self.torch.cuda.current_stream().synchronize()
         return h2d, d2h
 
-    def learned(self, args, plain_loop_ms, steps=30000, lr=5e-4):
+    def learned(self, args, plain_loop_ms, steps=30000, lr=1e-3):
         """Config-4 line: train the warm-start network on plain-FIRE pairs of a held-out batch
-        (every 4th stroke of 256 other molecules: ~21M pairs; Adam, batch 8192, z error weighted
-        10x), then
+        (every 4th stroke of 256 other molecules: ~21M pairs; Adam, batch 8192, cosine-decayed
+        learning rate, z error weighted 10x), then
         time the height-synchronous batched run with it (CUDA graph) against plain FIRE."""
         import torch
 
@@ -318,7 +318,7 @@ class BatchBench:
         t_gen = time.perf_counter() - t0
         net = WarmStartNet(seed=0)
         t0 = time.perf_counter()
-        log = net.train(X, T, steps=steps, batch=8192, lr=lr, log_every=steps // 3)
+        log = net.train(X, T, steps=steps, batch=8192, lr=lr, log_every=steps // 3, schedule="cosine")
         torch.cuda.synchronize()
         t_train = time.perf_counter() - t0
         npairs = int(X.shape[0])
@@ -359,7 +359,7 @@ class BatchBench:
             "layered_plain_ms_per_step": ms["layered_plain"],
             "fire_iters_per_pixel_z": {"plain_mean": float(it_plain.mean()), "plain_p99": float(np.percentile(it_plain, 99)), "learned_mean": float(it_l.mean()), "learned_p99": float(np.percentile(it_l, 99))},
             "df_vs_plain_fire": {"frac_over_0.1Hz": float((dd > 0.1).mean()), "p99.9_Hz": float(np.quantile(dd, 0.999)), "max_Hz": float(dd.max())},
-            "training": {"pairs": npairs, "steps": steps, "batch": 8192, "lr": lr, "loss_weights": [1.0, 1.0, 10.0], "generate_s": t_gen, "train_s": t_train, "loss": log},
+            "training": {"pairs": npairs, "steps": steps, "batch": 8192, "lr": lr, "schedule": "cosine", "loss_weights": [1.0, 1.0, 10.0], "generate_s": t_gen, "train_s": t_train, "loss": log},
         }
 
     def plain_ms(self, reps=2):

@@ -468,7 +468,7 @@ __device__ __forceinline__ void make_task(const BatchPrm &B, long long gs, const
 // One warp writes the rows of ntask (1..FEAT_TPC) tasks: FEAT_LPT lanes per task, stencil nodes
 // j, j + FEAT_LPT, ... for lane j (all its gathers in flight at once), values staged in the
 // warp's row buffers, then one 16-byte store per chunk (the feature layout of pp_mlp_dev.cuh).
-constexpr int FEAT_TPC = 4;              // tasks per warp call
+constexpr int FEAT_TPC = 8;              // tasks per warp call
 constexpr int FEAT_LPT = 32 / FEAT_TPC;  // lanes per task
 constexpr int FEAT_NPL = (27 + FEAT_LPT - 1) / FEAT_LPT;  // stencil nodes per lane
 __device__ __forceinline__ void warp_features(const FeatTask *tk, int ntask, __nv_bfloat16 (*row)[MLP_IN],
@@ -505,11 +505,13 @@ __device__ __forceinline__ void warp_features(const FeatTask *tk, int ntask, __n
         }
     }
     __syncwarp();
+    // chunk-major: one store instruction writes the same chunk of consecutive rows, which lie
+    // 16 bytes apart in the tile layout (full 128-byte lines for aligned groups of 8 strokes)
     constexpr int CH = MLP_IN / 8;  // 16-byte chunks per row
 #pragma unroll
     for (int r = 0; r < (FEAT_TPC * CH + 31) / 32; r++) {
-        const int qi = lane + 32 * r, t = qi / CH, ch = qi - t * CH;
-        if (t < ntask && tk[t].gs >= 0) {
+        const int qi = lane + 32 * r, ch = qi / FEAT_TPC, t = qi - ch * FEAT_TPC;
+        if (ch < CH && t < ntask && tk[t].gs >= 0) {
             const long long gs = tk[t].gs;
             const int4 v = reinterpret_cast<const int4 *>(row[t])[ch];
             if (L.xtiles)
@@ -523,15 +525,15 @@ __device__ __forceinline__ void warp_features(const FeatTask *tk, int ntask, __n
 
 // Feature kernel: the network inputs of every stroke at height iz (start: the displacement
 // converged at the height above, state, and its change there, dd; the rest displacement at
-// the first height).  Each warp takes FEAT_TPC strokes at a time: FEAT_TPC lanes build their
-// tasks, then the warp writes the rows (warp_features).
+// the first height).  Each warp takes 32 consecutive strokes at a time: every lane builds one
+// task, then the warp writes the rows FEAT_TPC at a time (warp_features).
 __global__ void __launch_bounds__(256) feature_kernel(const BatchPrm B, const LayerPrm L) {
-    __shared__ FeatTask fq[8][FEAT_TPC];
+    __shared__ FeatTask fq[8][32];
     __shared__ __align__(16) __nv_bfloat16 frow[8][FEAT_TPC][MLP_IN];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const long long step = (long long)gridDim.x * 8 * FEAT_TPC;
-    for (long long g0 = ((long long)blockIdx.x * 8 + w) * FEAT_TPC; g0 < B.nstrokes; g0 += step) {
-        if (lane < FEAT_TPC) {
+    const long long step = (long long)gridDim.x * 8 * 32;
+    for (long long g0 = ((long long)blockIdx.x * 8 + w) * 32; g0 < B.nstrokes; g0 += step) {
+        {
             const long long gs = g0 + lane;
             FeatTask &T = fq[w][lane];
             T.gs = -1;
@@ -548,50 +550,57 @@ __global__ void __launch_bounds__(256) feature_kernel(const BatchPrm B, const La
             }
         }
         __syncwarp();
-        warp_features(fq[w], FEAT_TPC, frow[w], L, L.iz);
+#pragma unroll 1
+        for (int k = 0; k < 32; k += FEAT_TPC) warp_features(&fq[w][k], FEAT_TPC, frow[w], L, L.iz);
     }
 }
 
-// Inference kernel: persistent CTAs keep the weights in shared memory and run the network on
-// input tiles fetched by bulk copies; the proposal of stroke gs is OUT_SCALE^-1 * y[0..2].
-__global__ void __launch_bounds__(128, 2) infer_kernel(const BatchPrm B, const LayerPrm L, const MLPTiles W,
-                                                       const unsigned char *Xtiles) {
+// Inference kernel: one persistent CTA per SM keeps the weights in shared memory; each of its
+// INFER_GROUPS warpgroups runs the network on its own input tiles (fetched by bulk copies into
+// its own activation buffer, accumulating in its own 128 TMEM columns), so the SM has that
+// many tiles in flight.  The proposal of stroke gs is OUT_SCALE^-1 * y[0..2].
+constexpr int INFER_GROUPS = 4;
+constexpr int INFER_SMEM = TILE_W1T + TILE_W2T + TILE_W3T + INFER_GROUPS * TILE_ACT;
+__global__ void __launch_bounds__(128 * INFER_GROUPS, 1) infer_kernel(const BatchPrm B, const LayerPrm L,
+                                                                      const MLPTiles W, const unsigned char *Xtiles) {
     extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t bar_mma, bar_copy;
+    __shared__ uint64_t bar_mma[INFER_GROUPS], bar_copy[INFER_GROUPS];
     __shared__ uint32_t tbase;
-    unsigned char *sW1t = sm, *sW2t = sW1t + TILE_W1T, *sW3t = sW2t + TILE_W2T, *act = sW3t + TILE_W3T;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, g = tid >> 7, row = tid & 127;
+    unsigned char *sW1t = sm, *sW2t = sW1t + TILE_W1T, *sW3t = sW2t + TILE_W2T;
+    unsigned char *act = sW3t + TILE_W3T + g * TILE_ACT;
     copy_tile(sW1t, W.W1t, TILE_W1T);
     copy_tile(sW2t, W.W2t, TILE_W2T);
     copy_tile(sW3t, W.W3t, TILE_W3T);
-    if (tid == 0) {
-        tc_mbar_init(&bar_mma);
-        tc_mbar_init(&bar_copy);
+    if (tid < INFER_GROUPS) {
+        tc_mbar_init(&bar_mma[tid]);
+        tc_mbar_init(&bar_copy[tid]);
     }
-    if (tid < 32) tmem_alloc(&tbase, 128);
+    if (tid < 32) tmem_alloc(&tbase, 128 * INFER_GROUPS);
     cta_handoff();
+    const uint32_t tm = tbase + 128u * (uint32_t)g;
     uint32_t ph = 0, phc = 0;
     bool ok = true;
     const long long ntiles = (B.nstrokes + 127) / 128;
     constexpr uint32_t XBYTES = (uint32_t)XTILE_BYTES;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (tid == 0) {
+    for (long long tile = (long long)blockIdx.x * INFER_GROUPS + g; tile < ntiles; tile += (long long)gridDim.x * INFER_GROUPS) {
+        if (row == 0) {
             fence_async_smem();  // earlier generic writes of act ordered before the async copy
-            mbar_expect_tx(&bar_copy, XBYTES);
-            bulk_g2s(act, Xtiles + tile * XBYTES, XBYTES, &bar_copy);
+            mbar_expect_tx(&bar_copy[g], XBYTES);
+            bulk_g2s(act, Xtiles + tile * XBYTES, XBYTES, &bar_copy[g]);
         }
-        ok &= tc_mbar_wait(&bar_copy, phc);
+        ok &= tc_mbar_wait(&bar_copy[g], phc);
         phc ^= 1u;
         float y[16];
-        ok &= mlp_forward(act, sW1t, sW2t, sW3t, W.b1, W.b2, W.b3, tbase, &bar_mma, ph, y);
-        const long long gs = tile * 128 + tid;
+        ok &= mlp_forward(act, sW1t, sW2t, sW3t, W.b1, W.b2, W.b3, tm, &bar_mma[g], ph, y, g);
+        const long long gs = tile * 128 + row;
         if (gs < B.nstrokes)
             L.prop[gs] = make_float4(y[0] * (1.f / OUT_SCALE), y[1] * (1.f / OUT_SCALE), y[2] * (1.f / OUT_SCALE), 0.f);
     }
-    if (!ok && tid == 0) raise_device_error(B.err, PPGPU_ERR_DEVICE_TIMEOUT);
+    if (!ok && row == 0) raise_device_error(B.err, PPGPU_ERR_DEVICE_TIMEOUT);
     tc_fence_before();
     __syncthreads();
-    if (tid < 32) tmem_dealloc(tbase, 128);
+    if (tid < 32) tmem_dealloc(tbase, 128 * INFER_GROUPS);
 }
 
 constexpr float LAYER_ACCEPT_F2 = 1.0f;  // (eV/A)^2: proposals with a larger residual fall back
@@ -1150,8 +1159,7 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     PPGPU_CHECK_LAUNCH("batch_kernel (force fields)");
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->dev);
-    const int smem_net = TILE_W1T + TILE_W2T + TILE_W3T + TILE_ACT;
-    if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_net), "infer smem");
+    if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM), "infer smem");
     const bool propose = mlp || rec_stride > 0;
     for (int iz = 0; iz < nz; iz++) {
         LayerPrm L;
@@ -1181,10 +1189,10 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
         L.prev_it_out = H->prev_it + (size_t)(iz & 1) * nsx;
         L.dd = H->dd;
         if (propose && ns > 0) {
-            feature_kernel<<<4 * sms, 256, 0, st>>>(H->prm, L);
+            feature_kernel<<<3 * sms, 256, 0, st>>>(H->prm, L);
             PPGPU_CHECK_LAUNCH("feature_kernel");
             if (mlp) {
-                infer_kernel<<<2 * sms, 128, smem_net, st>>>(H->prm, L, W, H->xtiles);
+                infer_kernel<<<sms, 128 * INFER_GROUPS, INFER_SMEM, st>>>(H->prm, L, W, H->xtiles);
                 PPGPU_CHECK_LAUNCH("infer_kernel");
             }
         }

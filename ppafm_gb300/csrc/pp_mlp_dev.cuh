@@ -97,6 +97,16 @@ __device__ __forceinline__ void cta_handoff() {
     tc_fence_after();
 }
 
+// The same for the 128 threads of warpgroup g alone (named barrier 1 + g), so several
+// warpgroups of a CTA can each run their own tile.
+__device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
+__device__ __forceinline__ void wg_handoff(int g) {
+    fence_async_smem();
+    tc_fence_before();
+    wg_sync(g);
+    tc_fence_after();
+}
+
 __device__ __forceinline__ uint32_t lane_addr(uint32_t tmem, int col) {
     const int warp = threadIdx.x >> 5;
     return tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)col;
@@ -113,7 +123,8 @@ __device__ __forceinline__ void store16_bf16(unsigned char *tile, int row, int k
     }
 }
 
-// act row <- bf16(SiLU(D row + b)) over 128 columns, 16 columns at a time.
+// act row <- bf16(SiLU(D row + b)) over 128 columns, 16 columns at a time (row = the
+// thread's index in its warpgroup = its TMEM lane).
 __device__ __forceinline__ void silu_epilogue(unsigned char *act, uint32_t tmem, const float *b) {
 #pragma unroll 1
     for (int c = 0; c < MLP_H; c += 16) {
@@ -121,36 +132,37 @@ __device__ __forceinline__ void silu_epilogue(unsigned char *act, uint32_t tmem,
         tmem_ld16(lane_addr(tmem, c), v);
 #pragma unroll
         for (int i = 0; i < 16; i++) v[i] = silu(v[i] + b[c + i]);
-        store16_bf16(act, threadIdx.x, c, v, MLP_H);
+        store16_bf16(act, threadIdx.x & 127, c, v, MLP_H);
     }
 }
 
-// Forward pass of the 128 samples whose inputs are in `act` (K = MLP_IN layout).  Leaves the
-// output row (16 floats, bias added) in y.  act is overwritten by the hidden activations.
-// Returns false if an MMA never completed (bounded wait).
+// Forward pass of the 128 samples whose inputs are in `act` (K = MLP_IN layout), run by
+// warpgroup g (its thread t owns sample t, TMEM lane t; MMAs accumulate at column tmem).
+// Leaves the output row (16 floats, bias added) in y.  act is overwritten by the hidden
+// activations.  Returns false if an MMA never completed (bounded wait).
 __device__ __forceinline__ bool mlp_forward(unsigned char *act, const unsigned char *W1t, const unsigned char *W2t,
                                             const unsigned char *W3t, const float *b1, const float *b2, const float *b3,
-                                            uint32_t tmem, uint64_t *bar, uint32_t &ph, float *y) {
-    const int tid = threadIdx.x;
+                                            uint32_t tmem, uint64_t *bar, uint32_t &ph, float *y, int g = 0) {
+    const bool leader = (threadIdx.x & 127) == 0;
     bool ok = true;
     // layer 1
-    if (tid == 0) {
+    if (leader) {
         tc_gemm(tmem, act, W1t, MLP_IN, MLP_H, false);
         tc_commit(bar);
     }
     ok &= mma_wait(bar, ph);
     silu_epilogue(act, tmem, b1);
-    cta_handoff();
+    wg_handoff(g);
     // layer 2
-    if (tid == 0) {
+    if (leader) {
         tc_gemm(tmem, act, W2t, MLP_H, MLP_H, false);
         tc_commit(bar);
     }
     ok &= mma_wait(bar, ph);
     silu_epilogue(act, tmem, b2);
-    cta_handoff();
+    wg_handoff(g);
     // layer 3
-    if (tid == 0) {
+    if (leader) {
         tc_gemm(tmem, act, W3t, MLP_H, MLP_OUT, false);
         tc_commit(bar);
     }
@@ -159,7 +171,7 @@ __device__ __forceinline__ bool mlp_forward(unsigned char *act, const unsigned c
 #pragma unroll
     for (int c = 0; c < MLP_OUT; c++) y[c] += b3[c];
     tc_fence_before();
-    __syncthreads();
+    wg_sync(g);
     tc_fence_after();
     return ok;
 }

@@ -16,6 +16,7 @@ many iterations a height takes.  Its training pairs come from plain FIRE itself
 """
 
 import ctypes
+import math
 
 import numpy as np
 import torch
@@ -72,9 +73,12 @@ class WarmStartNet:
         check(lib().ppgpu_mlp_forward(self.handle, tptr(X.contiguous()), n, tptr(Y), stream_handle()))
         return Y
 
-    def train(self, X, T, steps=1000, batch=8192, lr=1e-3, seed=0, log_every=100):
+    def train(self, X, T, steps=1000, batch=8192, lr=1e-3, seed=0, log_every=100, schedule="constant"):
         """Adam on the mean squared error of minibatches drawn uniformly from (X, T).
+        schedule: "constant" or "cosine" (lr decays to 2 % of lr by the last step).
         Returns [(step, loss)] every log_every steps."""
+        if schedule not in ("constant", "cosine"):
+            raise ValueError(f"unknown schedule {schedule!r}")
         n = X.shape[0]
         batch = min(batch, (n // 128) * 128)
         if batch < 128:
@@ -88,7 +92,8 @@ class WarmStartNet:
             idx = torch.randint(0, n, (batch,), generator=g, device=X.device, dtype=torch.int32)
             check(L.ppgpu_mlp_backward(self.handle, tptr(X), tptr(T), tptr(idx), batch, st))
             self.steps += 1
-            check(L.ppgpu_mlp_adam(self.handle, float(lr), self.steps, st))
+            lr_s = lr if schedule == "constant" else lr * (0.02 + 0.98 * 0.5 * (1.0 + math.cos(math.pi * s / max(1, steps - 1))))
+            check(L.ppgpu_mlp_adam(self.handle, float(lr_s), self.steps, st))
             if (s + 1) % log_every == 0 or s == steps - 1:
                 v = ctypes.c_double()
                 check(L.ppgpu_mlp_take_loss(self.handle, ctypes.byref(v), st))
