@@ -301,7 +301,7 @@ class BatchBench:
         self.torch.cuda.current_stream().synchronize()
         return h2d, d2h
 
-    def learned(self, args, plain_loop_ms, steps=30000, lr=1e-3):
+    def learned(self, args, plain_loop_ms, steps=120000, lr=1e-3):
         """Config-4 line: train the warm-start network on plain-FIRE pairs of a held-out batch
         (every 4th stroke of 256 other molecules: ~21M pairs; Adam, batch 8192, cosine-decayed
         learning rate, z error weighted 10x), then
@@ -362,7 +362,7 @@ class BatchBench:
             "training": {"pairs": npairs, "steps": steps, "batch": 8192, "lr": lr, "schedule": "cosine", "loss_weights": [1.0, 1.0, 10.0], "generate_s": t_gen, "train_s": t_train, "loss": log},
         }
 
-    def plain_ms(self, reps=2):
+    def plain_ms(self, reps=3):
         pls = self.BT.plain_loop(self.systems, self.w, self.relax)
         torch = self.torch
         for p in pls:

@@ -514,8 +514,8 @@ __device__ __forceinline__ void warp_features(const FeatTask *tk, int ntask, __n
         if (ch < CH && t < ntask && tk[t].gs >= 0) {
             const long long gs = tk[t].gs;
             const int4 v = reinterpret_cast<const int4 *>(row[t])[ch];
-            if (L.xtiles)
-                *reinterpret_cast<int4 *>(L.xtiles + (gs >> 7) * XTILE_BYTES + tile_off((int)(gs & 127), 8 * ch, MLP_IN)) = v;
+            if (L.xtiles)  // read once by the inference kernel: keep the force grids in L2 instead
+                st16_hint(L.xtiles + (gs >> 7) * XTILE_BYTES + tile_off((int)(gs & 127), 8 * ch, MLP_IN), v, l2_evict_first());
             if (L.rec_x && gs % L.rec_stride == 0)
                 reinterpret_cast<int4 *>(L.rec_x + ((gs / L.rec_stride) * L.nz_max + iz) * (MLP_IN * 2))[ch] = v;
         }
@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(128 * INFER_GROUPS, 1) infer_kernel(const Batc
         if (row == 0) {
             fence_async_smem();  // earlier generic writes of act ordered before the async copy
             mbar_expect_tx(&bar_copy[g], XBYTES);
-            bulk_g2s(act, Xtiles + tile * XBYTES, XBYTES, &bar_copy[g]);
+            bulk_g2s_hint(act, Xtiles + tile * XBYTES, XBYTES, &bar_copy[g], l2_evict_first());
         }
         ok &= tc_mbar_wait(&bar_copy[g], phc);
         phc ^= 1u;
