@@ -153,6 +153,12 @@ int ppgpu_relax_scan(const float *FE, const int *n, const double *cell, const do
                      float *ppos, int *iters, int nw, const double *df_weights, float *df,
                      unsigned long long *iter_total, void *stream);
 
+/* Lanes per stroke of ppgpu_relax_strokes / ppgpu_relax_scan (no reference counterpart):
+ * tps 1, 2, 4 or 8 lanes share each stroke's trilinear gathers (same results bit for bit);
+ * 0 restores the default, 1.  ppgpu_get_relax_tps returns the value used for nstroke strokes. */
+int ppgpu_set_relax_tps(int tps);
+int ppgpu_get_relax_tps(long long nstroke, int *out);
+
 /* AFMulator relaxation (relaxStrokesTilted, relax.cl:391-464, + convolveZ, relax.cl:571-608):
  * prm_afm[0..3] relax_params (dt, damp, -, -), [4..7] stiffness (kx,ky,kz,kr) already divided
  * by -eVA_Nm, [8..11] dpos0 (x,y,z,l0), [12..23] tip rows A,B,C (4 each, C[3] = -zstep),

@@ -88,10 +88,16 @@ __device__ __forceinline__ float4 interp_fe4(const float4 *__restrict__ FE, int 
 // double-floats, g_z = dic . (0, 0, z), so a height change needs no float64.
 constexpr int ZTAB = 4;
 
-template <bool SCAN>
+// TPS lanes per stroke (1, 2, 4 or 8): the lanes of a group hold the same state and split
+// each trilinear gather (interp_force_df_group, bit-identical to one lane); lane 0 of the
+// group writes the outputs.  More lanes per stroke put more warps in flight when a scan has
+// few strokes, which is what bounds this kernel.
+template <bool SCAN, int TPS>
 __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, const StrokeIO S, const ScanIO C) {
     extern __shared__ dfl ztab[];
-    const int s = blockIdx.x * RELAX_THREADS + threadIdx.x;
+    const int s = (blockIdx.x * RELAX_THREADS + threadIdx.x) / TPS;
+    const int sub = (int)(threadIdx.x % TPS);
+    const bool lead = sub == 0;
     const int nstroke = SCAN ? C.nx * C.ny : S.nstroke;
     const int nstep = SCAN ? C.nz : S.nstep;
     if (SCAN) {
@@ -147,15 +153,17 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
         set_height(0);
     }
 
-    while (__any_sync(FULL, active)) {
+    unsigned am;
+    while ((am = __ballot_sync(FULL, active)) != 0u) {
         if (!active) continue;
         dfl u[3], F[3];
         grid_coord_df(P.dic, P.diag, tf, d, u);
-        interp_force_df(P.FE, P.n0, P.n1, P.n2, base, u, F);
+        interp_force_df_group<TPS>(P.FE, P.n0, P.n1, P.n2, base, u, F, sub, am);
         if (fin) {
             // outputs of height iz: position after the last move, grid force there
             const dfl r[3] = {df_add(tip[0], d[0]), df_add(tip[1], d[1]), df_add(tip[2], d[2])};
-            if (SCAN) {
+            if (!lead) {
+            } else if (SCAN) {
                 const long long o = (long long)s * nstep + (nstep - 1 - iz);
                 if (C.fzs) C.fzs[o] = df_round(F[2]);
                 if (C.ppos) {
@@ -178,8 +186,8 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
             iz++;
             if (iz == nstep) {
                 active = false;
-                if (!SCAN && S.itrsum) S.itrsum[s] = itsum;
-                if (SCAN && C.df && C.fzs && C.nw > 0) {
+                if (!SCAN && S.itrsum && lead) S.itrsum[s] = itsum;
+                if (SCAN && C.df && C.fzs && C.nw > 0 && lead) {
                     // np.convolve(fzs, W, 'valid') along ascending z (Fz2df, common.py:421-430)
                     const float *f = C.fzs + (long long)s * nstep;
                     const int nout = nstep - C.nw + 1;
@@ -212,7 +220,7 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
         }
         const float3 f = pp_force_df(P, F, d);
         const float ff = relax_move_df(P, f, d, v, dt, acoef);
-        mine++;
+        mine += lead ? 1 : 0;
         if (ff < P.convF2f) {
             itcount = it;
             fin = true;
@@ -352,9 +360,42 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_afm_kernel(const AfmPrm P
 
 // ---------------------------------------------------------------------- host
 
+// Lanes per stroke (ppgpu_set_relax_tps).  One lane per stroke is the default: on GB300 the
+// scans measured here (16k-26k strokes) ran 15-20 % slower with 4 lanes per stroke, because
+// every lane of a group also executes the stroke's FIRE arithmetic, which outweighs the
+// latency hidden by the extra warps.
+static int g_relax_tps = 1;
+
+static int relax_tps(long long) { return g_relax_tps; }
+
+template <bool SCAN>
+static void launch_relax(int tps, long long nstroke, size_t smem, cudaStream_t st, const RelaxPrm &P, const StrokeIO &S,
+                         const ScanIO &C) {
+    const unsigned nblk = (unsigned)((nstroke * tps + RELAX_THREADS - 1) / RELAX_THREADS);
+    switch (tps) {
+    case 8: relax_kernel<SCAN, 8><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    case 4: relax_kernel<SCAN, 4><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    case 2: relax_kernel<SCAN, 2><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    default: relax_kernel<SCAN, 1><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    }
+}
+
 }  // namespace ppgpu
 
 using namespace ppgpu;
+
+extern "C" int ppgpu_set_relax_tps(int tps) {
+    if (tps != 0 && tps != 1 && tps != 2 && tps != 4 && tps != 8)
+        return set_error(PPGPU_ERR_ARG, "set_relax_tps: %d not in {0 (default), 1, 2, 4, 8}", tps);
+    g_relax_tps = tps ? tps : 1;
+    return set_ok();
+}
+
+extern "C" int ppgpu_get_relax_tps(long long nstroke, int *out) {
+    if (!out || nstroke < 0) return set_error(PPGPU_ERR_ARG, "get_relax_tps: bad arguments");
+    *out = relax_tps(nstroke);
+    return set_ok();
+}
 
 extern "C" int ppgpu_relax_strokes(const float *FE, const int *n, const double *cell, const double *prm,
                                    int probeStart, int relaxAlg, int nstroke, int nstep, const double *rTips,
@@ -370,8 +411,7 @@ extern "C" int ppgpu_relax_strokes(const float *FE, const int *n, const double *
     StrokeIO S = {nstroke, nstep, rTips, rs, fs, iters, itrsum};
     ScanIO C;
     memset(&C, 0, sizeof(C));
-    const unsigned nblk = (unsigned)((nstroke + RELAX_THREADS - 1) / RELAX_THREADS);
-    relax_kernel<false><<<nblk, RELAX_THREADS, 0, (cudaStream_t)stream>>>(P, S, C);
+    launch_relax<false>(relax_tps(nstroke), nstroke, 0, (cudaStream_t)stream, P, S, C);
     PPGPU_CHECK_LAUNCH("relax_kernel<strokes>");
     return set_ok();
 }
@@ -410,10 +450,9 @@ extern "C" int ppgpu_relax_scan(const float *FE, const int *n, const double *cel
     C.nw = df ? nw : 0;
     for (int i = 0; i < C.nw; i++) C.W[i] = (float)df_weights[i];
     const long long npix = (long long)nx * ny;
-    const unsigned nblk = (unsigned)((npix + RELAX_THREADS - 1) / RELAX_THREADS);
     const size_t smem = (size_t)nz * ZTAB * sizeof(dfl);
     if (smem > 48 * 1024) return set_error(PPGPU_ERR_ARG, "relax_scan: nz = %d heights exceed the table limit (1536)", nz);
-    relax_kernel<true><<<nblk, RELAX_THREADS, smem, (cudaStream_t)stream>>>(P, S, C);
+    launch_relax<true>(relax_tps(npix), npix, smem, (cudaStream_t)stream, P, S, C);
     PPGPU_CHECK_LAUNCH("relax_kernel<scan>");
     return set_ok();
 }

@@ -85,6 +85,70 @@ __device__ __forceinline__ void interp_force_df(const float4 *FE, int n0, int n1
     }
 }
 
+// interp_force_df split over a group of TPS lanes (TPS in {1, 2, 4, 8}, groups aligned in the
+// warp, sub = lane index in the group, mask = the warp's participating lanes): lane sub gathers
+// and weighs corners sub * 8/TPS .. +8/TPS-1, and the partial sums are combined by xor
+// shuffles in the same pairing as the one-lane sum ((c0+c1)+(c2+c3))+((c4+c5)+(c6+c7)).
+// TwoSum is exact whatever the operand order, so every lane of the group gets the one-lane
+// result bit for bit.
+template <int TPS, bool NC = true>
+__device__ __forceinline__ void interp_force_df_group(const float4 *FE, int n0, int n1, int n2, const int base[3],
+                                                      const dfl u[3], dfl F[3], int sub, unsigned mask) {
+    if constexpr (TPS == 1) {
+        interp_force_df<NC>(FE, n0, n1, n2, base, u, F);
+    } else {
+        constexpr int CPL = 8 / TPS;  // corners per lane
+        auto ld = [&](const float4 *q) { return NC ? ldg4(q) : *q; };
+        int ci[3];
+        dfl t[3], m[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            t[k] = split_cell(u[k], ci[k]);
+            ci[k] += base[k];
+            const dfl o = two_sum(1.f, -t[k].h);
+            m[k] = {o.h, __fsub_rn(o.l, t[k].l)};
+        }
+        const int ix0 = wrap_index(ci[0], n0), iy0 = wrap_index(ci[1], n1), iz0 = wrap_index(ci[2], n2);
+        const int ix1 = (ix0 + 1 == n0) ? 0 : ix0 + 1;
+        const int iy1 = (iy0 + 1 == n1) ? 0 : iy0 + 1;
+        const int iz1 = (iz0 + 1 == n2) ? 0 : iz0 + 1;
+        float4 c[CPL];
+        dfl w[CPL];
+#pragma unroll
+        for (int i = 0; i < CPL; i++) {
+            const int k = sub * CPL + i;  // corner bits (x, y, z) = (k >> 2, (k >> 1) & 1, k & 1)
+            const int bx = k >> 2, by = (k >> 1) & 1, bz = k & 1;
+            c[i] = ld(FE + ((long long)(bx ? ix1 : ix0) * n1 + (by ? iy1 : iy0)) * n2 + (bz ? iz1 : iz0));
+            w[i] = df_mul(df_mul(bx ? t[0] : m[0], by ? t[1] : m[1]), bz ? t[2] : m[2]);
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; comp++) {
+            dfl p[CPL];
+#pragma unroll
+            for (int i = 0; i < CPL; i++) {
+                const float v = comp == 0 ? c[i].x : (comp == 1 ? c[i].y : c[i].z);
+                p[i] = two_prod(w[i].h, v);
+                p[i].l = __fmaf_rn(w[i].l, v, p[i].l);
+            }
+            dfl r;
+            if constexpr (CPL == 4)
+                r = df_add_raw(df_add_raw(p[0], p[1]), df_add_raw(p[2], p[3]));
+            else if constexpr (CPL == 2)
+                r = df_add_raw(p[0], p[1]);
+            else
+                r = p[0];
+#pragma unroll
+            for (int off = 1; off < TPS; off <<= 1) {
+                dfl o;
+                o.h = __shfl_xor_sync(mask, r.h, off);
+                o.l = __shfl_xor_sync(mask, r.l, off);
+                r = df_add_raw(r, o);
+            }
+            F[comp] = two_sum(r.h, r.l);
+        }
+    }
+}
+
 // Grid coordinate g_k = r . dicell_row_k of a float64 position (Grid.h:46-50).
 __device__ __forceinline__ double3 to_grid(const RelaxPrm &P, double x, double y, double z) {
     return make_double3(fma(z, P.dicd[2], fma(y, P.dicd[1], x * P.dicd[0])),

@@ -139,3 +139,56 @@ def test_fz2df_gpu_golden(gpulib, golden):
     assert np.abs(d2 - g["df2"]).max() < 1e-3
     with pytest.raises(ValueError):
         common.Fz2df(g["Fz"][..., :5], dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)
+
+
+@pytest.mark.parametrize("tps", [2, 4, 8])
+def test_lanes_per_stroke_bit_identical(gpulib, oracle, golden, tps):
+    """Splitting each stroke's gathers over 2, 4 or 8 lanes gives the one-lane results bit for
+    bit (scan and stroke entry points), including iteration counts."""
+    import ctypes
+
+    import torch
+
+    from ppafm_gb300 import _lib, device
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = g["lvec"]
+    ff = device.DeviceFF(g["n"], lv).from_host_f64(FF.reshape(-1, 3))
+
+    def run():
+        out = device.relax_scan(ff, prm, xT - lv[0, 0], yT - lv[0, 1], zT[::-1] - lv[0, 2], pos_offset=lv[0], want_iters=True)
+        torch.cuda.synchronize()
+        return {k: v.clone() for k, v in out.items()}
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import core
+
+    FFc = np.ascontiguousarray(FF)
+    HL.setFF(FFc, lvec=lv)
+    core.setRelax(300, 1e-8, 0.5, 0.1)
+    core.setFIRE(1.1, 0.5, 0.99)
+    core.setTip(lRadial=4.0, kRadial=20.0 / -16.0217662, rPP0=np.array([0.0, 0.0, 0.0]), kSpring=np.array([0.25, 0.25, 0.0]) / -16.0217662)
+    rT = oracle.scan_tips(xT[::3], yT[::3], zT, lv[0])
+
+    def strokes():
+        rs, fs = np.zeros_like(rT), np.zeros_like(rT)
+        core.relaxTipStrokes_omp(rT, rs, fs, probeStart=1, relaxAlg=1)
+        return rs, fs
+
+    L = _lib.lib()
+    try:
+        _lib.check(L.ppgpu_set_relax_tps(1))
+        ref, ref_s = run(), strokes()
+        _lib.check(L.ppgpu_set_relax_tps(tps))
+        got, got_s = run(), strokes()
+    finally:
+        _lib.check(L.ppgpu_set_relax_tps(0))
+        core.deleteFF_Fpointer()
+    for k in ref:
+        assert ref[k].equal(got[k]), k
+    assert np.array_equal(ref_s[0], got_s[0]) and np.array_equal(ref_s[1], got_s[1])
+    t = ctypes.c_int()
+    _lib.check(L.ppgpu_get_relax_tps(16384, ctypes.byref(t)))
+    assert t.value in (1, 2, 4, 8)
+    with pytest.raises(_lib.PPGPUError):
+        _lib.check(L.ppgpu_set_relax_tps(3))
