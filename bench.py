@@ -491,7 +491,7 @@ def run_batch(args, rank, world, local):
             "frac": flops / (t_step_max / K) / 1e12 / peak if peak else None,
             "peak_source": "FFMA microbenchmark measured in this run; achieved counts only the force-field flops over the whole step",
             "flops_per_launch": flops,
-            "traffic": None,
+            "traffic": read_profile_traffic("batch_kernel", "molecule_batch") if (args.nmol, args.scale) == (256, 1.0) else None,
         },
         "cpu_baseline": None,
         "clocks": clk,
