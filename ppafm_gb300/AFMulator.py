@@ -46,7 +46,7 @@ class AFMulator:
         if rho is not None or rho_delta is not None:
             raise NotImplementedError("tip densities (Hartree / FDBM force fields) are not supported")
         self.iZPP = iZPP
-        self.tipR0 = tipR0
+        self.tipR0 = np.array(tipR0, dtype=np.float64)  # a copy: randomize_tip edits it in place
         self.f0Cantilever = f0Cantilever
         self.kCantilever = kCantilever
         self.npbc = npbc
@@ -157,8 +157,10 @@ class AFMulator:
         p[24:28] = 0.0
         return p
 
-    def evalAFM(self, X=None, stream=None, keep_device=False, want_paths=False, want_iters=False):
-        """Relaxation + z convolution of the prepared force field (AFMulator.py:447-479)."""
+    def evalAFM(self, X=None, stream=None, keep_device=False, want_paths=False, want_iters=False, out=None):
+        """Relaxation + z convolution of the prepared force field (AFMulator.py:447-479).
+        out: a contiguous float32 device tensor [nx, ny, nz - df_steps + 1] that receives the
+        image (returned as is, nothing is copied to the host)."""
         ff = self._ff
         nx, ny, nz = self.scan_dim
         npix = nx * ny
@@ -178,7 +180,13 @@ class AFMulator:
         prm = self._afm_params()
         W = np.ascontiguousarray(self.dfWeight, dtype=np.float64)
         o = self._out
-        check(lib().ppgpu_relax_afm(tptr(ff.FE), iptr(ff.n), dptr(invCell), dptr(prm), npix, tptr(self._points), nz, tptr(o["FEs"]), tptr(o.get("paths")), tptr(o.get("iters")), nw, dptr(W), tptr(o["X"]), tptr(self.counter), stream_handle(stream)))
+        if out is not None:
+            if tuple(out.shape) != (nx, ny, nout) or out.dtype != torch.float32 or not out.is_contiguous() or out.device != dev:
+                raise ValueError(f"out must be a contiguous float32 tensor of shape {(nx, ny, nout)} on {dev}")
+        Xt = o["X"] if out is None else out
+        check(lib().ppgpu_relax_afm(tptr(ff.FE), iptr(ff.n), dptr(invCell), dptr(prm), npix, tptr(self._points), nz, tptr(o["FEs"]), tptr(o.get("paths")), tptr(o.get("iters")), nw, dptr(W), tptr(Xt), tptr(self.counter), stream_handle(stream)))
+        if out is not None:
+            return out
         Xd = o["X"].view(nx, ny, nout)
         if keep_device:
             return Xd

@@ -1,0 +1,104 @@
+"""The ML generators on the GPU path: the reference's generator test (batch count and
+shapes, tests/test_generator.py of ppafm) and image-for-image equality with AFMulator.eval
+for both the deferred (one copy per batch) and the per-image host-copy mode."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_generator_afm_trainer_batches(gpulib):
+    from ppafm_gb300.AFMulator import AFMulator
+    from ppafm_gb300.ml.Generator import GeneratorAFMtrainer
+
+    n_sample, batch_size, n_atoms = 12, 5, 10
+    rng = np.random.default_rng(0)
+    np.random.seed(0)
+
+    class TestTrainer(GeneratorAFMtrainer):
+        def on_batch_start(self):
+            self.randomize_tip(max_tilt=0.5)
+
+        def on_afm_start(self):
+            self.randomize_distance(delta=0.5)
+
+    def generator():
+        for _ in range(n_sample):
+            yield {"xyzs": 10 * rng.random((n_atoms, 3)), "Zs": rng.integers(1, 16, n_atoms)}
+
+    class Disks:  # a stand-in aux map (the reference's are OpenCL); follows the scan window
+        scan_window = None
+
+        def __call__(self, xyzqs, Zs, pot, rot):
+            return np.full((100, 100), float(len(Zs)), dtype=np.float32)
+
+    afmulator = AFMulator(scan_dim=(100, 100, 20), scan_window=((0, 0, 5), (10, 10, 7)))
+    aux = Disks()
+    trainer = TestTrainer(afmulator=afmulator, aux_maps=[aux], sample_generator=generator(), sim_type="LJ", batch_size=batch_size, iZPPs=[8, 54])
+    i_batch = -1
+    for i_batch, (Xs, Ys, mols, sws) in enumerate(trainer):
+        nb = 5 if i_batch < 2 else 2
+        assert Xs.shape == (nb, 2, 100, 100, 11)
+        assert Ys.shape == (nb, 1, 100, 100)
+        assert len(mols) == nb and all(m.shape == (n_atoms, 5) for m in mols)
+        assert sws.shape == (nb, 2, 2, 3)
+        assert np.isfinite(Xs).all() and np.abs(Xs).max() > 0
+    assert i_batch == 2
+    assert aux.scan_window is not None
+    with pytest.raises(NotImplementedError):
+        GeneratorAFMtrainer(afmulator, [], generator(), sim_type="LJ+Hartree")
+
+
+def _write_molecules(tmp_path, n, rng):
+    from ppafm_gb300.io import saveXYZ
+
+    paths = []
+    for k in range(n):
+        na = int(rng.integers(8, 20))
+        xyz = np.c_[rng.random((na, 2)) * 8.0, rng.random(na) * 0.5]
+        Zs = rng.choice([1, 6, 7, 8], na)
+        q = rng.uniform(-0.3, 0.3, na)
+        q -= q.mean()
+        p = tmp_path / f"mol{k}.xyz"
+        saveXYZ(p, xyz, Zs, q)
+        paths.append(str(p))
+    return paths
+
+
+@pytest.mark.parametrize("host_copy_each", [False, True])
+def test_inverse_trainer_matches_eval(gpulib, tmp_path, host_copy_each):
+
+    from ppafm_gb300.AFMulator import AFMulator
+    from ppafm_gb300.ml.Generator import InverseAFMtrainer
+
+    rng = np.random.default_rng(5)
+    paths = _write_molecules(tmp_path, 5, rng)
+    seen = []
+
+    class Recorder(InverseAFMtrainer):
+        def on_afm_start(self):  # what AFMulator.eval gets for this image
+            seen.append((self.xyzs.copy(), self.Zs.copy(), self.qs.copy(), self.REAs.copy(), self.afmulator.iZPP, self.afmulator.Qs.copy(), self.afmulator.QZs.copy()))
+
+    class HostEach(Recorder):
+        def on_afm_end(self):
+            assert isinstance(self.Xs, np.ndarray)
+            self.host_images.append(self.Xs.copy())
+
+    cls = HostEach if host_copy_each else Recorder
+    afm = AFMulator(scan_dim=(64, 64, 20), scan_window=((2.0, 2.0, 7.0), (10.0, 10.0, 9.0)))
+    tr = cls(afm, [], paths, batch_size=3, iZPPs=[8, 8], Qs=[[-10, 20, -10, 0], [0, 0, 0, 0]], QZs=[[0.1, 0, -0.1, 0], [0, 0, 0, 0]])
+    tr.host_images = []
+    assert len(tr) == 1
+    batches = list(tr)
+    assert [b[0][0].shape[0] for b in batches] == [3, 2]
+    images = [X[t][s] for Xs, _, _ in batches for s in range(Xs[0].shape[0]) for t in range(2) for X in [Xs]]
+    assert len(images) == len(seen) == 10
+    ref = AFMulator(scan_dim=(64, 64, 20), scan_window=((2.0, 2.0, 7.0), (10.0, 10.0, 9.0)))
+    for img, (xyz, Zs, qs, REAs, iZPP, Qs, QZs) in zip(images, seen):
+        ref.iZPP = iZPP
+        ref.setQs(Qs, QZs)
+        want = ref.eval(xyz, Zs, qs, REAs=REAs)
+        assert np.array_equal(img, want)
+    if host_copy_each:
+        assert all(np.array_equal(a, b) for a, b in zip(tr.host_images, images))
