@@ -363,3 +363,39 @@ class DensityOverlapPipeline:
 
     def iterations(self):
         return int(self.counter.item())
+
+
+# ------------------------------------------------------------ file hand-off between stages
+# The relaxed-scan stage writes Fz to <dir>/OutFz (cli/relaxed_scan.py:184-188); the plotting
+# stage reads it back, converts to Δf and writes <dir>/df with the lattice of the Δf stack
+# (cli/plot_results.py:296-316).  Same files, Fz2df on the GPU.
+
+
+def save_OutFz(dirname, fzs, lvec_scan, data_format="xsf", head=None):
+    """Writes the relaxed scan's Fz [nx, ny, nz] as <dirname>/OutFz.xsf (or .npz)."""
+    import os
+
+    from . import io as pio
+
+    os.makedirs(dirname, exist_ok=True)
+    kw = {} if head is None else dict(head=head, atomic_info=head)
+    pio.save_scal_field(os.path.join(dirname, "OutFz"), fzs, lvec_scan, data_format=data_format, **kw)
+
+
+def OutFz_to_df(dirname, dz, amplitude, k0, f0, data_format="xsf", save_df=True):
+    """Reads <dirname>/OutFz, converts it to Δf (common.Fz2df, on the GPU) and, with save_df,
+    writes <dirname>/df.  The Δf stack's lattice starts amplitude/2 higher and is amplitude
+    shorter along z.  Returns (dfs, lvec_df)."""
+    import os
+
+    from . import io as pio
+
+    fzs, lvec, _, info = pio.load_scal_field(os.path.join(dirname, "OutFz"), data_format=data_format)
+    dfs = PPU.Fz2df(fzs, dz=dz, k0=k0, f0=f0, amplitude=amplitude)
+    lvec_df = np.array(lvec.copy())
+    lvec_df[0][2] += amplitude / 2
+    lvec_df[3][2] -= amplitude
+    if save_df:
+        kw = {} if data_format != "xsf" or not isinstance(info, list) else dict(head=info)
+        pio.save_scal_field(os.path.join(dirname, "df"), dfs, lvec_df, data_format=data_format, **kw)
+    return dfs, lvec_df

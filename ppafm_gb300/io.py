@@ -1,5 +1,5 @@
-"""Molecule files: the xyz reader and writer of ppafm/io.py:19-110 (the format the ML
-generator reads its molecules from).
+"""Files of the hot path's stages, restating ppafm/io.py: molecules (xyz, io.py:19-110) and
+grids (XSF datagrids and npz, io.py:563-620, 716-880).
 
 An xyz file is: the atom count, a comment line, then one line per atom with the element
 (symbol or atomic number), x, y, z and optional extra columns.  Charges are the first extra
@@ -67,3 +67,151 @@ def saveXYZ(fname, xyzs, Zs, qs=None, comment="", append=False):
             if qs is not None:
                 line += f" {qs[i]:10.6f}"
             f.write(line + "\n")
+
+
+# --------------------------------------------------------------------- grid files
+# XSF datagrids and npz grids of ppafm/io.py:563-620, 716-880: the files the reference's
+# command-line stages hand to each other (force fields, Fz and Δf stacks).  A datagrid has
+# one more point than the data along each axis: the first plane is repeated as the last.
+
+XSF_HEAD_DEFAULT = """
+ATOMS
+ 1   0.0   0.0   0.0
+
+BEGIN_BLOCK_DATAGRID_3D
+   some_datagrid
+   BEGIN_DATAGRID_3D_whatever
+"""
+
+
+def _ortho_lvec(sh, dd):
+    return [[0, 0, 0], [sh[2] * dd[0], 0, 0], [0, sh[1] * dd[1], 0], [0, 0, sh[0] * dd[2]]]
+
+
+def _row(vals):
+    return " ".join(str(x) for x in vals) + "\n"
+
+
+def saveXSFData(fname, data, lvec=None, dd=None, head=XSF_HEAD_DEFAULT, data_is_xyz_order=True):
+    """Writes a scalar grid (x, y, z order unless data_is_xyz_order is False) as an XSF datagrid,
+    values "%10.5e" with x fastest, the periodic edge repeated."""
+    data = np.asarray(data)
+    if data_is_xyz_order:
+        data = data.transpose((2, 1, 0))
+    if lvec is None:
+        lvec = _ortho_lvec(data.shape, dd if dd is not None else [1.0, 1.0, 1.0])
+    n = data.shape
+    d2 = np.zeros(np.array(n) + 1)
+    d2[:-1, :-1, :-1] = data
+    d2[-1, :, :] = d2[0, :, :]
+    d2[:, -1, :] = d2[:, 0, :]
+    d2[:, :, -1] = d2[:, :, 0]
+    with open(fname, "w") as f:
+        for line in head:
+            f.write(line)
+        f.write(_row((n[2] + 1, n[1] + 1, n[0] + 1)))
+        for vec in lvec:
+            f.write(_row(vec))
+        np.savetxt(f, d2.reshape(-1, 1), fmt="%10.5e")
+        f.write("   END_DATAGRID_3D\n")
+        f.write("END_BLOCK_DATAGRID_3D\n")
+
+
+def loadXSFData(fname, xyz_order=True):
+    """(data, lvec [4, 3], grid size, header lines) of an XSF datagrid; data in x, y, z order
+    unless xyz_order is False, without the repeated edge."""
+    head = []
+    with open(fname) as f:
+        while True:
+            line = f.readline()
+            head.append(line)
+            if not line or "BEGIN_DATAGRID_3D" in line:
+                break
+        nDim = np.array([int(x) for x in f.readline().split()][::-1])
+        lvec = np.array([[float(x) for x in f.readline().split()] for _ in range(4)])
+        count = int(np.prod(nDim))
+        vals = np.array(f.read().split()[:count], dtype=np.float64)
+    if vals.size != count:
+        raise ValueError(f"{fname}: {vals.size} grid values, expected {count}")
+    F = vals.reshape(nDim)[:-1, :-1, :-1]
+    if xyz_order:
+        F = F.transpose((2, 1, 0))
+        nDim = nDim[::-1].copy()
+    return F.copy(), lvec, nDim - 1, head
+
+
+def packVecGrid(Fx, Fy, Fz, FF=None):
+    if FF is None:
+        FF = np.zeros(np.shape(Fx) + (3,))
+    FF[..., 0] = Fx
+    FF[..., 1] = Fy
+    FF[..., 2] = Fz
+    return FF
+
+
+def unpackVecGrid(FF):
+    return FF[..., 0].copy(), FF[..., 1].copy(), FF[..., 2].copy()
+
+
+def limit_vec_field(FF, Fmax=100.0):
+    """|F| <= Fmax in place, directions kept (io.py:766-778; on the GPU: ppgpu_clamp_grid)."""
+    FR = np.sqrt(FF[..., 0] ** 2 + FF[..., 1] ** 2 + FF[..., 2] ** 2).ravel()
+    mask = FR > Fmax
+    for k in range(3):
+        FF[..., k].flat[mask] *= Fmax / FR[mask]
+
+
+def saveNpy(fname, data, lvec, atomic_info):
+    np.savez(fname + ".npz", data=data, lvec=lvec, atoms=atomic_info[0], lvec0=atomic_info[1])
+
+
+def loadNpy(fname):
+    d = np.load(fname + ".npz")
+    return d["data"].copy(), d["lvec"], (d["atoms"], d["lvec0"])
+
+
+def save_vec_field(fname, data, lvec, data_format="xsf", head=XSF_HEAD_DEFAULT, atomic_info=None):
+    """fname_x/_y/_z.xsf, or fname.npz with keys FF, lvec, atoms, lvec0 (data [.., .., .., 3])."""
+    if data_format == "xsf":
+        for k, c in enumerate("xyz"):
+            saveXSFData(f"{fname}_{c}.xsf", data[..., k], lvec, head=head)
+    elif data_format == "npy":
+        atomic_info = atomic_info if atomic_info is not None else (np.zeros((4, 1)), lvec)
+        np.savez(fname + ".npz", FF=data, lvec=lvec, atoms=atomic_info[0], lvec0=atomic_info[1])
+    else:
+        raise ValueError(f"Cannot save vector field in format: {data_format}")
+
+
+def load_vec_field(fname, data_format="xsf"):
+    """(data [.., .., .., 3], lvec, grid size, header or (atoms, lvec0))."""
+    if data_format == "xsf":
+        comps = [loadXSFData(f"{fname}_{c}.xsf") for c in "xyz"]
+        data = packVecGrid(comps[0][0], comps[1][0], comps[2][0])
+        lvec, nDim, info = comps[2][1], comps[2][2], comps[2][3]
+    elif data_format == "npy":
+        d = np.load(fname + ".npz")
+        data, lvec, info = d["FF"], d["lvec"], (d["atoms"], d["lvec0"])
+        nDim = data.shape
+    else:
+        raise ValueError(f"Cannot load vector field in format: {data_format}")
+    return data.copy(), lvec, nDim, info
+
+
+def save_scal_field(fname, data, lvec, data_format="xsf", head=XSF_HEAD_DEFAULT, atomic_info=None):
+    if data_format == "xsf":
+        saveXSFData(fname + ".xsf", data, lvec, head=head)
+    elif data_format == "npy":
+        saveNpy(fname, data, lvec, atomic_info if atomic_info is not None else (np.zeros((4, 1)), lvec))
+    else:
+        raise ValueError(f"Cannot save scalar field in format: {data_format}")
+
+
+def load_scal_field(fname, data_format="xsf"):
+    if data_format == "xsf":
+        data, lvec, nDim, info = loadXSFData(fname + ".xsf")
+    elif data_format == "npy":
+        data, lvec, info = loadNpy(fname)
+        nDim = data.shape
+    else:
+        raise ValueError(f"Cannot load scalar field in format: {data_format}")
+    return data.copy(), lvec, nDim, info

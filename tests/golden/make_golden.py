@@ -37,8 +37,14 @@ def setup_reference(ref_root):
     return tmp
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root="/root/reference", only=None):
     tmp = setup_reference(ref_root)
+    if only == "xsf":
+        try:
+            make_xsf(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        return
     try:
         import ppafm.common as PPU
         import ppafm.core as core
@@ -188,6 +194,26 @@ def main(ref_root="/root/reference"):
         print("golden fixtures written to", HERE)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
+
+
+def make_xsf(tmp):
+    """Grid files written by the reference's io (io.py:575-598, 781-842): an XSF scalar field,
+    an XSF vector field (three files) and the npz forms, under tests/golden/xsf/."""
+    import ppafm.io as pio
+
+    out = os.path.join(HERE, "xsf")
+    os.makedirs(out, exist_ok=True)
+    rng = np.random.default_rng(777)
+    lvec = np.array([[0.5, -0.25, 1.0], [6.0, 0.0, 0.0], [1.5, 5.0, 0.0], [0.0, 0.0, 4.0]])
+    S = rng.normal(size=(5, 4, 3))
+    V = rng.normal(size=(5, 4, 3, 3))
+    pio.saveXSFData(os.path.join(out, "scal.xsf"), S, lvec)
+    pio.save_vec_field(os.path.join(out, "vec"), V, lvec, data_format="xsf")
+    pio.save_vec_field(os.path.join(out, "vec"), V, lvec, data_format="npy")
+    pio.save_scal_field(os.path.join(out, "scal"), S, lvec, data_format="npy")
+    pio.saveXSFData(os.path.join(out, "ortho.xsf"), S[:, :, :2], dd=[0.1, 0.2, 0.3])
+    np.savez(os.path.join(out, "inputs.npz"), S=S, V=V, lvec=lvec)
+    print("xsf fixtures written to", out)
 
 
 if __name__ == "__main__":

@@ -192,3 +192,19 @@ def test_lanes_per_stroke_bit_identical(gpulib, oracle, golden, tps):
     assert t.value in (1, 2, 4, 8)
     with pytest.raises(_lib.PPGPUError):
         _lib.check(L.ppgpu_set_relax_tps(3))
+
+
+@pytest.mark.parametrize("fmt", ["xsf", "npy"])
+def test_outfz_file_handoff(gpulib, golden, tmp_path, fmt):
+    """Relaxed-scan Fz through the OutFz file and back to Δf (the CLI stages' hand-off):
+    Δf equals the reference's within 0.1 Hz after the 6-digit XSF round trip."""
+    from ppafm_gb300 import HighLevel as HL
+
+    g = golden("relax")
+    lv = np.array(g["lvecScan"])
+    HL.save_OutFz(str(tmp_path), g["fzs"], lv, data_format=fmt)
+    dfs, lvec_df = HL.OutFz_to_df(str(tmp_path), dz=0.1, amplitude=1.0, k0=1800.0, f0=30000.0, data_format=fmt)
+    assert np.abs(dfs - g["df"]).max() < DF_TOL
+    assert np.isclose(lvec_df[0][2], lv[0][2] + 0.5) and np.isclose(lvec_df[3][2], lv[3][2] - 1.0)
+    ext = ".xsf" if fmt == "xsf" else ".npz"
+    assert (tmp_path / ("df" + ext)).exists()

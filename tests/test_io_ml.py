@@ -66,3 +66,53 @@ def test_rotation_helpers():
     up, side = np.eye(3), np.array([[0.0, 0, 1], [0, 1, 0], [1, 0, 0]])
     # looking down z every atom is at the top (entropy 3); down x only one is
     assert sortRotationsByEntropy(flat, [side, up])[0] is up
+
+
+def _xsf_inputs():
+    import os
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "xsf", "inputs.npz"))
+    return d["S"], d["V"], d["lvec"]
+
+
+def test_xsf_files_match_the_reference(tmp_path):
+    """Byte-identical XSF files (scalar, vector, default orthogonal cell) and identical loads of
+    the files the reference wrote (tests/golden/xsf, made by tests/golden/make_golden.py)."""
+    import os
+
+    from ppafm_gb300 import io as pio
+
+    g = os.path.join(os.path.dirname(__file__), "golden", "xsf")
+    S, V, lvec = _xsf_inputs()
+    pio.saveXSFData(tmp_path / "scal.xsf", S, lvec)
+    assert (tmp_path / "scal.xsf").read_text() == open(os.path.join(g, "scal.xsf")).read()
+    pio.saveXSFData(tmp_path / "ortho.xsf", S[:, :, :2], dd=[0.1, 0.2, 0.3])
+    assert (tmp_path / "ortho.xsf").read_text() == open(os.path.join(g, "ortho.xsf")).read()
+    pio.save_vec_field(str(tmp_path / "vec"), V, lvec, data_format="xsf")
+    for c in "xyz":
+        assert (tmp_path / f"vec_{c}.xsf").read_text() == open(os.path.join(g, f"vec_{c}.xsf")).read()
+    F, lv, n, head = pio.loadXSFData(os.path.join(g, "scal.xsf"))
+    assert np.allclose(F, S, rtol=1e-5, atol=1e-5) and np.allclose(lv, lvec) and list(n) == list(S.shape)
+    assert any("BEGIN_DATAGRID_3D" in h for h in head)
+    FF, lv, n, _ = pio.load_vec_field(os.path.join(g, "vec"), "xsf")
+    assert FF.shape == V.shape and np.allclose(FF, V, rtol=1e-5, atol=1e-5)
+    FF, lv, n, info = pio.load_vec_field(os.path.join(g, "vec"), "npy")
+    assert np.array_equal(FF, V) and np.array_equal(lv, lvec) and np.array_equal(info[1], lvec)
+    D, lv, n, info = pio.load_scal_field(os.path.join(g, "scal"), "npy")
+    assert np.array_equal(D, S)
+    # npz written here loads with the same keys
+    pio.save_vec_field(str(tmp_path / "v2"), V, lvec, data_format="npy")
+    ref = np.load(os.path.join(g, "vec.npz"))
+    got = np.load(tmp_path / "v2.npz")
+    assert sorted(ref.files) == sorted(got.files) and all(np.array_equal(ref[k], got[k]) for k in ref.files)
+    with pytest.raises(ValueError):
+        pio.load_vec_field(str(tmp_path / "v2"), "cube")
+
+
+def test_limit_vec_field_golden(golden):
+    from ppafm_gb300 import io as pio
+
+    g = golden("clamp")
+    G = g["G"].copy()
+    pio.limit_vec_field(G, Fmax=10.0)
+    assert np.array_equal(G, g["Gc"])
