@@ -68,7 +68,8 @@ void getLennardJonesFF(int natoms, double *Ratoms, double *cLJs);
 /* ProbeParticle.cpp:540  (core.py:270) -- kind 0 = s, 1 = pz, 2 = dz2 tip */
 void getCoulombFF(int natoms, double *Ratoms, double *kQQs, int kind);
 /* ProbeParticle.cpp:633  (core.py:312) -- returns the stroke's iteration sum.
- * splineParams must be NULL: the radial tip spline is not part of this library. */
+ * splineParams: NULL, or a TIP::SplineParams {int rff_n; double *rff_xs; double *rff_ydys;}
+ * whose radial force replaces the harmonic radial spring for this call. */
 int relaxTipStroke(int probeStart, int relaxAlg, int nstep, double *rTips, double *rs, double *fs,
                    void *splineParams);
 /* ProbeParticle.cpp:682  (core.py:322) -- returns 0 like the reference; the total
@@ -152,6 +153,14 @@ int ppgpu_relax_scan(const float *FE, const int *n, const double *cell, const do
                      const double *xs, const double *ys, const double *zs, const double *pos_offset, float *fzs,
                      float *ppos, int *iters, int nw, const double *df_weights, float *df,
                      unsigned long long *iter_total, void *stream);
+
+/* Radial tip spline of the relaxation (TIP::SplineParams + forceRSpline,
+ * ProbeParticle.cpp:58-62, 212-225): n knots xs (float64, ascending) and n (value, slope)
+ * pairs ydys of the radial force; it replaces the harmonic radial spring in
+ * ppgpu_relax_strokes / ppgpu_relax_scan calls made after it is set; n = 0 clears it.  The
+ * drop-in relaxTipStroke(s) take the same data as their SplineParams argument (per call).
+ * The batched launch refuses to be created while a spline is set. */
+int ppgpu_set_tip_spline(int n, const double *xs, const double *ydys);
 
 /* Lanes per stroke of ppgpu_relax_strokes / ppgpu_relax_scan (no reference counterpart):
  * tps 1, 2, 4 or 8 lanes share each stroke's trilinear gathers (same results bit for bit);

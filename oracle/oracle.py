@@ -58,7 +58,7 @@ def lib():
         L.oc_ff_subgrid.argtypes = [ip, dp, ip, ip, c_int, dp, dp, c_int, dp, dp, c_int]
         L.oc_lj_grid.argtypes = [ip, dp, c_int, dp, dp, dp, dp, c_int]
         L.oc_coulomb_grid.argtypes = [ip, dp, c_int, dp, dp, c_int, dp, dp, c_int]
-        L.oc_relax_strokes.argtypes = [ip, dp, dp, dp, c_int, c_int, c_int, c_int, dp, dp, dp, ip, ip, c_int]
+        L.oc_relax_strokes.argtypes = [ip, dp, dp, dp, c_int, c_int, c_int, c_int, dp, dp, dp, ip, ip, c_int, c_int, dp, dp]
         L.oc_fz2df.argtypes = [c_longlong, c_int, dp, c_int, dp, c_double, dp, c_int]
         L.oc_afm_ff_qzs.argtypes = [ip, fp, fp, fp, fp, c_int, fp, fp, fp, fp, fp, c_int]
         L.oc_afm_relax_tilted.argtypes = [fp, ip, fp, c_int, fp, c_int, fp, fp, fp, fp, fp, fp, fp, ip, c_int]
@@ -164,10 +164,11 @@ def relax_param_vector(tip, maxIters=1000, convF2=1e-8, dt=0.1, damping=0.1, fin
     return v
 
 
-def relax_strokes(n, cell, gridF, params, rTips, probeStart=1, relaxAlg=1, nthreads=0):
+def relax_strokes(n, cell, gridF, params, rTips, probeStart=1, relaxAlg=1, nthreads=0, spline=None):
     """relaxTipStrokes_omp (ProbeParticle.cpp:682-701) over strokes laid out as
-    rTips[..., nstep, 3] (every leading index is one stroke).  Returns
-    (rs, fs, itrsum per stroke, iterations per step)."""
+    rTips[..., nstep, 3] (every leading index is one stroke).  spline = (xs [n], ydys [n, 2])
+    replaces the radial spring by forceRSpline.  Returns (rs, fs, itrsum per stroke,
+    iterations per step)."""
     n = _i32(n)
     cell = _c64(cell).reshape(3, 3)
     gridF = _c64(gridF)
@@ -180,7 +181,13 @@ def relax_strokes(n, cell, gridF, params, rTips, probeStart=1, relaxAlg=1, nthre
     fs = np.zeros(shp)
     sums = np.zeros(nstroke, dtype=np.int32)
     iters = np.zeros(shp[:-1], dtype=np.int32)
-    lib().oc_relax_strokes(_p(n, c_int), _p(cell, c_double), _p(gridF, c_double), _p(params, c_double), probeStart, relaxAlg, nstroke, nstep, _p(rTips, c_double), _p(rs, c_double), _p(fs, c_double), _p(sums, c_int), _p(iters, c_int), nthreads)
+    sx = sy = None
+    ns = 0
+    if spline is not None:
+        sx = _c64(spline[0])
+        sy = _c64(spline[1]).reshape(-1)
+        ns = len(sx)
+    lib().oc_relax_strokes(_p(n, c_int), _p(cell, c_double), _p(gridF, c_double), _p(params, c_double), probeStart, relaxAlg, nstroke, nstep, _p(rTips, c_double), _p(rs, c_double), _p(fs, c_double), _p(sums, c_int), _p(iters, c_int), nthreads, ns, None if sx is None else _p(sx, c_double), None if sy is None else _p(sy, c_double))
     return rs, fs, sums, iters
 
 
@@ -344,11 +351,11 @@ def scan_tips(xTips, yTips, zTips, origin):
     return rTips
 
 
-def relaxed_scan(n, cell, gridF, params, xTips, yTips, zTips, origin, nthreads=0):
+def relaxed_scan(n, cell, gridF, params, xTips, yTips, zTips, origin, nthreads=0, spline=None):
     """relaxedScan3D_omp + the origin handling of perform_relaxation (HighLevel.py:104-124,
     162-172): returns fzs [nx,ny,nz] and PPpos [nx,ny,nz,3], ascending z, and iterations."""
     rTips = scan_tips(xTips, yTips, zTips, origin)
-    rs, fs, sums, iters = relax_strokes(n, cell, gridF, params, rTips, nthreads=nthreads)
+    rs, fs, sums, iters = relax_strokes(n, cell, gridF, params, rTips, nthreads=nthreads, spline=spline)
     rs = rs[:, :, ::-1, :].copy() + np.asarray(origin)[None, None, None, :]
     fzs = fs[:, :, ::-1, 2].copy()
     return fzs, rs, iters[:, :, ::-1].copy()

@@ -225,7 +225,45 @@ typedef struct {
     /* relaxation (ProbeParticle.cpp:74-114) */
     int maxIters;
     double convF2, dt, damping, finc, fdec, falpha;
+    /* radial tip spline (TIP::SplineParams, ProbeParticle.cpp:58-62); spl_n 0: harmonic */
+    int spl_n;
+    const double *spl_xs, *spl_ydys;
 } oc_relax_ctx;
+
+/* Interval search of Spline_Hermite::find_index (spline_hermite.h:159-169): halving steps
+ * from n/2 down to 1, advancing while the knot is below x. */
+static inline int oc_spline_index(int n, double x, const double *xs)
+{
+    int i = 0, di = n;
+    while (di > 1) {
+        di >>= 1;
+        int j = i + di;
+        if (xs[j] < x) i = j;
+    }
+    return i;
+}
+
+/* Cubic Hermite value (spline_hermite.h:45-51) at u in [0,1] from end values and slopes. */
+static inline double oc_hermite(double u, double y0, double y1, double dy0, double dy1)
+{
+    double y01 = y0 - y1;
+    return y0 + u * (dy0 + u * (-3 * y01 - 2 * dy0 - dy1 + u * (2 * y01 + dy0 + dy1)));
+}
+
+/* Radial tip force from the spline of |d| (forceRSpline, ProbeParticle.cpp:212-225); the
+ * interval index is kept at most n - 2 (the reference reads past its table beyond the last
+ * knot). */
+static inline double oc_spline_radial(const oc_relax_ctx *C, double x)
+{
+    int i = oc_spline_index(C->spl_n, x, C->spl_xs);
+    if (i > C->spl_n - 2) i = C->spl_n - 2;
+    double x0 = C->spl_xs[i], x1 = C->spl_xs[i + 1];
+    double dx = x1 - x0;
+    double denom = 1 / dx;
+    double u = (x - x0) * denom;
+    const double *yd = C->spl_ydys + 2 * i;
+    return oc_hermite(u, yd[0], yd[2], yd[1] * dx, yd[3] * dx);
+}
 
 /* One axis of the periodic index/weight set-up (Grid.h:66-69). */
 static inline void oc_wrap_axis(double r, int n, int *im, int *it, double *m, double *t)
@@ -289,7 +327,7 @@ static inline void oc_pp_force(const oc_relax_ctx *C, const double rTip[3], cons
     for (int k = 0; k < 3; k++) d[k] = r[k] - rTip[k];
     oc_interp(C, g[0], g[1], g[2], f);
     double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    double s = C->kRadial * (l - C->lRadial) / l;
+    double s = (C->spl_n > 0) ? oc_spline_radial(C, l) / l : C->kRadial * (l - C->lRadial) / l;
     for (int k = 0; k < 3; k++) f[k] += d[k] * s;
     for (int k = 0; k < 3; k++) d[k] -= C->rPP0[k];
     for (int k = 0; k < 3; k++) f[k] += d[k] * C->kSpring[k];
@@ -371,13 +409,19 @@ static int oc_relax_stroke(const oc_relax_ctx *C, int probeStart, int relaxAlg, 
  * [s*nstep, (s+1)*nstep) of rTips/rs/fs.  Per-stroke iteration sums go to itrsums
  * (nullable) and per-step iteration counts to iters (nullable, [nstroke*nstep]).
  * params: maxIters, convF2, dt, damping, finc, fdec, falpha, lRadial, kRadial,
- *         rPP0[3] (already made consistent with lRadial), kSpring[3]. */
+ *         rPP0[3] (already made consistent with lRadial), kSpring[3].
+ * spl_n knots spl_xs and (value, slope) pairs spl_ydys: the radial tip spline replacing the
+ * harmonic radial spring (spl_n 0 or NULL arrays: harmonic). */
 void oc_relax_strokes(const int n[3], const double cell[9], const double *gridF,
                       const double *params, int probeStart, int relaxAlg,
                       int nstroke, int nstep, const double *rTips, double *rs, double *fs,
-                      int *itrsums, int *iters, int nthreads)
+                      int *itrsums, int *iters, int nthreads,
+                      int spl_n, const double *spl_xs, const double *spl_ydys)
 {
     oc_relax_ctx C;
+    C.spl_n = (spl_xs && spl_ydys && spl_n >= 2) ? spl_n : 0;
+    C.spl_xs = spl_xs;
+    C.spl_ydys = spl_ydys;
     double dcell[9];
     for (int k = 0; k < 3; k++) C.n[k] = n[k];
     oc_grid_setup(n, cell, dcell, C.dicell);

@@ -20,7 +20,8 @@ import torch
 
 from . import common as PPU
 from . import core
-from .device import DeviceFF, iter_counter, pack_atoms, relax_params, relax_scan
+from .device import DeviceFF, iter_counter, pack_atoms, relax_params, relax_scan, relax_strokes
+from .device import tip_spline as tip_spline_ctx
 from .fieldFFT import FFTGrid
 from ._lib import FF_COULOMB, FF_LJ, FF_LJC
 
@@ -75,10 +76,39 @@ def setFF(FF=None, computeVpot=False, n=None, lvec=None, parameters=None):
     return FF, V
 
 
+def trjByDir(n, d, p0):
+    """Tip trajectory of a tilted scan (HighLevel.py:36-41): n points from p0 along d, in
+    approach order."""
+    trj = np.zeros((n, 3))
+    for k in range(3):
+        trj[:, k] = p0[k] + (np.arange(n)[::-1]) * d[k]
+    return trj
+
+
+def relaxedScan3D(xTips, yTips, zTips, trj=None, bF3d=False, tip_spline=None):
+    """HighLevel.py:63-101 (one relaxTipStroke per pixel) as one batched stroke relaxation:
+    pixel (x, y) follows trj + (x, y, 0), trj defaulting to the straight approach over zTips."""
+    nx, ny, nz = len(xTips), len(yTips), len(zTips)
+    if trj is None:
+        trj = np.zeros((nz, 3))
+        trj[:, 2] = zTips[::-1]
+    trj = np.asarray(trj, dtype=np.float64)
+    rTips = np.zeros((nx, ny, len(trj), 3))
+    rTips[:, :, :, 0] = trj[None, None, :, 0] + np.asarray(xTips)[:, None, None]
+    rTips[:, :, :, 1] = trj[None, None, :, 1] + np.asarray(yTips)[None, :, None]
+    rTips[:, :, :, 2] = trj[None, None, :, 2]
+    rs = np.zeros_like(rTips)
+    fs = np.zeros_like(rTips)
+    core.relaxTipStrokes_omp(rTips, rs, fs, tip_spline=tip_spline)
+    PPpos = rs[:, :, ::-1, :].copy()
+    fzs = fs[:, :, ::-1, :].copy() if bF3d else fs[:, :, ::-1, 2].transpose(2, 1, 0).copy()
+    return fzs, PPpos
+
+
 def relaxedScan3D_omp(xTips, yTips, zTips, trj=None, bF3d=False, tip_spline=None):
-    """HighLevel.py:104-124 through the drop-in core (FF registered with setFF)."""
-    if trj is not None:
-        raise NotImplementedError("tilted trajectories are not supported")
+    """HighLevel.py:104-124 through the drop-in core (FF registered with setFF).  Like the
+    reference, the trajectory argument is accepted and not used: the tips approach straight
+    down over zTips."""
     nx, ny, nz = len(xTips), len(yTips), len(zTips)
     rTips = np.zeros((nx, ny, nz, 3))
     rTips[:, :, :, 0] = xTips[:, None, None]
@@ -117,10 +147,7 @@ def perform_relaxation(lvec, FFLJ, FFel=None, FFpauli=None, FFboltz=None, FFkpfm
     terms) composed on the host like the reference, then one device relaxed scan.
     ``relax`` optionally overrides maxIters/convF2/dt/damping (the reference reads the
     core's global setRelax state)."""
-    if tip_spline is not None:
-        raise NotImplementedError("tip_spline is not supported")
-    if _get(parameters, "tiltedScan", False):
-        raise NotImplementedError("tilted scans are not supported")
+    tilted = bool(_get(parameters, "tiltedScan", False))
     lvec = np.asarray(lvec, dtype=np.float64)
     xTips, yTips, zTips, lvecScan = PPU.prepareScanGrids(_get(parameters, "scanMin"), _get(parameters, "scanMax"), _get(parameters, "scanStep"), _get(parameters, "r0Probe"))
     FF = FFLJ.copy()
@@ -134,9 +161,26 @@ def perform_relaxation(lvec, FFLJ, FFel=None, FFpauli=None, FFboltz=None, FFkpfm
         FF += FFboltz
     ff = DeviceFF(FF.shape[:3], lvec).from_host_f64(FF.reshape(-1, 3))
     prm = tip_vector(parameters, relax)
-    out = relax_scan(ff, prm, xTips - lvec[0, 0], yTips - lvec[0, 1], zTips[::-1] - lvec[0, 2], pos_offset=lvec[0])
-    fzs = out["fzs"].cpu().numpy().astype(np.float64)
-    PPpos = out["ppos"].cpu().numpy().astype(np.float64)
+    with tip_spline_ctx(tip_spline):
+        return _relax_and_collect(ff, prm, lvec, xTips, yTips, zTips, lvecScan, tilted, bPPdisp, parameters)
+
+
+def _relax_and_collect(ff, prm, lvec, xTips, yTips, zTips, lvecScan, tilted, bPPdisp, parameters):
+    if tilted:
+        # the reference builds the tilted trajectory and passes it to relaxedScan3D_omp,
+        # which does not use it (HighLevel.py:164-167, 104-124): the tips approach straight
+        # down and the full force vector is kept for Fz2df_tilt
+        rTips = np.zeros((len(xTips), len(yTips), len(zTips), 3))
+        rTips[..., 0] = (xTips - lvec[0, 0])[:, None, None]
+        rTips[..., 1] = (yTips - lvec[0, 1])[None, :, None]
+        rTips[..., 2] = (zTips[::-1] - lvec[0, 2])[None, None, :]
+        rs, fs, _, _ = relax_strokes(ff, prm, rTips)
+        fzs = fs.flip(2).cpu().numpy()
+        PPpos = rs.flip(2).cpu().numpy() + lvec[0]
+    else:
+        out = relax_scan(ff, prm, xTips - lvec[0, 0], yTips - lvec[0, 1], zTips[::-1] - lvec[0, 2], pos_offset=lvec[0])
+        fzs = out["fzs"].cpu().numpy().astype(np.float64)
+        PPpos = out["ppos"].cpu().numpy().astype(np.float64)
     PPdisp = None
     if bPPdisp:
         r0 = _get(parameters, "r0Probe")

@@ -56,6 +56,7 @@ SIGNATURES = {
     "ppgpu_ff_subgrid": ([c_void_p, _ip, _dp, _ip, _ip, c_void_p, c_int, c_int, c_int, c_int, c_double, c_double, _dp, _dp, c_int, c_void_p], c_int),
     "ppgpu_relax_strokes": ([c_void_p, _ip, _dp, _dp, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
     "ppgpu_relax_scan": ([c_void_p, _ip, _dp, _dp, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, _dp, c_void_p, c_void_p, c_void_p, c_int, _dp, c_void_p, c_void_p, c_void_p], c_int),
+    "ppgpu_set_tip_spline": ([c_int, _dp, _dp], c_int),
     "ppgpu_set_relax_tps": ([c_int], c_int),
     "ppgpu_get_relax_tps": ([c_longlong, _ip], c_int),
     "ppgpu_relax_afm": ([c_void_p, _ip, _dp, _dp, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, _dp, c_void_p, c_void_p, c_void_p], c_int),

@@ -85,6 +85,17 @@ def Fz2df(F, dz, k0, f0, amplitude=1.0, units=16.0217656, out=None, stream=None)
     return o
 
 
+def Fz2df_tilt(F, d, k0, f0, amplitude=1.0, units=16.0217656):
+    """Frequency shift of a tilted scan (common.py:433-445): each force component of
+    F [nx, ny, nz, 3] convolved along the scan with get_df_weight(amplitude, |d|) on the
+    GPU, projected on the scan direction d, scaled by units*f0/k0 (float64 result)."""
+    d = np.asarray(d, dtype=np.float64)
+    dr = float(np.sqrt(d[0] ** 2 + d[1] ** 2 + d[2] ** 2))
+    F = np.asarray(F)
+    comps = [Fz2df(np.ascontiguousarray(F[..., k]), dz=dr, k0=1.0, f0=1.0, amplitude=amplitude, units=1.0) for k in range(3)]
+    return (comps[0] * d[0] + comps[1] * d[1] + comps[2] * d[2]) * units * f0 / k0
+
+
 # ------------------------------------------------------------- atoms and LJ
 
 

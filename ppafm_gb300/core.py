@@ -8,10 +8,10 @@ relaxation state, force fields accumulated into the array registered with
 Differences from the reference, all deliberate:
   * ``setRelax`` takes ``convF2`` as documented (the reference wrapper references an
     undefined name, ppafm/core.py:97-98);
-  * a non-None ``tip_spline`` raises (the radial tip spline is outside this library);
   * a failed call raises ``PPGPUError`` instead of printing or exiting.
 """
 
+import ctypes
 import weakref
 
 import numpy as np
@@ -33,6 +33,7 @@ __all__ = [
     "getCoulombFF",
     "relaxTipStroke",
     "relaxTipStrokes_omp",
+    "SplineParameters",
     "last_iterations",
     "PPGPUError",
 ]
@@ -124,25 +125,50 @@ def getCoulombFF(Rs, kQQs, kind=0):
     check_state()
 
 
+class SplineParameters(ctypes.Structure):
+    """Radial tip spline (core.py:132-155, TIP::SplineParams): knots xs and per knot the radial
+    force and its slope, ydys [n, 2]."""
+
+    _fields_ = [("rff_n", ctypes.c_int), ("rff_xs", ctypes.POINTER(ctypes.c_double)), ("rff_ydys", ctypes.POINTER(ctypes.c_double))]
+
+    def __init__(self, xs, ydys):
+        super().__init__()
+        self.np_rff_xs = np.ascontiguousarray(xs, dtype=np.double)
+        self.np_rff_ydys = np.ascontiguousarray(ydys, dtype=np.double)
+        self.rff_n = len(self.np_rff_xs)
+        self.rff_xs = np.ctypeslib.as_ctypes(self.np_rff_xs)
+        self.rff_ydys = np.ctypeslib.as_ctypes(self.np_rff_ydys.reshape(-1))
+
+    @classmethod
+    def from_file(cls, file_path):
+        d = np.genfromtxt(file_path)
+        return cls(d[:, 0], d[:, 1:])
+
+
+def _spline_ptr(tip_spline):
+    if tip_spline is None:
+        return None
+    if not isinstance(tip_spline, ctypes.Structure):
+        raise TypeError("tip_spline must be a SplineParameters structure (or None)")
+    return ctypes.cast(ctypes.pointer(tip_spline), ctypes.c_void_p)
+
+
 def relaxTipStroke(rTips, rs, fs, probeStart=1, relaxAlg=1, tip_spline=None):
-    """core.py:312-314: one stroke [nstep,3]; returns the iteration sum."""
-    if tip_spline is not None:
-        raise PPGPUError(1, "tip_spline is not supported")
+    """core.py:312-314: one stroke [nstep,3]; returns the iteration sum.  tip_spline: a
+    SplineParameters (ctypes structure of the same layout) replacing the radial spring."""
     for a, nm in ((rTips, "rTips"), (rs, "rs"), (fs, "fs")):
         _f64(a, 2, nm)
-    r = lib().relaxTipStroke(int(probeStart), int(relaxAlg), len(rTips), dptr(rTips), dptr(rs), dptr(fs), None)
+    r = lib().relaxTipStroke(int(probeStart), int(relaxAlg), len(rTips), dptr(rTips), dptr(rs), dptr(fs), _spline_ptr(tip_spline))
     check_state()
     return r
 
 
 def relaxTipStrokes_omp(rTips, rs, fs, probeStart=1, relaxAlg=1, tip_spline=None):
     """core.py:322-324: all strokes of rTips [nx,ny,nz,3]; returns 0 like the reference."""
-    if tip_spline is not None:
-        raise PPGPUError(1, "tip_spline is not supported")
     for a, nm in ((rTips, "rTips"), (rs, "rs"), (fs, "fs")):
         _f64(a, 4, nm)
     nx, ny, nz, _ = rTips.shape
-    r = lib().relaxTipStrokes_omp(nx, ny, int(probeStart), int(relaxAlg), nz, dptr(rTips), dptr(rs), dptr(fs), None)
+    r = lib().relaxTipStrokes_omp(nx, ny, int(probeStart), int(relaxAlg), nz, dptr(rTips), dptr(rs), dptr(fs), _spline_ptr(tip_spline))
     check_state()
     return r
 

@@ -237,9 +237,8 @@ static void facade_params(double *prm) {
     }
 }
 
-static int facade_relax(int nstroke, int probeStart, int relaxAlg, int nstep, const double *rTips, double *rs,
-                        double *fs, void *spline, int *itrsum_out) {
-    if (spline) return set_error(PPGPU_ERR_ARG, "radial tip splines are not supported (pass None)");
+static int facade_relax_body(int nstroke, int probeStart, int relaxAlg, int nstep, const double *rTips, double *rs,
+                             double *fs, int *itrsum_out) {
     if (!g_f.has_n || !g_f.has_cell) return set_error(PPGPU_ERR_STATE, "setGridN/setGridCell must be called first");
     if (!g_f.gridF) return set_error(PPGPU_ERR_STATE, "setFF_Fpointer must be called first");
     if (nstroke < 0 || nstep < 0) return set_error(PPGPU_ERR_ARG, "negative sizes");
@@ -280,6 +279,36 @@ static int facade_relax(int nstroke, int probeStart, int relaxAlg, int nstep, co
     g_f.last_iters = (long long)tot;
     if (itrsum_out) *itrsum_out = sum0;
     return set_ok();
+}
+
+// TIP::SplineParams (ProbeParticle.cpp:58-62): the struct ppafm/core.py passes by pointer.
+struct SplineParamsC {
+    int rff_n;
+    double *rff_xs;
+    double *rff_ydys;
+};
+
+struct FacadeRelaxArgs {
+    int nstroke, probeStart, relaxAlg, nstep;
+    const double *rTips;
+    double *rs, *fs;
+    int *itrsum_out;
+};
+
+static int facade_relax_tramp(void *p) {
+    FacadeRelaxArgs *a = (FacadeRelaxArgs *)p;
+    return facade_relax_body(a->nstroke, a->probeStart, a->relaxAlg, a->nstep, a->rTips, a->rs, a->fs, a->itrsum_out);
+}
+
+// relaxTipStroke(s): with a spline, its radial force replaces the harmonic radial spring for
+// this call (forceRSpline, ProbeParticle.cpp:212-225).
+static int facade_relax(int nstroke, int probeStart, int relaxAlg, int nstep, const double *rTips, double *rs,
+                        double *fs, void *spline, int *itrsum_out) {
+    if (!spline) return facade_relax_body(nstroke, probeStart, relaxAlg, nstep, rTips, rs, fs, itrsum_out);
+    const SplineParamsC *sp = (const SplineParamsC *)spline;
+    if (sp->rff_n < 2 || !sp->rff_xs || !sp->rff_ydys) return set_error(PPGPU_ERR_ARG, "tip spline: need at least 2 knots and both arrays");
+    FacadeRelaxArgs a = {nstroke, probeStart, relaxAlg, nstep, rTips, rs, fs, itrsum_out};
+    return with_tip_spline(sp->rff_n, sp->rff_xs, sp->rff_ydys, facade_relax_tramp, &a);
 }
 
 }  // namespace ppgpu

@@ -917,6 +917,8 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
         chunk = tuning ? tuning[3] : 64;
     if (ctas_per_sm < 1 || ctas_per_sm > 2 || tw < 1 || th < 1 || tw * th > 4096 || chunk < 1 || chunk > 4096)
         return set_error(PPGPU_ERR_ARG, "batch_create: bad tuning (ctas/SM 1..2, tile, chunk 1..4096)");
+    if (g_tip_spline.n > 0)
+        return set_error(PPGPU_ERR_ARG, "batch_create: the batched path uses the harmonic radial spring (clear the tip spline)");
     // relaxation constants (the grid fields of RelaxPrm are unused here)
     BatchPrm B;
     memset(&B, 0, sizeof(B));

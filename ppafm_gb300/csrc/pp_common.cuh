@@ -17,6 +17,9 @@ int set_ok();
 int cuda_fail(cudaError_t e, const char *what);
 // Per-device error word that kernels set when a bounded wait gives up.
 int *device_error_word();
+// Runs fn(arg) with the radial tip spline (n knots xs, (value, slope) pairs ydys; n 0: none)
+// in place of the current one, then restores it; returns fn's status (pp_relax.cu).
+int with_tip_spline(int n, const double *xs, const double *ydys, int (*fn)(void *), void *arg);
 
 #define PPGPU_CUDA(call, what)                           \
     do {                                                 \

@@ -77,6 +77,18 @@ __device__ __forceinline__ float df_round(dfl a) { return __fadd_rn(a.h, a.l); }
 
 __device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
 
+// a / b: a quotient of the high parts, corrected once from the remainder a - q b (formed
+// with TwoProduct), as in the double-word division of Dekker.
+__device__ __forceinline__ dfl df_div(dfl a, dfl b) {
+    const float q1 = __fdiv_rn(a.h, b.h);
+    const dfl p = two_prod(q1, b.h);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.h, p.h), p.l), __fsub_rn(a.l, __fmul_rn(q1, b.l)));
+    return fast_two_sum(q1, __fdiv_rn(r, b.h));
+}
+
+// a < b for normalised double-floats.
+__device__ __forceinline__ bool df_lt(dfl a, dfl b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+
 // floor(x) as a float and an int for |x| < 2^22 with float32 adds only (no conversion
 // instructions): x + 1.5*2^23 rounds x to the nearest integer, held in the low mantissa bits.
 __device__ __forceinline__ float floor_small(float x, int &i) {

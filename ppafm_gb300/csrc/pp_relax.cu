@@ -29,6 +29,8 @@
 //  * Trilinear weights are explicit (no texture filtering).
 #include <cmath>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "pp_common.cuh"
 #include "pp_df.cuh"
@@ -360,6 +362,61 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_afm_kernel(const AfmPrm P
 
 // ---------------------------------------------------------------------- host
 
+TipSpline g_tip_spline = {0, nullptr, nullptr};
+static void *g_spline_mem = nullptr;
+static std::vector<double> g_spline_xs, g_spline_ydys;  // host copies (for save/restore)
+
+// Uploads the spline tables (see TipSpline); n == 0 clears.  cudaFree of the previous tables
+// waits for the kernels that may still read them.
+static int upload_tip_spline(int n, const double *xs, const double *ydys) {
+    if (n == 0 || !xs || !ydys) {
+        if (g_spline_mem) cudaFree(g_spline_mem);
+        g_spline_mem = nullptr;
+        g_tip_spline = {0, nullptr, nullptr};
+        g_spline_xs.clear();
+        g_spline_ydys.clear();
+        return set_ok();
+    }
+    if (n < 2) return set_error(PPGPU_ERR_ARG, "tip spline: %d knots (at least 2)", n);
+    std::vector<dfl> tab((size_t)n + 6 * (size_t)(n - 1));
+    for (int i = 0; i < n; i++) tab[i] = df_from(xs[i]);
+    for (int i = 0; i < n - 1; i++) {
+        const double x0 = xs[i], dx = xs[i + 1] - x0, denom = 1 / dx;
+        const double y0 = ydys[2 * i], y1 = ydys[2 * i + 2], dy0 = ydys[2 * i + 1] * dx, dy1 = ydys[2 * i + 3] * dx;
+        const double y01 = y0 - y1;
+        const double c[6] = {x0, denom, y0, dy0, -3 * y01 - 2 * dy0 - dy1, 2 * y01 + dy0 + dy1};
+        for (int k = 0; k < 6; k++) tab[n + 6 * i + k] = df_from(c[k]);
+    }
+    void *mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, tab.size() * sizeof(dfl));
+    if (e != cudaSuccess) return cuda_fail(e, "tip spline tables");
+    e = cudaMemcpy(mem, tab.data(), tab.size() * sizeof(dfl), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(mem);
+        return cuda_fail(e, "tip spline upload");
+    }
+    if (g_spline_mem) cudaFree(g_spline_mem);
+    g_spline_mem = mem;
+    g_tip_spline = {n, (const dfl *)mem, (const dfl *)mem + n};
+    g_spline_xs.assign(xs, xs + n);
+    g_spline_ydys.assign(ydys, ydys + 2 * (size_t)n);
+    return set_ok();
+}
+
+// Runs fn with the tip spline (n, xs, ydys) in place of the current one, then restores it.
+int with_tip_spline(int n, const double *xs, const double *ydys, int (*fn)(void *), void *arg) {
+    std::vector<double> sx = g_spline_xs, sy = g_spline_ydys;
+    const int n0 = (int)sx.size();
+    int s = upload_tip_spline(n, xs, ydys);
+    if (s) return s;
+    s = fn(arg);
+    const std::string msg = s ? std::string(ppgpu_last_error()) : std::string();
+    const int st = s ? ppgpu_last_status() : 0;
+    const int r = upload_tip_spline(n0, n0 ? sx.data() : nullptr, n0 ? sy.data() : nullptr);
+    if (s) return set_error(st, "%s", msg.c_str());
+    return r;
+}
+
 // Lanes per stroke (ppgpu_set_relax_tps).  One lane per stroke is the default: on GB300 the
 // scans measured here (16k-26k strokes) ran 15-20 % slower with 4 lanes per stroke, because
 // every lane of a group also executes the stroke's FIRE arithmetic, which outweighs the
@@ -389,6 +446,11 @@ extern "C" int ppgpu_set_relax_tps(int tps) {
         return set_error(PPGPU_ERR_ARG, "set_relax_tps: %d not in {0 (default), 1, 2, 4, 8}", tps);
     g_relax_tps = tps ? tps : 1;
     return set_ok();
+}
+
+extern "C" int ppgpu_set_tip_spline(int n, const double *xs, const double *ydys) {
+    if (n < 0) return set_error(PPGPU_ERR_ARG, "set_tip_spline: negative knot count");
+    return upload_tip_spline(n, xs, ydys);
 }
 
 extern "C" int ppgpu_get_relax_tps(long long nstroke, int *out) {

@@ -14,6 +14,19 @@ constexpr int RELAX_THREADS = 64;  // small blocks spread the strokes evenly ove
 constexpr int MAX_DF_TAPS = 64;
 constexpr unsigned FULL = 0xffffffffu;
 
+// Radial tip spline (TIP::SplineParams, ProbeParticle.cpp:58-62) in device memory: knots
+// and, per interval, x0, 1/dx and the coefficients c0..c3 of the cubic Hermite piece in
+// u = (x - x0)/dx (spline_hermite.h:45-51), all double-floats.  n == 0: harmonic spring.
+struct TipSpline {
+    int n;
+    const dfl *xs;   // [n]
+    const dfl *seg;  // [n - 1][6]
+};
+// The spline that fill_relax_prm puts into the relaxation parameters (set by
+// ppgpu_set_tip_spline; defined in pp_relax.cu).
+extern TipSpline g_tip_spline;
+
+
 struct RelaxPrm {
     const float4 *FE;
     int n0, n1, n2;
@@ -32,7 +45,27 @@ struct RelaxPrm {
     dfl nr0[3], kSf[3];    // -rPP0, kSpring
     dfl r0[3];             // rPP0
     float convF2f, dtmaxf, acoef0f, fincf, fdecf, falphaf;
+    TipSpline spl;         // radial tip spline (n 0: the harmonic radial spring)
 };
+
+// Radial force of the tip spline at |d| = x (forceRSpline, ProbeParticle.cpp:212-225): the
+// interval from the halving search of Spline_Hermite::find_index (spline_hermite.h:159-169),
+// kept at most n - 2 (the reference reads past its table beyond the last knot), then the
+// cubic in u by Horner's rule.
+__device__ __forceinline__ dfl spline_radial_df(const TipSpline &S, dfl x) {
+    int i = 0;
+    for (int di = S.n; di > 1;) {
+        di >>= 1;
+        if (df_lt(S.xs[i + di], x)) i += di;
+    }
+    i = min(i, S.n - 2);
+    const dfl *c = S.seg + 6 * i;
+    const dfl u = df_mul(df_add(x, df_neg(c[0])), c[1]);
+    dfl r = df_add(c[4], df_mul(u, c[5]));
+    r = df_add(c[3], df_mul(u, r));
+    return df_add(c[2], df_mul(u, r));
+}
+
 
 // ----------------------------------------------------------- interpolation
 
@@ -183,12 +216,17 @@ __device__ __forceinline__ float3 pp_force_df(const RelaxPrm &P, const dfl F[3],
     const dfl LL = two_prod(L, L);
     const float res = __fadd_rn(__fsub_rn(__fsub_rn(l2.h, LL.h), LL.l), l2.l);
     const dfl l = fast_two_sum(L, __fmul_rn(res, __fmul_rn(0.5f, rs)));
-    const dfl x = df_add(l, P.nl0);  // l - l0
-    // q = (l - l0) / l: approximate quotient plus the correction from its exact remainder
-    const float qh = __fmul_rn(x.h, rs);
-    const dfl ql = two_prod(qh, l.h);
-    const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(x.h, ql.h), ql.l), x.l), __fmul_rn(qh, l.l));
-    const dfl s = df_mul(P.kRadf, two_sum(qh, __fmul_rn(rem, rs)));
+    dfl s;
+    if (P.spl.n > 0) {
+        s = df_div(spline_radial_df(P.spl, l), l);  // radial spline force / l
+    } else {
+        const dfl x = df_add(l, P.nl0);  // l - l0
+        // q = (l - l0) / l: approximate quotient plus the correction from its exact remainder
+        const float qh = __fmul_rn(x.h, rs);
+        const dfl ql = two_prod(qh, l.h);
+        const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(x.h, ql.h), ql.l), x.l), __fmul_rn(qh, l.l));
+        s = df_mul(P.kRadf, two_sum(qh, __fmul_rn(rem, rs)));
+    }
     // f = F + d s + (d - r0) kS: the three high parts summed error-free, every low part and
     // product error added once at the end (the result is rounded to float32)
     float f[3];
@@ -317,6 +355,7 @@ static inline int fill_relax_prm(RelaxPrm &P, const float *FE, const int *n, con
         P.r0[k] = df_from(P.rPP0[k]);
         P.kSf[k] = df_from(P.kSpring[k]);
     }
+    P.spl = g_tip_spline;
     P.convF2f = (float)P.convF2;
     P.dtmaxf = (float)P.dtmax;
     P.acoef0f = (float)P.acoef0;

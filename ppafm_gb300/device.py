@@ -7,6 +7,7 @@ torch only allocates the buffers and supplies the stream; all arithmetic is in
 libppgpu.so.  Every function raises ``PPGPUError`` on failure -- there is no CPU fallback.
 """
 
+import contextlib
 import ctypes
 
 import numpy as np
@@ -129,6 +130,29 @@ def relax_params(maxIters=1000, convF2=1e-8, dt=0.1, damping=0.1, finc=1.1, fdec
     p[9:12] = rPP0
     p[12:15] = kSpring
     return p
+
+
+@contextlib.contextmanager
+def tip_spline(spline):
+    """Radial tip spline for the relaxations run inside the block (ppgpu_set_tip_spline):
+    None, a core.SplineParameters (or any object with np_rff_xs / np_rff_ydys), or a pair
+    (xs [n], ydys [n, 2])."""
+    if spline is None:
+        yield
+        return
+    if hasattr(spline, "np_rff_xs"):
+        xs, yd = spline.np_rff_xs, spline.np_rff_ydys
+    else:
+        xs, yd = spline
+    xs = np.ascontiguousarray(xs, dtype=np.float64)
+    yd = np.ascontiguousarray(yd, dtype=np.float64).reshape(-1)
+    if yd.size != 2 * xs.size:
+        raise ValueError("tip spline: ydys needs a (value, slope) pair per knot")
+    check(lib().ppgpu_set_tip_spline(len(xs), dptr(xs), dptr(yd)))
+    try:
+        yield
+    finally:
+        check(lib().ppgpu_set_tip_spline(0, None, None))
 
 
 def relax_strokes(ff, prm, rTips, probeStart=1, relaxAlg=1, iters=False, counter=None, stream=None):

@@ -2,7 +2,8 @@
 
 Run where the reference checkout exists (it is read only):
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [/root/reference]           # all fixtures
+    python tests/golden/make_golden.py /root/reference extras      # xsf/ and tilt.npz only
 
 The script copies the reference's ``ppafm`` package to a temporary directory, compiles
 its two C++ modules there from their own sources with g++ (ProbeParticle, GridUtils; the
@@ -39,9 +40,10 @@ def setup_reference(ref_root):
 
 def main(ref_root="/root/reference", only=None):
     tmp = setup_reference(ref_root)
-    if only == "xsf":
+    if only == "extras":
         try:
             make_xsf(tmp)
+            make_tilt(tmp)
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         return
@@ -214,6 +216,21 @@ def make_xsf(tmp):
     pio.saveXSFData(os.path.join(out, "ortho.xsf"), S[:, :, :2], dd=[0.1, 0.2, 0.3])
     np.savez(os.path.join(out, "inputs.npz"), S=S, V=V, lvec=lvec)
     print("xsf fixtures written to", out)
+
+
+def make_tilt(tmp):
+    """Fz2df_tilt of a tilted scan's force vectors (common.py:433-445) -> tests/golden/tilt.npz."""
+    import ppafm.common as PPU
+
+    rng = np.random.default_rng(4242)
+    F = rng.normal(size=(4, 3, 30, 3)) * 0.05
+    cases = {}
+    for i, (d, amp) in enumerate((((0.02, -0.01, 0.1), 1.0), ((0.0, 0.0, 0.1), 0.5), ((0.05, 0.05, 0.08), 1.3))):
+        cases[f"d_{i}"] = np.array(d)
+        cases[f"amp_{i}"] = np.array(amp)
+        cases[f"df_{i}"] = PPU.Fz2df_tilt(F, d, k0=1800.0, f0=30300.0, amplitude=amp)
+    np.savez_compressed(os.path.join(HERE, "tilt.npz"), F=F, **cases)
+    print("tilt fixture written")
 
 
 if __name__ == "__main__":

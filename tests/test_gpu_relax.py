@@ -121,9 +121,11 @@ def test_relax_edge_cases(gpulib, oracle, golden):
     # empty stroke set
     e = np.zeros((0, 3, 5, 3))
     assert core.relaxTipStrokes_omp(e, e.copy(), e.copy()) == 0
-    # spline tips are refused, not silently ignored
-    with pytest.raises(PPGPUError):
+    # a tip spline must be a SplineParameters structure with at least two knots
+    with pytest.raises(TypeError):
         core.relaxTipStrokes_omp(rT, rs, fs, tip_spline=object())
+    with pytest.raises(PPGPUError, match="knots"):
+        core.relaxTipStrokes_omp(rT, rs, fs, tip_spline=core.SplineParameters([4.0], [[0.0, 1.0]]))
     core.deleteFF_Fpointer()
     with pytest.raises(PPGPUError):
         core.relaxTipStrokes_omp(rT, rs, fs)
@@ -208,3 +210,96 @@ def test_outfz_file_handoff(gpulib, golden, tmp_path, fmt):
     assert np.isclose(lvec_df[0][2], lv[0][2] + 0.5) and np.isclose(lvec_df[3][2], lv[3][2] - 1.0)
     ext = ".xsf" if fmt == "xsf" else ".npz"
     assert (tmp_path / ("df" + ext)).exists()
+
+
+def test_fz2df_tilt_golden(gpulib, golden):
+    """Fz2df_tilt (common.py:433-445) against the reference's values."""
+    from ppafm_gb300 import common
+
+    g = golden("tilt")
+    for i in range(3):
+        got = common.Fz2df_tilt(g["F"], g[f"d_{i}"], k0=1800.0, f0=30300.0, amplitude=float(g[f"amp_{i}"]))
+        want = g[f"df_{i}"]
+        assert got.shape == want.shape
+        assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max() + 1e-6, i
+
+
+def test_tilted_scan_relaxation(gpulib, oracle, golden):
+    """perform_relaxation with tiltedScan keeps the full force vector (the reference's
+    relaxedScan3D_omp ignores the trajectory): positions as the plain scan's, Fz equal to the
+    plain scan's, and Fz2df_tilt along z equal to |d| Fz2df."""
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import common
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    p = dict(charge=0.0, klat=float(g["klat"]), krad=float(g["krad"]), r0Probe=list(g["r0Probe"]), scanMin=list(g["scanMin"]), scanMax=list(g["scanMax"]), scanStep=list(g["scanStep"]), tiltedScan=False, scanTilt=[0.0, 0.0, 0.1])
+    relax = dict(maxIters=300, convF2=1e-8, dt=0.5, damping=0.1)
+    f_plain, pp_plain, _, _ = HL.perform_relaxation(g["lvec"], FF, parameters=p, relax=relax)
+    p["tiltedScan"] = True
+    f_tilt, pp_tilt, _, lvs = HL.perform_relaxation(g["lvec"], FF, parameters=p, relax=relax)
+    assert f_tilt.shape == f_plain.shape + (3,)
+    dpos = np.linalg.norm(pp_tilt - g["PPpos"], axis=-1)
+    flips = _check_positions(dpos)
+    assert np.abs(f_tilt[..., 2] - f_plain)[~flips].max() < 1e-4
+    # along z the tilted conversion is the plain one times the step length (the projection
+    # on d is not normalised, common.py:443-445)
+    df_t = common.Fz2df_tilt(f_tilt, [0.0, 0.0, 0.1], k0=1800.0, f0=30000.0, amplitude=1.0)
+    df_p = common.Fz2df(f_tilt[..., 2], dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)
+    assert np.abs(df_t - 0.1 * df_p).max() < 1e-6 * max(1.0, np.abs(df_p).max())
+
+
+def _spline(krad):
+    """A radial tip spline: 9 knots (not a power of two, so the reference's halving interval
+    search is exercised as it is), 1.3 times stiffer than the harmonic spring plus a cubic."""
+    k = 1.3 * krad / -16.0217662
+    xs = np.linspace(3.0, 5.0, 9)
+    ydys = np.column_stack([k * (xs - 4.0) + 0.5 * (xs - 4.0) ** 3, k + 1.5 * (xs - 4.0) ** 2])
+    return xs, ydys
+
+
+def test_tip_spline_strokes_and_scan_vs_oracle(gpulib, oracle, golden):
+    """Radial tip spline (forceRSpline) through the drop-in strokes call and through
+    perform_relaxation's scan, against the oracle (itself bit-identical to the reference)."""
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import core
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = g["lvec"]
+    xs, ydys = _spline(float(g["krad"]))
+    FFc = np.ascontiguousarray(FF)
+    HL.setFF(FFc, lvec=lv)
+    core.setRelax(300, 1e-8, 0.5, 0.1)
+    core.setFIRE(1.1, 0.5, 0.99)
+    core.setTip(lRadial=4.0, kRadial=float(g["krad"]) / -16.0217662, rPP0=np.array([0.0, 0.0, 0.0]), kSpring=np.array([g["klat"], g["klat"], 0.0]) / -16.0217662)
+    rT = oracle.scan_tips(xT[::3], yT[::3], zT, lv[0])
+    rs = np.zeros_like(rT)
+    fs = np.zeros_like(rT)
+    try:
+        core.relaxTipStrokes_omp(rT, rs, fs, tip_spline=core.SplineParameters(xs, ydys))
+    finally:
+        core.deleteFF_Fpointer()
+    rs2, fs2, _, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, prm, rT, spline=(xs, ydys))
+    flips = _check_positions(np.linalg.norm(rs - rs2, axis=-1))
+    assert np.abs(fs - fs2)[~flips].max() < 1e-4
+    rs3, _, _, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, prm, rT)
+    assert np.abs(rs3 - rs2).max() > 1e-3  # the spline changes the relaxed positions
+    # the scan path (relax_scan inside perform_relaxation)
+    p = dict(charge=0.0, klat=float(g["klat"]), krad=float(g["krad"]), r0Probe=list(g["r0Probe"]), scanMin=list(g["scanMin"]), scanMax=list(g["scanMax"]), scanStep=list(g["scanStep"]))
+    fzs, PPpos, _, _ = HL.perform_relaxation(lv, FF, parameters=p, relax=dict(maxIters=300, convF2=1e-8, dt=0.5, damping=0.1), tip_spline=core.SplineParameters(xs, ydys))
+    fz_o, pp_o, _ = oracle.relaxed_scan(g["n"], lv[1:], FF, prm, xT, yT, zT, lv[0], spline=(xs, ydys))
+    flips = _check_positions(np.linalg.norm(PPpos - pp_o, axis=-1))
+    assert np.abs(fzs - fz_o)[~flips].max() < 1e-4
+
+
+def test_batch_refuses_tip_spline(gpulib):
+    from ppafm_gb300 import device, workloads
+    from ppafm_gb300._lib import PPGPUError
+    from ppafm_gb300.batch import BatchPipeline
+
+    systems = workloads.molecule_batch(seed=1, nmol=1, scale=0.2)
+    w = systems[0]
+    relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    with device.tip_spline(_spline(20.0)):
+        with pytest.raises(PPGPUError, match="spline"):
+            BatchPipeline(systems, w, relax=relax)
+    BatchPipeline(systems, w, relax=relax).close()  # cleared again

@@ -183,6 +183,27 @@ def test_oracle_vs_compiled_reference(oracle):
         L.relaxTipStrokes_omp(3, 4, ps, alg, 7, rT, rs, fs, None)
         rs2, fs2, _, _ = oracle.relax_strokes(n, cell, FF, prm, rT, probeStart=ps, relaxAlg=alg)
         assert np.array_equal(rs, rs2) and np.array_equal(fs, fs2), (maxit, dt, alg, ps)
+    # radial tip spline (forceRSpline): 7 knots (the reference's halving search skips some
+    # intervals when the count is not a power of two), a stiff radial force around l0 = 3.5
+    import ctypes
+
+    class SplineParams(ctypes.Structure):
+        _fields_ = [("rff_n", ctypes.c_int), ("rff_xs", ctypes.POINTER(ctypes.c_double)), ("rff_ydys", ctypes.POINTER(ctypes.c_double))]
+
+    xs = np.linspace(2.0, 5.0, 7)
+    k = 15 / -oracle.eVA_Nm
+    ydys = np.ascontiguousarray(np.column_stack([k * (xs - 3.5) + 0.05 * (xs - 3.5) ** 3, k + 0.15 * (xs - 3.5) ** 2]))
+    sp = SplineParams(len(xs), xs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ydys.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    L.setRelax(300, 1e-8, 0.5, 0.1)
+    for ps in (1, 0):
+        rs = np.zeros_like(rT)
+        fs = np.zeros_like(rT)
+        L.relaxTipStrokes_omp(3, 4, ps, 1, 7, rT, rs, fs, ctypes.cast(ctypes.pointer(sp), ctypes.c_void_p))
+        prm = oracle.relax_param_vector(tip, maxIters=300, convF2=1e-8, dt=0.5, damping=0.1)
+        rs2, fs2, _, _ = oracle.relax_strokes(n, cell, FF, prm, rT, probeStart=ps, relaxAlg=1, spline=(xs, ydys))
+        assert np.array_equal(rs, rs2) and np.array_equal(fs, fs2), ps
+        rs3, _, _, _ = oracle.relax_strokes(n, cell, FF, prm, rT, probeStart=ps, relaxAlg=1)
+        assert not np.array_equal(rs3, rs2)  # the spline is in effect
 
 
 def test_poisson_plane_wave_skewed_cell(oracle):
