@@ -200,6 +200,11 @@ int ppgpu_fft_density_power(void *handle, float *rho, double B, int fix_negative
  * zero mean.  No counterpart in the reference (it reads potentials from DFT files). */
 int ppgpu_fft_poisson(void *handle, const float *rho_charge, const double *lvec, float *V, void *stream);
 
+/* AFMulator Hartree route, cross-correlation (FFTCrossCorrelation.correlate,
+ * ppafm/ocl/field.py:800-840): E = IFFT(conj(FFT(rho)) FFT(V)) * scale / N on the plan's grid
+ * (scale: the tip density's voxel volume in the reference). */
+int ppgpu_fft_correlate(void *handle, const float *V, const float *rho, double scale, float *E, void *stream);
+
 /* Sum of normalised 3-D Gaussians on a periodic grid (minimum-image distances): atoms is a
  * DEVICE float64 array [natoms][5] = (x, y, z relative to the origin, sigma, weight).  Builds
  * synthetic electron and tip densities; no counterpart in the reference (it reads densities
@@ -279,6 +284,20 @@ int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const double *W,
                 void *stream);
 /* |F| <= Fmax clamp of a float4 grid, direction preserved (io.py:766-778). */
 int ppgpu_clamp_grid(float *FE, long long npts, double Fmax, void *stream);
+
+/* DataGrid.interp_at (ppafm/ocl/field.py:515-572, kernel interp_at, FF.cl:1010-1046): out
+ * [nout0][nout1][nout2] float32 = periodic trilinear interpolation of in[nin0][nin1][nin2]
+ * (origin origin_in[3], step vectors step_in[3][3] as rows) at origin_out + i a + j b + k c
+ * (step_out rows), rotated about rot_center[3] by rot[3][3] (rows; NULL = none). */
+int ppgpu_interp_grid(const float *in, const int *nin, const double *origin_in, const double *step_in, float *out,
+                      const int *nout, const double *origin_out, const double *step_out, const double *rot,
+                      const double *rot_center, void *stream);
+
+/* DataGrid.grad (ppafm/ocl/field.py:454-513, kernel grad, FF.cl:920-961) in C order: FE float4
+ * [n0][n1][n2] = scale[0..3] * (dE/dx, dE/dy, dE/dz, E), periodic centred differences with the
+ * steps step[3]; accumulate != 0 adds to FE. */
+int ppgpu_grad_fd(const float *E, const int *n, const double *step, const double *scale, float *FE, int accumulate,
+                  void *stream);
 /* FE_out = a*FE_a + b*FE_b (float4 grids; E included). */
 int ppgpu_axpby_grid(float *FE_out, const float *FE_a, double a, const float *FE_b, double b, long long npts,
                      void *stream);

@@ -535,6 +535,65 @@ def afm_ff_qzs(nDim, lvec, xyzs, qs, cLJs, Qs, QZs, nthreads=0):
     return FE
 
 
+def interp_at(arr, lvec_in, nout, origin_out, step_out, rot=np.eye(3), rot_center=np.zeros(3)):
+    """Periodic trilinear interpolation of a grid onto rotated grid points (interp_at +
+    linearInterpB, ppafm/ocl/cl/FF.cl:34-72, 1010-1046), in float32 like the kernel; output
+    [nout0, nout1, nout2], C order."""
+    arr = np.asarray(arr, np.float32)
+    n = np.array(arr.shape)
+    lvec_in = np.asarray(lvec_in, np.float64)
+    T = np.linalg.inv(lvec_in[1:] / n[:, None]).T.astype(np.float32)
+    f32 = np.float32
+    i, j, k = np.meshgrid(*[np.arange(m, dtype=np.float32) for m in nout], indexing="ij")
+    so = np.asarray(step_out, np.float32)
+    o = np.asarray(origin_out, np.float32)
+    pos = [o[c] + i * so[0, c] + j * so[1, c] + k * so[2, c] for c in range(3)]
+    rc = np.asarray(rot_center, np.float32)
+    R = np.asarray(rot, np.float32)
+    d = [pos[c] - rc[c] for c in range(3)]
+    pos = [rc[c] + (R[c, 0] * d[0] + R[c, 1] * d[1] + R[c, 2] * d[2]) for c in range(3)]
+    oi = np.asarray(lvec_in[0], np.float32)
+    cc = [pos[c] - oi[c] for c in range(3)]
+    g = [cc[0] * T[a, 0] + cc[1] * T[a, 1] + cc[2] * T[a, 2] for a in range(3)]
+    fl = [np.floor(x) for x in g]
+    t = [np.minimum(g[a] - fl[a], f32(0.99999994)) for a in range(3)]
+    i0 = [np.mod(fl[a].astype(np.int64), n[a]) for a in range(3)]
+    i1 = [(i0[a] + 1) % n[a] for a in range(3)]
+    out = np.zeros(tuple(nout), np.float32)
+    for bx in (0, 1):
+        for by in (0, 1):
+            for bz in (0, 1):
+                w = (t[0] if bx else 1 - t[0]) * (t[1] if by else 1 - t[1]) * (t[2] if bz else 1 - t[2])
+                out += w * arr[(i1 if bx else i0)[0], (i1 if by else i0)[1], (i1 if bz else i0)[2]]
+    return out
+
+
+def hartree_ff(nDim, lvec, pot_array, pot_lvec, rho_multipole, sigma, xyzs, cLJs, rot_ff, rot_center, nthreads=0):
+    """calc_force_hartree (ppafm/ocl/field.py:1446-1504) restated: the potential interpolated
+    onto the force-field grid, cross-correlated with the multipole tip density by FFT (float64
+    numpy), F = -grad E by periodic centred differences, plus Lennard-Jones (evalLJ form,
+    R2SAFE 1e-6).  FE [nz, ny, nx, 4] x-fastest like afm_ff_qzs."""
+    nDim = np.asarray(nDim)
+    lvec = np.asarray(lvec, np.float64)
+    step = lvec[1:4] / nDim[:, None]
+    pot_i = interp_at(pot_array, pot_lvec, nDim, lvec[0], step, rot_ff, rot_center).astype(np.float64)
+    L = np.linalg.norm(lvec[1:4], axis=1)
+    coords = []
+    for a in range(3):
+        c = np.linspace(0, L[a] * (1 - 1 / nDim[a]), nDim[a])
+        c[c >= L[a] / 2] -= L[a]
+        coords.append(c)
+    X, Y, Z = np.meshgrid(*coords, indexing="ij")
+    rho = getProbeDensity(np.vstack([np.zeros(3), lvec[1:4]]), X, Y, Z, L / nDim, sigma=sigma, multipole_dict=rho_multipole)
+    rho = rho.astype(np.float32).astype(np.float64)
+    E = np.real(np.fft.ifftn(np.conj(np.fft.fftn(rho)) * np.fft.fftn(pot_i))) * abs(np.linalg.det(step))
+    hs = np.diag(step)
+    F = [-0.5 * (np.roll(E, -1, axis=a) - np.roll(E, 1, axis=a)) / hs[a] for a in range(3)]
+    FEc = np.stack(F + [E], axis=-1)
+    LJ = afm_ff_qzs(nDim, lvec, xyzs, np.zeros(len(xyzs)), cLJs, np.zeros(4), np.zeros(4), nthreads=nthreads)
+    return (FEc.transpose(2, 1, 0, 3) + LJ).astype(np.float32)
+
+
 def afm_ff_qzs64(nDim, lvec, xyzs, qs, cLJs, Qs, QZs, points=None):
     """evalLJC_QZs_noPos's sum in float64 (numpy), at the listed grid points (ia,ib,ic) or
     all points; returns [npoints, 4] (Fx, Fy, Fz, E)."""
@@ -609,15 +668,25 @@ class AFMulator:
         self.dfWeight = get_simple_df_weight(df_steps, dz=self.dz).astype(np.float32)
         self.dfWeight *= eVA_Nm * f0Cantilever / kCantilever
 
-    def eval(self, xyzs, Zs, qs, sample_lvec=None, nthreads=0, return_all=False):
+    def eval(self, xyzs, Zs, qs, sample_lvec=None, nthreads=0, return_all=False, pot=None, rho=None, sigma=0.71, rot=np.eye(3)):
+        """pot = (array [n0,n1,n2], lvec [4,3]) selects the Hartree route with the multipole tip
+        density rho (dict); otherwise point charges qs."""
+        if pot is not None:
+            sample_lvec = np.asarray(pot[1])[1:] if sample_lvec is None else sample_lvec
+            qs = np.zeros(len(Zs))
         npbc = self.npbc if sample_lvec is not None else (0, 0, 0)
         REAs = getAtomsREA(self.iZPP, Zs, self.FFparams)
         cLJs = REA2LJ(REAs)
         xyzs = np.asarray(xyzs, np.float64)
         qs = np.asarray(qs, np.float64)
+        rot_center = xyzs.mean(axis=0)
         if sum(npbc) > 0:
             Zs, xyzs, qs, cLJs = PBCAtoms3D_np(Zs, xyzs, qs, cLJs, sample_lvec, npbc=npbc)
-        FE = afm_ff_qzs(self.nDim, self.lvec, xyzs, qs, cLJs, self.Qs, self.QZs, nthreads=nthreads)
+        xyzs = np.dot(xyzs - rot_center, np.asarray(rot).T) + rot_center
+        if pot is not None:
+            FE = hartree_ff(self.nDim, self.lvec, pot[0], pot[1], rho, sigma, xyzs, cLJs, np.linalg.inv(rot), rot_center, nthreads=nthreads)
+        else:
+            FE = afm_ff_qzs(self.nDim, self.lvec, xyzs, qs, cLJs, self.Qs, self.QZs, nthreads=nthreads)
         cell = self.lvec[1:4]
         invCell = np.transpose(np.linalg.inv(cell)).astype(np.float32)
         pos0 = np.array([0, 0, self.scan_window[1][2]]) - self.lvec[0]

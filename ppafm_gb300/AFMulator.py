@@ -1,15 +1,22 @@
 """AFMulator with the reference's constructor and ``eval`` signature
-(ppafm/ocl/AFMulator.py:83-173), point-charge method, on libppgpu.
+(ppafm/ocl/AFMulator.py:83-173) on libppgpu: point-charge and Hartree force fields.
 
-eval(xyzs, Zs, qs) builds the Lennard-Jones + tip-point-charge force field
-(evalLJC_QZs_noPos, ppafm/ocl/cl/FF.cl:366-423) in HBM, relaxes every pixel column with
-the tilted-stroke FIRE of relaxStrokesTilted (ppafm/ocl/cl/relax.cl:391-464) and applies
-the z convolution (convolveZ, relax.cl:571-608) in the same kernel, returning the Δf
-stack X [nx, ny, nz - df_steps + 1].  Interpolation uses exact float32 trilinear weights
-where the reference samples an OpenCL image with hardware filtering.
+eval(xyzs, Zs, qs) builds the force field in HBM, relaxes every pixel column with the
+tilted-stroke FIRE of relaxStrokesTilted (ppafm/ocl/cl/relax.cl:391-464) and applies the z
+convolution (convolveZ, relax.cl:571-608) in the same kernel, returning the Δf stack
+X [nx, ny, nz - df_steps + 1].  Interpolation uses exact float32 trilinear weights where the
+reference samples an OpenCL image with hardware filtering.
 
-Not provided: Hartree-potential and FDBM force fields (``qs`` as a potential,
-``rho``/``rho_delta``/``rho_sample``), plotting.
+Force fields:
+  * point charges (qs an array): Lennard-Jones + tip point charges (evalLJC_QZs_noPos,
+    ppafm/ocl/cl/FF.cl:366-423);
+  * Hartree (qs a HartreePotential, a tip density set with ``rho``): the potential
+    interpolated onto the force-field grid (interp_at), cross-correlated with the tip density
+    by FFT, differentiated by centred differences, plus Lennard-Jones (calc_force_hartree,
+    ppafm/ocl/field.py:1446-1504).
+
+Not provided: the Hartree route with a point-charge tip (no ``rho``), FDBM (``rho_delta``,
+``rho_sample``), tip densities on grids other than the force field's, plotting.
 """
 
 import time
@@ -20,8 +27,49 @@ import torch
 from . import common
 from ._lib import AFM_NPARAM, FF_QZS, check, dptr, iptr, lib, stream_handle, tptr
 from .device import DeviceFF, iter_counter, pack_atoms
+from .fieldFFT import FFTGrid
 
 VALID_SIZES = np.array([16, 32, 64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048])
+
+
+class DataGrid:
+    """A scalar field on a periodic grid (ppafm/ocl/field.py:115-200): array [n0, n1, n2]
+    float32 (C order, the first axis along the first lattice vector) and lvec [4, 3] (origin,
+    then the lattice vectors)."""
+
+    def __init__(self, array, lvec):
+        self.array = np.ascontiguousarray(array, dtype=np.float32)
+        if self.array.ndim != 3:
+            raise ValueError(f"a scalar grid needs 3 dimensions, got {self.array.ndim}")
+        self.shape = tuple(self.array.shape)
+        self.lvec = np.array(lvec, dtype=np.float64)
+        assert self.lvec.shape == (4, 3), f"lvec should have shape (4, 3), but has shape {self.lvec.shape}"
+        self.origin = self.lvec[0]
+        self._dev = None
+
+    @property
+    def step(self):
+        """Single steps along each lattice vector (rows)."""
+        return np.stack([self.lvec[i + 1] / self.shape[i] for i in range(3)])
+
+    @property
+    def cell_vol(self):
+        a, b, c = self.step
+        return abs(np.cross(a, b).dot(c))
+
+    def device(self):
+        """The array in device memory (uploaded once)."""
+        if self._dev is None:
+            self._dev = torch.from_numpy(self.array).cuda()
+        return self._dev
+
+
+class HartreePotential(DataGrid):
+    """Sample Hartree potential in volts."""
+
+
+class TipDensity(DataGrid):
+    """Tip charge density in e/A^3, centred on the grid origin (wrapped)."""
 
 
 def get_lvec(scan_window, pad=(3.0, 3.0, 5.0), tipR0=(0.0, 0.0, 3.0), pixPerAngstrome=10):
@@ -43,8 +91,8 @@ class AFMulator:
 
     def __init__(self, pixPerAngstrome=10, lvec=None, scan_dim=(128, 128, 30), scan_window=((2.0, 2.0, 7.0), (18.0, 18.0, 10.0)), iZPP=8, QZs=[0.1, 0, -0.1, 0], Qs=[-10, 20, -10, 0], rho=None, sigma=0.71, rho_delta=None, A_pauli=18.0, B_pauli=1.0,
                  fdbm_vdw_type="D3", d3_params="PBE", lj_vdw_damp=2, df_steps=10, tipR0=[0.0, 0.0, 3.0], tipStiffness=[0.25, 0.25, 0.0, 30.0], npbc=(1, 1, 0), f0Cantilever=30300, kCantilever=1800, colorscale="gray", minimize_memory=False):
-        if rho is not None or rho_delta is not None:
-            raise NotImplementedError("tip densities (Hartree / FDBM force fields) are not supported")
+        if rho_delta is not None:
+            raise NotImplementedError("tip delta densities (FDBM) are not supported")
         self.iZPP = iZPP
         self.tipR0 = np.array(tipR0, dtype=np.float64)  # a copy: randomize_tip edits it in place
         self.f0Cantilever = f0Cantilever
@@ -59,9 +107,13 @@ class AFMulator:
         self.typeParams = common.loadSpecies()
         self.counter = None
         self._ff = None
+        self.rho = None
+        self._rho_dev = None
+        self._fft = None
         self.setScanWindow(scan_window, scan_dim, df_steps)
         self.setLvec(lvec, pixPerAngstrome)
         self.setQs(Qs, QZs)
+        self.setRho(rho, sigma, B_pauli)
         self.last_timing = {}
 
     # ------------------------------------------------------------------ set-up
@@ -72,6 +124,7 @@ class AFMulator:
         self.lvec = np.asarray(lvec, dtype=np.float64) if lvec is not None else get_lvec(self.scan_window, tipR0=self.tipR0, pixPerAngstrome=self.pixPerAngstrome)
         self.nDim = common.genFFSampling(self.lvec, pixPerAngstrome=self.pixPerAngstrome)
         self._ff = None
+        self._rho_dev = None  # the tip density follows the force-field grid
 
     def setScanWindow(self, scan_window=None, scan_dim=None, df_steps=None):
         """Scan geometry and the Δf weights (AFMulator.py:211-241)."""
@@ -99,8 +152,60 @@ class AFMulator:
         self.stiffness = np.array(tipStiffness, dtype=np.float32) / np.float32(-common.eVA_Nm)
 
     def setRho(self, rho=None, sigma=0.71, B_pauli=1.0):
-        if rho is not None:
-            raise NotImplementedError("tip densities are not supported")
+        """Tip charge density for the Hartree route (AFMulator.py:243-288): a multipole dict
+        (e.g. {"dz2": -0.1}) made on the force-field grid like MultipoleTipDensity, or a
+        TipDensity on that grid; None removes it."""
+        if rho is not None and not isinstance(rho, (dict, TipDensity)):
+            raise ValueError(f"rho should be a dict or a TipDensity, but got `{type(rho)}`")
+        if not np.allclose(B_pauli, 1.0):
+            raise NotImplementedError("density exponents other than 1 belong to FDBM, which is not supported")
+        self.rho = rho
+        self.sigma = sigma
+        self.B_pauli = B_pauli
+        self._rho_dev = None
+
+    def _tip_density(self):
+        """The tip density on the force-field grid (device, cached)."""
+        if self._rho_dev is not None:
+            return self._rho_dev
+        n = tuple(int(x) for x in self.nDim)
+        if self._fft is None or tuple(self._fft.n) != n:
+            self._fft = FFTGrid(n)
+        if isinstance(self.rho, dict):
+            # MultipoleTipDensity (field.py:653-700): getProbeDensity on coordinates wrapped
+            # around the grid origin
+            self._rho_dev = self._fft.probe_density(np.vstack([np.zeros(3), self.lvec[1:4]]), self.sigma, self.rho)
+        else:
+            if tuple(self.rho.shape) != n or not np.allclose(self.rho.lvec[1:], self.lvec[1:]):
+                raise NotImplementedError("the tip density must be given on the force-field grid")
+            self._rho_dev = self.rho.device()
+        return self._rho_dev
+
+    def _hartree_ff(self, pot, atoms_rec, na, rot, rot_center, stream=None):
+        """calc_force_hartree (field.py:1446-1504) on the force-field grid: the potential
+        interpolated onto it (rotated by the inverse of the atoms' rotation), cross-correlated
+        with the tip density, F = -grad E by centred differences, then + Lennard-Jones."""
+        if self.rho is None:
+            raise NotImplementedError("the Hartree route needs a tip density (AFMulator(rho=...)); the point-charge tip variant is not supported")
+        lv = self.lvec
+        if (np.abs(lv[1:4] - np.diag(np.diag(lv[1:4]))) > 0).any():
+            raise NotImplementedError("Forcefield calculation via FFT for non-rectangular grids is not implemented.")
+        rho = self._tip_density()
+        n = np.array(self.nDim, dtype=np.int32)
+        step_out = np.ascontiguousarray(lv[1:4] / n[:, None], dtype=np.float64)
+        pot_i = self._fft.empty()
+        rot_ff = np.ascontiguousarray(np.linalg.inv(rot), dtype=np.float64)
+        check(lib().ppgpu_interp_grid(tptr(pot.device()), iptr(np.array(pot.shape, dtype=np.int32)), dptr(np.ascontiguousarray(pot.origin, dtype=np.float64)),
+                                      dptr(np.ascontiguousarray(pot.step, dtype=np.float64)), tptr(pot_i), iptr(n), dptr(np.ascontiguousarray(lv[0], dtype=np.float64)),
+                                      dptr(step_out), dptr(rot_ff), dptr(np.ascontiguousarray(rot_center, dtype=np.float64)), stream_handle(stream)))
+        vox = abs(np.linalg.det(step_out))
+        E = self._fft.correlate(pot_i, rho, scale=vox, stream=stream)
+        if self._ff is None:
+            self._ff = DeviceFF(self.nDim, self.lvec)
+        check(lib().ppgpu_grad_fd(tptr(E), iptr(n), dptr(np.ascontiguousarray(np.diag(step_out))), dptr(np.array([-1.0, -1.0, -1.0, 1.0])), tptr(self._ff.FE), 0, stream_handle(stream)))
+        zero4 = np.zeros(4)
+        self._ff.compute(atoms_rec, na, 0, FF_QZS, Qs=zero4, QZs=zero4, with_E=True, accumulate=True, stream=stream)
+        return self._ff
 
     # --------------------------------------------------------------- imaging
 
@@ -108,11 +213,16 @@ class AFMulator:
         """Point-charge force field on the device (AFMulator.py:321-429, field.py:1608-1713)."""
         if rho_sample is not None:
             raise NotImplementedError("FDBM (rho_sample) is not supported")
-        if qs is not None and not isinstance(qs, np.ndarray):
+        pot = None
+        if isinstance(qs, HartreePotential):
+            pot = qs
+            qs = np.zeros(len(Zs))
+            self.sample_lvec = np.asarray(sample_lvec) if sample_lvec is not None else pot.lvec[1:]
+        elif qs is not None and not isinstance(qs, np.ndarray):
             qs = np.asarray(qs)
         if qs is None:
             qs = np.zeros(len(Zs))
-        if sample_lvec is not None:
+        if sample_lvec is not None and pot is None:
             self.sample_lvec = np.asarray(sample_lvec)
         npbc = self.npbc if self.sample_lvec is not None else (0, 0, 0)
         xyzs = np.asarray(xyzs)
@@ -133,6 +243,8 @@ class AFMulator:
         R = atoms32[:, :3].astype(np.float64) - self.lvec[0]
         rec, na, nch = pack_atoms(R, c32.astype(np.float64), atoms32[:, 3].astype(np.float64))
         self._atoms = rec
+        if pot is not None:
+            return self._hartree_ff(pot, rec, na, np.asarray(rot, dtype=np.float64), np.asarray(rot_center, dtype=np.float64), stream=stream)
         self._ff.compute(rec, na, nch, FF_QZS, Qs=self.Qs.astype(np.float64), QZs=self.QZs.astype(np.float64), with_E=True, stream=stream)
         return self._ff
 

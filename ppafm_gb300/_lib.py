@@ -62,6 +62,8 @@ SIGNATURES = {
     "ppgpu_relax_afm": ([c_void_p, _ip, _dp, _dp, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, _dp, c_void_p, c_void_p, c_void_p], c_int),
     "ppgpu_fz2df": ([c_void_p, c_longlong, c_int, c_int, _dp, c_double, c_void_p, c_void_p], c_int),
     "ppgpu_clamp_grid": ([c_void_p, c_longlong, c_double, c_void_p], c_int),
+    "ppgpu_interp_grid": ([c_void_p, _ip, _dp, _dp, c_void_p, _ip, _dp, _dp, _dp, _dp, c_void_p], c_int),
+    "ppgpu_grad_fd": ([c_void_p, _ip, _dp, _dp, c_void_p, c_int, c_void_p], c_int),
     "ppgpu_axpby_grid": ([c_void_p, c_void_p, c_double, c_void_p, c_double, c_longlong, c_void_p], c_int),
     "ppgpu_grid_from_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_void_p], c_int),
     "ppgpu_grid_to_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_int, c_void_p], c_int),
@@ -72,6 +74,7 @@ SIGNATURES = {
     "ppgpu_fft_probe_density": ([c_void_p, c_void_p, _dp, c_double, _dp, c_void_p], c_int),
     "ppgpu_fft_density_power": ([c_void_p, c_void_p, c_double, c_int, c_void_p], c_int),
     "ppgpu_fft_poisson": ([c_void_p, c_void_p, _dp, c_void_p, c_void_p], c_int),
+    "ppgpu_fft_correlate": ([c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p], c_int),
     "ppgpu_gaussian_density": ([c_void_p, _ip, _dp, c_int, c_void_p, c_int, c_void_p], c_int),
     "ppgpu_lj_grid_f64_noalloc": ([c_void_p, c_void_p, _ip, _dp, c_int, c_void_p, c_void_p, c_void_p], c_int),
     "ppgpu_batch_create": ([c_void_p, c_int, _dp, c_double, c_double, c_int, _dp, _ip, POINTER(c_void_p)], c_int),

@@ -291,6 +291,19 @@ __global__ void poisson_kernel(C *Rk, PoissonPrm P) {
     Rk[q] = Cx<C>::make(r.x * f, r.y * f);
 }
 
+// ------------------------------------------------------------ cross-correlation
+
+// S = conj(R) V s over the half spectrum (the AFMulator's FFTCrossCorrelation,
+// ppafm/ocl/field.py:707-840: conj_mult then the scaled inverse transform).
+template <typename C>
+__global__ void corr_mul_kernel(const C *__restrict__ Vk, const C *__restrict__ Rk, C *__restrict__ Sk, long long Nh,
+                                typename Cx<C>::real s) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= Nh) return;
+    const C a = Vk[q], b = Rk[q];
+    Sk[q] = Cx<C>::make((b.x * a.x + b.y * a.y) * s, (b.x * a.y - b.y * a.x) * s);
+}
+
 // ------------------------------------------------------------- Gaussian densities
 
 // rho[p] (+)= sum_i w_i g(|p - R_i|; s_i), normalised 3-D Gaussians, minimum-image distance
@@ -574,5 +587,35 @@ extern "C" int ppgpu_gaussian_density(float *rho, const int *n, const double *lv
     gauss_density_kernel<<<blocks_for(N), FFT_THREADS, 0, (cudaStream_t)stream>>>(rho, n[0], n[1], n[2], C, atoms,
                                                                                 natoms, accumulate);
     PPGPU_CHECK_LAUNCH("gauss_density_kernel");
+    return set_ok();
+}
+
+/* E = IFFT(conj(FFT(rho)) FFT(V)) * scale / N: the circular cross-correlation of the AFMulator's
+ * Hartree route (FFTCrossCorrelation.correlate, ppafm/ocl/field.py:800-840, with reikna's
+ * normalised inverse).  V, rho, E: float32 grids of the plan's size. */
+extern "C" int ppgpu_fft_correlate(void *handle, const float *V, const float *rho, double scale, float *E, void *stream) {
+    FFTPlan *P = (FFTPlan *)handle;
+    if (!P || !V || !rho || !E) return set_error(PPGPU_ERR_ARG, "correlate: null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    PPGPU_CUFFT(cufftSetStream(P->r2c, st), "cufftSetStream");
+    PPGPU_CUFFT(cufftSetStream(P->c2r1, st), "cufftSetStream");
+    double *stage = (double *)P->planar;
+    int rc;
+    if ((rc = forward(P, V, P->Vk, stage, st, "forward V")) != PPGPU_OK) return rc;
+    if ((rc = forward(P, rho, P->Rk, stage, st, "forward rho")) != PPGPU_OK) return rc;
+    const double s = scale / (double)P->N;
+    if (P->f64) {
+        corr_mul_kernel<cufftDoubleComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>(
+            (const cufftDoubleComplex *)P->Vk, (const cufftDoubleComplex *)P->Rk, (cufftDoubleComplex *)P->S4, P->Nh, s);
+        PPGPU_CHECK_LAUNCH("corr_mul_kernel");
+        PPGPU_CUFFT(cufftExecZ2D(P->c2r1, (cufftDoubleComplex *)P->S4, stage), "inverse E");
+        f64_to_f32_kernel<<<blocks_for(P->N), FFT_THREADS, 0, st>>>(E, stage, P->N);
+        PPGPU_CHECK_LAUNCH("f64_to_f32_kernel");
+    } else {
+        corr_mul_kernel<cufftComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>(
+            (const cufftComplex *)P->Vk, (const cufftComplex *)P->Rk, (cufftComplex *)P->S4, P->Nh, (float)s);
+        PPGPU_CHECK_LAUNCH("corr_mul_kernel");
+        PPGPU_CUFFT(cufftExecC2R(P->c2r1, (cufftComplex *)P->S4, E), "inverse E");
+    }
     return set_ok();
 }

@@ -110,6 +110,80 @@ __global__ void __launch_bounds__(256) ffma_kernel(float *sink, int iters) {
     if (s == 12345.678f) sink[threadIdx.x] = s;  // keeps the chains alive
 }
 
+// ------------------------------------------------ grids of the AFMulator's Hartree route
+
+// Periodic trilinear interpolation of a scalar grid at point pos (linearInterpB,
+// ppafm/ocl/cl/FF.cl:34-72): lattice coordinate (pos - origin) . T rows, float32.
+__device__ __forceinline__ float lin_interp_b(const float *in, int3 n, float3 o, float3 TA, float3 TB, float3 TC,
+                                              float3 pos) {
+    const float3 c = make_float3(pos.x - o.x, pos.y - o.y, pos.z - o.z);
+    const float3 g = make_float3(c.x * TA.x + c.y * TA.y + c.z * TA.z, c.x * TB.x + c.y * TB.y + c.z * TB.z,
+                                 c.x * TC.x + c.y * TC.y + c.z * TC.z);
+    const float fx = floorf(g.x), fy = floorf(g.y), fz = floorf(g.z);
+    // fract(): x - floor(x), kept below 1
+    const float dx = fminf(g.x - fx, 0x1.fffffep-1f), dy = fminf(g.y - fy, 0x1.fffffep-1f),
+                dz = fminf(g.z - fz, 0x1.fffffep-1f);
+    auto wrap = [](int i, int m) {
+        const int r = i % m;
+        return r >= 0 ? r : r + m;
+    };
+    const int i0 = wrap((int)fx, n.x), j0 = wrap((int)fy, n.y), k0 = wrap((int)fz, n.z);
+    const int i1 = (i0 + 1) % n.x, j1 = (j0 + 1) % n.y, k1 = (k0 + 1) % n.z;
+    const long long nyz = (long long)n.y * n.z;
+    auto at = [&](int i, int j, int k) { return in[i * nyz + (long long)j * n.z + k]; };
+    return (1 - dx) * (1 - dy) * (1 - dz) * at(i0, j0, k0) + (1 - dx) * (1 - dy) * dz * at(i0, j0, k1) +
+           (1 - dx) * dy * (1 - dz) * at(i0, j1, k0) + (1 - dx) * dy * dz * at(i0, j1, k1) +
+           dx * (1 - dy) * (1 - dz) * at(i1, j0, k0) + dx * (1 - dy) * dz * at(i1, j0, k1) +
+           dx * dy * (1 - dz) * at(i1, j1, k0) + dx * dy * dz * at(i1, j1, k1);
+}
+
+struct InterpPrm {
+    int3 nin, nout;
+    float3 TA, TB, TC, oin;          // input lattice transform rows, input origin
+    float3 sA, sB, sC, oout;         // output grid steps and origin
+    float3 rA, rB, rC, rc;           // rotation rows and centre
+};
+
+// interp_at (ppafm/ocl/cl/FF.cl:1010-1046): output point (i, j, k), C order, rotated about rc.
+__global__ void interp_at_kernel(const float *__restrict__ in, float *__restrict__ out, InterpPrm P, long long nout) {
+    for (long long ind = blockIdx.x * (long long)blockDim.x + threadIdx.x; ind < nout;
+         ind += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(ind / ((long long)P.nout.y * P.nout.z));
+        const int j = (int)((ind / P.nout.z) % P.nout.y);
+        const int k = (int)(ind % P.nout.z);
+        float3 pos = make_float3(P.oout.x + i * P.sA.x + j * P.sB.x + k * P.sC.x, P.oout.y + i * P.sA.y + j * P.sB.y + k * P.sC.y,
+                                 P.oout.z + i * P.sA.z + j * P.sB.z + k * P.sC.z);
+        const float3 d = make_float3(pos.x - P.rc.x, pos.y - P.rc.y, pos.z - P.rc.z);
+        pos = make_float3(P.rc.x + (P.rA.x * d.x + P.rA.y * d.y + P.rA.z * d.z), P.rc.y + (P.rB.x * d.x + P.rB.y * d.y + P.rB.z * d.z),
+                          P.rc.z + (P.rC.x * d.x + P.rC.y * d.y + P.rC.z * d.z));
+        out[ind] = lin_interp_b(in, P.nin, P.oin, P.TA, P.TB, P.TC, pos);
+    }
+}
+
+// grad (ppafm/ocl/cl/FF.cl:920-961) in C order: FE = scale * (dE/dx, dE/dy, dE/dz, E) by
+// periodic centred differences; accumulate adds to FE.
+__global__ void grad_fd_kernel(const float *__restrict__ E, float4 *__restrict__ FE, int3 n, float3 step, float4 scale,
+                               int accumulate, long long npts) {
+    for (long long ind = blockIdx.x * (long long)blockDim.x + threadIdx.x; ind < npts;
+         ind += (long long)gridDim.x * blockDim.x) {
+        const long long nyz = (long long)n.y * n.z;
+        const int i = (int)(ind / nyz), j = (int)((ind % nyz) / n.z), k = (int)(ind % n.z);
+        const long long ip = i > 0 ? ind - nyz : ind + (long long)(n.x - 1) * nyz;
+        const long long jp = j > 0 ? ind - n.z : ind + (long long)(n.y - 1) * n.z;
+        const long long kp = k > 0 ? ind - 1 : ind + (n.z - 1);
+        const long long in_ = i < n.x - 1 ? ind + nyz : ind - (long long)(n.x - 1) * nyz;
+        const long long jn = j < n.y - 1 ? ind + n.z : ind - (long long)(n.y - 1) * n.z;
+        const long long kn = k < n.z - 1 ? ind + 1 : ind - (n.z - 1);
+        float4 f = make_float4(scale.x * (0.5f * (E[in_] - E[ip]) / step.x), scale.y * (0.5f * (E[jn] - E[jp]) / step.y),
+                               scale.z * (0.5f * (E[kn] - E[kp]) / step.z), scale.w * E[ind]);
+        if (accumulate) {
+            const float4 o = FE[ind];
+            f = make_float4(f.x + o.x, f.y + o.y, f.z + o.z, f.w + o.w);
+        }
+        FE[ind] = f;
+    }
+}
+
 }  // namespace ppgpu
 
 using namespace ppgpu;
@@ -174,5 +248,66 @@ extern "C" int ppgpu_ffma_peak(float *scratch, int iters, long long *fma_count, 
     ffma_kernel<<<nblk, 256, 0, (cudaStream_t)stream>>>(scratch, iters);
     PPGPU_CHECK_LAUNCH("ffma_kernel");
     if (fma_count) *fma_count = (long long)nblk * 256 * 8 * (long long)iters;
+    return set_ok();
+}
+
+static float3 f3(const double *v) { return make_float3((float)v[0], (float)v[1], (float)v[2]); }
+
+/* interp_at (ppafm/ocl/cl/FF.cl:1010-1046, DataGrid.interp_at, ppafm/ocl/field.py:515-572):
+ * out[nout0][nout1][nout2] = periodic trilinear interpolation of in[nin0][nin1][nin2] (lattice
+ * origin origin_in, steps step_in rows) at origin_out + i a + j b + k c (step_out rows), rotated
+ * about rot_center by rot (rows).  float32 arithmetic like the reference. */
+extern "C" int ppgpu_interp_grid(const float *in, const int *nin, const double *origin_in, const double *step_in,
+                                 float *out, const int *nout, const double *origin_out, const double *step_out,
+                                 const double *rot, const double *rot_center, void *stream) {
+    if (!in || !nin || !origin_in || !step_in || !out || !nout || !origin_out || !step_out)
+        return set_error(PPGPU_ERR_ARG, "interp_grid: null argument");
+    for (int k = 0; k < 3; k++)
+        if (nin[k] <= 0 || nout[k] <= 0) return set_error(PPGPU_ERR_ARG, "interp_grid: sizes must be positive");
+    // T = inv(step_in)^T rows (g = coord . T rows)
+    const double *m = step_in;
+    const double A = m[4] * m[8] - m[5] * m[7], B = -(m[3] * m[8] - m[5] * m[6]), C = m[3] * m[7] - m[4] * m[6];
+    const double det = m[0] * A + m[1] * B + m[2] * C;
+    if (!(det != 0.0)) return set_error(PPGPU_ERR_ARG, "interp_grid: singular input cell");
+    double inv[9] = {A / det, -(m[1] * m[8] - m[2] * m[7]) / det, (m[1] * m[5] - m[2] * m[4]) / det,
+                     B / det, (m[0] * m[8] - m[2] * m[6]) / det, -(m[0] * m[5] - m[2] * m[3]) / det,
+                     C / det, -(m[0] * m[7] - m[1] * m[6]) / det, (m[0] * m[4] - m[1] * m[3]) / det};
+    const double T[9] = {inv[0], inv[3], inv[6], inv[1], inv[4], inv[7], inv[2], inv[5], inv[8]};
+    const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, Z[3] = {0, 0, 0};
+    const double *R = rot ? rot : I, *rc = rot_center ? rot_center : Z;
+    InterpPrm P;
+    P.nin = make_int3(nin[0], nin[1], nin[2]);
+    P.nout = make_int3(nout[0], nout[1], nout[2]);
+    P.TA = f3(T);
+    P.TB = f3(T + 3);
+    P.TC = f3(T + 6);
+    P.oin = f3(origin_in);
+    P.sA = f3(step_out);
+    P.sB = f3(step_out + 3);
+    P.sC = f3(step_out + 6);
+    P.oout = f3(origin_out);
+    P.rA = f3(R);
+    P.rB = f3(R + 3);
+    P.rC = f3(R + 6);
+    P.rc = f3(rc);
+    const long long n = (long long)nout[0] * nout[1] * nout[2];
+    interp_at_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(in, out, P, n);
+    PPGPU_CHECK_LAUNCH("interp_at_kernel");
+    return set_ok();
+}
+
+/* grad (ppafm/ocl/cl/FF.cl:920-961, DataGrid.grad, ppafm/ocl/field.py:454-513) in C order:
+ * FE[n0][n1][n2] float4 = scale[0..3] * (dE/dx, dE/dy, dE/dz, E), periodic centred differences
+ * with the grid steps step[3]; accumulate adds to FE. */
+extern "C" int ppgpu_grad_fd(const float *E, const int *n, const double *step, const double *scale, float *FE,
+                             int accumulate, void *stream) {
+    if (!E || !n || !step || !scale || !FE) return set_error(PPGPU_ERR_ARG, "grad_fd: null argument");
+    for (int k = 0; k < 3; k++)
+        if (n[k] <= 0) return set_error(PPGPU_ERR_ARG, "grad_fd: sizes must be positive");
+    const long long npts = (long long)n[0] * n[1] * n[2];
+    grad_fd_kernel<<<stream_blocks(npts), GRID_THREADS, 0, (cudaStream_t)stream>>>(
+        E, reinterpret_cast<float4 *>(FE), make_int3(n[0], n[1], n[2]), f3(step),
+        make_float4((float)scale[0], (float)scale[1], (float)scale[2], (float)scale[3]), accumulate, npts);
+    PPGPU_CHECK_LAUNCH("grad_fd_kernel");
     return set_ok();
 }

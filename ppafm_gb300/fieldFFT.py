@@ -90,6 +90,12 @@ class FFTGrid:
         check(lib().ppgpu_fft_poisson(self.handle, tptr(rho_charge.contiguous()), dptr(_lvec4(lvec)), tptr(out), stream_handle(stream)))
         return out
 
+    def correlate(self, V, rho, scale=1.0, out=None, stream=None):
+        """IFFT(conj(FFT(rho)) FFT(V)) * scale / N (the AFMulator's FFT cross-correlation)."""
+        out = self.empty() if out is None else out
+        check(lib().ppgpu_fft_correlate(self.handle, tptr(V.contiguous()), tptr(rho.contiguous()), float(scale), tptr(out), stream_handle(stream)))
+        return out
+
     def gaussians(self, lvec, atoms, out=None, accumulate=False, stream=None):
         """Sum of normalised Gaussians; atoms [n,5] = (x, y, z relative to the origin, sigma, weight)."""
         out = self.empty() if out is None else out

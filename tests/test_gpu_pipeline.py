@@ -82,4 +82,53 @@ def test_afmulator_vs_oracle(gpulib, oracle):
     X2 = afm(xyzs, Zs, qs, sample_lvec=lvec_sample)
     assert np.array_equal(X, X2)
     with pytest.raises(NotImplementedError):
-        AFMulator(rho={"s": 1.0})
+        AFMulator(rho_delta={"s": 1.0})  # FDBM
+
+
+def _hartree_case(oracle):
+    rng = np.random.default_rng(9)
+    na = 16
+    xyzs = np.column_stack([rng.uniform(5, 11, na), rng.uniform(5, 11, na), rng.uniform(-0.3, 0.3, na)])
+    Zs = rng.choice([1, 6, 7, 8], size=na)
+    q = rng.uniform(-0.4, 0.4, na)
+    q -= q.mean()
+    # Hartree potential of Gaussian charges on a 16 x 16 x 20 A cell, 48 x 48 x 60 points
+    lvp = np.array([[0.0, 0, -10.0], [16.0, 0, 0], [0, 16.0, 0], [0, 0, 20.0]])
+    n = (48, 48, 60)
+    atoms = np.column_stack([xyzs - lvp[0], np.full(na, 0.7), q])
+    rho = oracle.gaussian_density(n, lvp, atoms)
+    pot = oracle.poisson_hartree(rho, lvp).astype(np.float32)
+    return xyzs, Zs, pot, lvp
+
+
+@pytest.mark.parametrize("rotate", [False, True])
+def test_afmulator_hartree_vs_oracle(gpulib, oracle, rotate):
+    """The Hartree route (potential interpolated onto the force-field grid, FFT
+    cross-correlation with the dz2 tip density, centred-difference gradient, + Lennard-Jones)
+    against its float64-FFT restatement: force field and Δf images."""
+    from ppafm_gb300 import species
+    from ppafm_gb300.AFMulator import AFMulator, HartreePotential
+
+    xyzs, Zs, pot, lvp = _hartree_case(oracle)
+    kw = dict(pixPerAngstrome=10, scan_dim=(32, 28, 24), scan_window=((4.0, 4.0, 7.0), (12.0, 11.0, 9.4)), df_steps=8, npbc=(1, 1, 0))
+    rot = np.eye(3)
+    if rotate:
+        c, s_ = np.cos(0.3), np.sin(0.3)
+        rot = np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1.0]])
+    afm = AFMulator(rho={"dz2": -0.1}, sigma=0.71, **kw)
+    X = afm.eval(xyzs, Zs, HartreePotential(pot, lvp), rot=rot)
+    FE = afm.downloadFF()
+    T = species.loadSpecies()
+    FFp = np.array([(r[0], r[1], r[2]) for r in T])
+    ora = oracle.AFMulator(FFp, **kw)
+    Xo, aux = ora.eval(xyzs, Zs, None, pot=(pot, lvp), rho={"dz2": -0.1}, sigma=0.71, rot=rot, return_all=True)
+    FEo = aux["FE"].transpose(2, 1, 0, 3)
+    assert FE.shape == FEo.shape
+    scale = np.abs(FEo[..., :3].astype(np.float64)).max()
+    # the clamp-free LJ core makes the largest forces; compare where |F| is in the imaging range
+    m = np.linalg.norm(FEo[..., :3].astype(np.float64), axis=-1) < 10.0
+    assert np.abs(FE[..., :3] - FEo[..., :3])[m].max() <= 1e-4 * min(scale, 10.0) + 1e-5
+    d = np.abs(X - Xo)
+    assert (d > 0.1).mean() < 0.01 and np.median(d) < 1e-2
+    with pytest.raises(NotImplementedError):
+        AFMulator(**kw).eval(xyzs, Zs, HartreePotential(pot, lvp))  # no tip density
