@@ -202,7 +202,8 @@ int ppgpu_fft_poisson(void *handle, const float *rho_charge, const double *lvec,
 
 /* AFMulator Hartree route, cross-correlation (FFTCrossCorrelation.correlate,
  * ppafm/ocl/field.py:800-840): E = IFFT(conj(FFT(rho)) FFT(V)) * scale / N on the plan's grid
- * (scale: the tip density's voxel volume in the reference). */
+ * (scale: the tip density's voxel volume in the reference).  The plan keeps the spectrum of
+ * rho; rho NULL reuses it. */
 int ppgpu_fft_correlate(void *handle, const float *V, const float *rho, double scale, float *E, void *stream);
 
 /* Sum of normalised 3-D Gaussians on a periodic grid (minimum-image distances): atoms is a

@@ -109,6 +109,7 @@ class AFMulator:
         self._ff = None
         self.rho = None
         self._rho_dev = None
+        self._rho_spectrum_of = None
         self._fft = None
         self.setScanWindow(scan_window, scan_dim, df_steps)
         self.setLvec(lvec, pixPerAngstrome)
@@ -171,6 +172,7 @@ class AFMulator:
         n = tuple(int(x) for x in self.nDim)
         if self._fft is None or tuple(self._fft.n) != n:
             self._fft = FFTGrid(n)
+        self._rho_spectrum_of = None
         if isinstance(self.rho, dict):
             # MultipoleTipDensity (field.py:653-700): getProbeDensity on coordinates wrapped
             # around the grid origin
@@ -199,7 +201,9 @@ class AFMulator:
                                       dptr(np.ascontiguousarray(pot.step, dtype=np.float64)), tptr(pot_i), iptr(n), dptr(np.ascontiguousarray(lv[0], dtype=np.float64)),
                                       dptr(step_out), dptr(rot_ff), dptr(np.ascontiguousarray(rot_center, dtype=np.float64)), stream_handle(stream)))
         vox = abs(np.linalg.det(step_out))
-        E = self._fft.correlate(pot_i, rho, scale=vox, stream=stream)
+        fresh = self._rho_spectrum_of is not rho  # the tip's spectrum is transformed once
+        E = self._fft.correlate(pot_i, rho if fresh else None, scale=vox, stream=stream)
+        self._rho_spectrum_of = rho
         if self._ff is None:
             self._ff = DeviceFF(self.nDim, self.lvec)
         check(lib().ppgpu_grad_fd(tptr(E), iptr(n), dptr(np.ascontiguousarray(np.diag(step_out))), dptr(np.array([-1.0, -1.0, -1.0, 1.0])), tptr(self._ff.FE), 0, stream_handle(stream)))

@@ -37,6 +37,7 @@ struct FFTPlan {
     bool f64;         // transforms and spectra in float64 (cufft D2Z/Z2D)
     cufftHandle r2c = 0, c2r4 = 0, c2r1 = 0;
     void *Vk = nullptr, *Rk = nullptr, *S4 = nullptr;  // cufftComplex or cufftDoubleComplex
+    void *Tk = nullptr;  // spectrum of the last correlation kernel (ppgpu_fft_correlate)
     void *planar = nullptr;  // 4 real planes (float or double)
     double *sums = nullptr;  // reduction scratch
 };
@@ -423,6 +424,7 @@ extern "C" int ppgpu_fft_destroy(void *handle) {
     cudaFree(P->Vk);
     cudaFree(P->Rk);
     cudaFree(P->S4);
+    cudaFree(P->Tk);
     cudaFree(P->planar);
     cudaFree(P->sums);
     delete P;
@@ -592,28 +594,41 @@ extern "C" int ppgpu_gaussian_density(float *rho, const int *n, const double *lv
 
 /* E = IFFT(conj(FFT(rho)) FFT(V)) * scale / N: the circular cross-correlation of the AFMulator's
  * Hartree route (FFTCrossCorrelation.correlate, ppafm/ocl/field.py:800-840, with reikna's
- * normalised inverse).  V, rho, E: float32 grids of the plan's size. */
+ * normalised inverse).  V, rho, E: float32 grids of the plan's size.  The spectrum of rho is
+ * kept with the plan: rho NULL reuses the last one (like the reference, which transforms the
+ * tip density once, FFTCrossCorrelation._set_rho). */
 extern "C" int ppgpu_fft_correlate(void *handle, const float *V, const float *rho, double scale, float *E, void *stream) {
     FFTPlan *P = (FFTPlan *)handle;
-    if (!P || !V || !rho || !E) return set_error(PPGPU_ERR_ARG, "correlate: null argument");
+    if (!P || !V || !E) return set_error(PPGPU_ERR_ARG, "correlate: null argument");
+    if (!rho && !P->Tk) return set_error(PPGPU_ERR_STATE, "correlate: no kernel spectrum yet (pass rho)");
     cudaStream_t st = (cudaStream_t)stream;
     PPGPU_CUFFT(cufftSetStream(P->r2c, st), "cufftSetStream");
     PPGPU_CUFFT(cufftSetStream(P->c2r1, st), "cufftSetStream");
     double *stage = (double *)P->planar;
     int rc;
+    if (rho) {
+        if (!P->Tk) {
+            const size_t cs = P->f64 ? sizeof(cufftDoubleComplex) : sizeof(cufftComplex);
+            cudaError_t e = cudaMalloc(&P->Tk, P->Nh * cs);
+            if (e != cudaSuccess) {
+                P->Tk = nullptr;
+                return cuda_fail(e, "correlation spectrum");
+            }
+        }
+        if ((rc = forward(P, rho, P->Tk, stage, st, "forward rho")) != PPGPU_OK) return rc;
+    }
     if ((rc = forward(P, V, P->Vk, stage, st, "forward V")) != PPGPU_OK) return rc;
-    if ((rc = forward(P, rho, P->Rk, stage, st, "forward rho")) != PPGPU_OK) return rc;
     const double s = scale / (double)P->N;
     if (P->f64) {
         corr_mul_kernel<cufftDoubleComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>(
-            (const cufftDoubleComplex *)P->Vk, (const cufftDoubleComplex *)P->Rk, (cufftDoubleComplex *)P->S4, P->Nh, s);
+            (const cufftDoubleComplex *)P->Vk, (const cufftDoubleComplex *)P->Tk, (cufftDoubleComplex *)P->S4, P->Nh, s);
         PPGPU_CHECK_LAUNCH("corr_mul_kernel");
         PPGPU_CUFFT(cufftExecZ2D(P->c2r1, (cufftDoubleComplex *)P->S4, stage), "inverse E");
         f64_to_f32_kernel<<<blocks_for(P->N), FFT_THREADS, 0, st>>>(E, stage, P->N);
         PPGPU_CHECK_LAUNCH("f64_to_f32_kernel");
     } else {
         corr_mul_kernel<cufftComplex><<<spec_blocks(P), FFT_THREADS, 0, st>>>(
-            (const cufftComplex *)P->Vk, (const cufftComplex *)P->Rk, (cufftComplex *)P->S4, P->Nh, (float)s);
+            (const cufftComplex *)P->Vk, (const cufftComplex *)P->Tk, (cufftComplex *)P->S4, P->Nh, (float)s);
         PPGPU_CHECK_LAUNCH("corr_mul_kernel");
         PPGPU_CUFFT(cufftExecC2R(P->c2r1, (cufftComplex *)P->S4, E), "inverse E");
     }

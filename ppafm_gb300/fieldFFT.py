@@ -91,9 +91,10 @@ class FFTGrid:
         return out
 
     def correlate(self, V, rho, scale=1.0, out=None, stream=None):
-        """IFFT(conj(FFT(rho)) FFT(V)) * scale / N (the AFMulator's FFT cross-correlation)."""
+        """IFFT(conj(FFT(rho)) FFT(V)) * scale / N (the AFMulator's FFT cross-correlation);
+        rho None reuses the spectrum of the last rho."""
         out = self.empty() if out is None else out
-        check(lib().ppgpu_fft_correlate(self.handle, tptr(V.contiguous()), tptr(rho.contiguous()), float(scale), tptr(out), stream_handle(stream)))
+        check(lib().ppgpu_fft_correlate(self.handle, tptr(V.contiguous()), None if rho is None else tptr(rho.contiguous()), float(scale), tptr(out), stream_handle(stream)))
         return out
 
     def gaussians(self, lvec, atoms, out=None, accumulate=False, stream=None):

@@ -130,5 +130,7 @@ def test_afmulator_hartree_vs_oracle(gpulib, oracle, rotate):
     assert np.abs(FE[..., :3] - FEo[..., :3])[m].max() <= 1e-4 * min(scale, 10.0) + 1e-5
     d = np.abs(X - Xo)
     assert (d > 0.1).mean() < 0.01 and np.median(d) < 1e-2
+    # the tip's spectrum is transformed once and reused: the same image again
+    assert np.array_equal(afm.eval(xyzs, Zs, HartreePotential(pot, lvp), rot=rot), X)
     with pytest.raises(NotImplementedError):
         AFMulator(**kw).eval(xyzs, Zs, HartreePotential(pot, lvp))  # no tip density
