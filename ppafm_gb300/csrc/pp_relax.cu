@@ -94,7 +94,7 @@ constexpr int ZTAB = 4;
 // each trilinear gather (interp_force_df_group, bit-identical to one lane); lane 0 of the
 // group writes the outputs.  More lanes per stroke put more warps in flight when a scan has
 // few strokes, which is what bounds this kernel.
-template <bool SCAN, int TPS>
+template <bool SCAN, int TPS, bool SPL>
 __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, const StrokeIO S, const ScanIO C) {
     extern __shared__ dfl ztab[];
     const int s = (blockIdx.x * RELAX_THREADS + threadIdx.x) / TPS;
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(RELAX_THREADS) relax_kernel(const RelaxPrm P, 
             itcount = 0;
             continue;
         }
-        const float3 f = pp_force_df(P, F, d);
+        const float3 f = pp_force_df<SPL>(P, F, d);
         const float ff = relax_move_df(P, f, d, v, dt, acoef);
         mine += lead ? 1 : 0;
         if (ff < P.convF2f) {
@@ -425,16 +425,25 @@ static int g_relax_tps = 1;
 
 static int relax_tps(long long) { return g_relax_tps; }
 
+template <bool SCAN, bool SPL>
+static void launch_relax_t(int tps, unsigned nblk, size_t smem, cudaStream_t st, const RelaxPrm &P, const StrokeIO &S,
+                           const ScanIO &C) {
+    switch (tps) {
+    case 8: relax_kernel<SCAN, 8, SPL><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    case 4: relax_kernel<SCAN, 4, SPL><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    case 2: relax_kernel<SCAN, 2, SPL><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    default: relax_kernel<SCAN, 1, SPL><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
+    }
+}
+
 template <bool SCAN>
 static void launch_relax(int tps, long long nstroke, size_t smem, cudaStream_t st, const RelaxPrm &P, const StrokeIO &S,
                          const ScanIO &C) {
     const unsigned nblk = (unsigned)((nstroke * tps + RELAX_THREADS - 1) / RELAX_THREADS);
-    switch (tps) {
-    case 8: relax_kernel<SCAN, 8><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
-    case 4: relax_kernel<SCAN, 4><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
-    case 2: relax_kernel<SCAN, 2><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
-    default: relax_kernel<SCAN, 1><<<nblk, RELAX_THREADS, smem, st>>>(P, S, C); break;
-    }
+    if (P.spl.n > 0)
+        launch_relax_t<SCAN, true>(tps, nblk, smem, st, P, S, C);
+    else
+        launch_relax_t<SCAN, false>(tps, nblk, smem, st, P, S, C);
 }
 
 }  // namespace ppgpu

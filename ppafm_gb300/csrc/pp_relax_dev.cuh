@@ -207,6 +207,9 @@ __device__ __forceinline__ void grid_coord_df(const dfl *dic, bool diag, const d
 // ProbeParticle.cpp:282-294; forceRSpring, Forces.h:85-89) in double-float, returned as the
 // float32 residual: the radial spring is stiff, so l - l0 is a small difference of ~4 A
 // lengths, and the force is a small difference of the grid force and the springs.
+// SPL: the radial force comes from the tip spline (P.spl) instead of the harmonic spring
+// (a template parameter, so the harmonic kernels carry no spline code).
+template <bool SPL = false>
 __device__ __forceinline__ float3 pp_force_df(const RelaxPrm &P, const dfl F[3], const dfl d[3]) {
     const dfl l2 = df_add(df_add(df_sq(d[0]), df_sq(d[1])), df_sq(d[2]));
     // l = sqrt(l2) and 1/l: approximate float32 root, then one correction from the exact
@@ -217,7 +220,7 @@ __device__ __forceinline__ float3 pp_force_df(const RelaxPrm &P, const dfl F[3],
     const float res = __fadd_rn(__fsub_rn(__fsub_rn(l2.h, LL.h), LL.l), l2.l);
     const dfl l = fast_two_sum(L, __fmul_rn(res, __fmul_rn(0.5f, rs)));
     dfl s;
-    if (P.spl.n > 0) {
+    if constexpr (SPL) {
         s = df_div(spline_radial_df(P.spl, l), l);  // radial spline force / l
     } else {
         const dfl x = df_add(l, P.nl0);  // l - l0
