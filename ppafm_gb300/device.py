@@ -31,7 +31,7 @@ from ._lib import (
     tptr,
 )
 
-__all__ = ["pack_atoms", "DeviceFF", "relax_params", "relax_scan", "relax_strokes", "iter_counter"]
+__all__ = ["pack_atoms", "DeviceFF", "relax_params", "relax_scan", "relax_strokes", "iter_counter", "tip_spline", "autotune_relax_tps"]
 
 
 def _require_cuda():
@@ -153,6 +153,30 @@ def tip_spline(spline):
         yield
     finally:
         check(lib().ppgpu_set_tip_spline(0, None, None))
+
+
+def autotune_relax_tps(ff, prm, xs, ys, zs, candidates=(1, 2, 4, 8), reps=2, apply=True):
+    """Times relax_scan with each number of lanes per stroke on this scan and (apply) keeps the
+    fastest for the relaxations that follow.  Returns (best, {tps: ms})."""
+    times = {}
+    out = {}
+    try:
+        for t in candidates:
+            check(lib().ppgpu_set_relax_tps(int(t)))
+            relax_scan(ff, prm, xs, ys, zs, out=out)  # warm-up (and buffers)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                relax_scan(ff, prm, xs, ys, zs, out=out)
+            b.record()
+            b.synchronize()
+            times[int(t)] = a.elapsed_time(b) / reps
+    finally:
+        best = min(times, key=times.get) if times else 1
+        check(lib().ppgpu_set_relax_tps(best if apply else 0))
+    return best, times
 
 
 def relax_strokes(ff, prm, rTips, probeStart=1, relaxAlg=1, iters=False, counter=None, stream=None):

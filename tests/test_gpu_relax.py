@@ -303,3 +303,28 @@ def test_batch_refuses_tip_spline(gpulib):
         with pytest.raises(PPGPUError, match="spline"):
             BatchPipeline(systems, w, relax=relax)
     BatchPipeline(systems, w, relax=relax).close()  # cleared again
+
+
+def test_autotune_lanes_per_stroke(gpulib, oracle, golden):
+    """The lanes-per-stroke autotuner times every candidate, keeps the fastest, and the scan
+    it leaves selected gives the same result as one lane."""
+    import ctypes
+
+    from ppafm_gb300 import _lib, device
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = g["lvec"]
+    ff = device.DeviceFF(g["n"], lv).from_host_f64(FF.reshape(-1, 3))
+    L = _lib.lib()
+    try:
+        best, times = device.autotune_relax_tps(ff, prm, xT - lv[0, 0], yT - lv[0, 1], zT[::-1] - lv[0, 2], candidates=(1, 2, 4), reps=1)
+        assert best in (1, 2, 4) and set(times) == {1, 2, 4} and all(t > 0 for t in times.values())
+        t = ctypes.c_int()
+        _lib.check(L.ppgpu_get_relax_tps(1000, ctypes.byref(t)))
+        assert t.value == best
+        got = device.relax_scan(ff, prm, xT - lv[0, 0], yT - lv[0, 1], zT[::-1] - lv[0, 2])
+        _lib.check(L.ppgpu_set_relax_tps(1))
+        ref = device.relax_scan(ff, prm, xT - lv[0, 0], yT - lv[0, 1], zT[::-1] - lv[0, 2])
+        assert got["ppos"].equal(ref["ppos"]) and got["fzs"].equal(ref["fzs"])
+    finally:
+        _lib.check(L.ppgpu_set_relax_tps(0))
