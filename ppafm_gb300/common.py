@@ -130,22 +130,31 @@ def get_C612(i, j, FFparams):
 
 
 def getAtomsLJ(iZprobe, iZs, FFparams):
-    """(c6, c12) of every atom against the probe (common.py:860-868)."""
-    cLJs = np.zeros((len(iZs), 2))
-    for i, z in enumerate(iZs):
-        cLJs[i] = get_C612(iZprobe - 1, z - 1, FFparams)
-    return cLJs
+    """(c6, c12) of every atom against the probe (common.py:860-868); evaluated once per
+    element with the scalar expressions of get_C612, so every value is the reference's."""
+    iZs = np.asarray(iZs, dtype=np.int64).reshape(-1)
+    if iZs.size == 0:
+        return np.zeros((0, 2))
+    uniq, inv = np.unique(iZs, return_inverse=True)
+    table = np.array([get_C612(iZprobe - 1, int(z) - 1, FFparams) for z in uniq], dtype=np.float64)
+    return table[inv.reshape(-1)]
 
 
 def getAtomsREA(iZprobe, iZs, FFparams, alphaFac=-1.0):
-    """(R, E, alpha) pair parameters (common.py:880-892)."""
-    REAs = np.zeros((len(iZs), 4))
+    """(R, E, alpha) pair parameters (common.py:880-892), once per element."""
+    iZs = np.asarray(iZs, dtype=np.int64).reshape(-1)
+    REAs = np.zeros((iZs.size, 4))
+    if iZs.size == 0:
+        return REAs
     i = iZprobe - 1
-    for ii, z in enumerate(iZs):
-        j = z - 1
-        REAs[ii, 0] = FFparams[i][0] + FFparams[j][0]
-        REAs[ii, 1] = np.sqrt(FFparams[i][1] * FFparams[j][1])
-        REAs[ii, 2] = FFparams[j][2] * alphaFac
+    uniq, inv = np.unique(iZs, return_inverse=True)
+    table = np.zeros((len(uniq), 3))
+    for k, z in enumerate(uniq):
+        j = int(z) - 1
+        table[k, 0] = FFparams[i][0] + FFparams[j][0]
+        table[k, 1] = np.sqrt(FFparams[i][1] * FFparams[j][1])
+        table[k, 2] = FFparams[j][2] * alphaFac
+    REAs[:, :3] = table[inv.reshape(-1)]
     return REAs
 
 
