@@ -299,6 +299,19 @@ int ppgpu_interp_grid(const float *in, const int *nin, const double *origin_in, 
  * steps step[3]; accumulate != 0 adds to FE. */
 int ppgpu_grad_fd(const float *E, const int *n, const double *step, const double *scale, float *FE, int accumulate,
                   void *stream);
+/* ForceField.run_gradPotentialGrid (ppafm/ocl/field.py:1225-1317, kernel gradPotentialGrid,
+ * FF.cl:964-1008): field float4 [nout0][nout1][nout2] = (-dV/dx, -dV/dy, -dV/dz, V) at
+ * origin_out + i a + j b + k c (step_out rows), centred differences with steps h[3] of the
+ * periodic trilinear interpolation of pot[nin0][nin1][nin2] (origin_in, step_in rows). */
+int ppgpu_grad_potential_grid(const float *pot, const int *nin, const double *origin_in, const double *step_in,
+                              float *field, const int *nout, const double *origin_out, const double *step_out,
+                              const double *h, void *stream);
+/* The tip charges of ForceField.run_evalLJC_Hartree (ppafm/ocl/field.py:1168-1223, kernel
+ * evalLJC_Hartree, FF.cl:860-915): FE float4 [n0][n1][n2] (+)= sum_q Qs[q] * field(p + (0, 0,
+ * QZs[q])) at the grid points p = origin + i a + j b + k c (step rows), the float4 field on the
+ * same grid interpolated periodically; accumulate != 0 adds to FE (the Lennard-Jones part). */
+int ppgpu_tip_charges_field(const float *field, const int *n, const double *origin, const double *step,
+                            const double *Qs, const double *QZs, float *FE, int accumulate, void *stream);
 /* FE_out = a*FE_a + b*FE_b (float4 grids; E included). */
 int ppgpu_axpby_grid(float *FE_out, const float *FE_a, double a, const float *FE_b, double b, long long npts,
                      void *stream);

@@ -552,20 +552,77 @@ def interp_at(arr, lvec_in, nout, origin_out, step_out, rot=np.eye(3), rot_cente
     R = np.asarray(rot, np.float32)
     d = [pos[c] - rc[c] for c in range(3)]
     pos = [rc[c] + (R[c, 0] * d[0] + R[c, 1] * d[1] + R[c, 2] * d[2]) for c in range(3)]
-    oi = np.asarray(lvec_in[0], np.float32)
+    return _lerp_b(arr, lvec_in[0], T, pos)
+
+
+def _lerp_b(arr, origin, T, pos):
+    """linearInterpB / linearInterpB4 (ppafm/ocl/cl/FF.cl:34-113) at the float32 points
+    pos = [x, y, z] of a periodic grid arr [n0, n1, n2(, 4)] (C order) with lattice origin
+    origin and transform rows T (lattice coordinate = (pos - origin) . T rows)."""
+    f32 = np.float32
+    n = np.array(arr.shape[:3])
+    T = np.asarray(T, np.float32)
+    oi = np.asarray(origin, np.float32)
     cc = [pos[c] - oi[c] for c in range(3)]
     g = [cc[0] * T[a, 0] + cc[1] * T[a, 1] + cc[2] * T[a, 2] for a in range(3)]
     fl = [np.floor(x) for x in g]
     t = [np.minimum(g[a] - fl[a], f32(0.99999994)) for a in range(3)]
     i0 = [np.mod(fl[a].astype(np.int64), n[a]) for a in range(3)]
     i1 = [(i0[a] + 1) % n[a] for a in range(3)]
-    out = np.zeros(tuple(nout), np.float32)
+    out = np.zeros(pos[0].shape + arr.shape[3:], np.float32)
+    vec = arr.ndim == 4
     for bx in (0, 1):
         for by in (0, 1):
             for bz in (0, 1):
                 w = (t[0] if bx else 1 - t[0]) * (t[1] if by else 1 - t[1]) * (t[2] if bz else 1 - t[2])
-                out += w * arr[(i1 if bx else i0)[0], (i1 if by else i0)[1], (i1 if bz else i0)[2]]
+                v = arr[(i1 if bx else i0)[0], (i1 if by else i0)[1], (i1 if bz else i0)[2]]
+                out += (w[..., None] if vec else w) * v
     return out
+
+
+def hartree_ff_point_charges(nDim, lvec, pot_array, pot_lvec, xyzs, cLJs, Qs, QZs, h=0.05, nthreads=0):
+    """The Hartree route with a point-charge tip (ppafm/ocl/field.py:1168-1315, used by makeFF
+    at :1716-1720 when no tip density is set), float32 like the kernels: the electric field
+    on the force-field grid -- the potential's periodic centred differences where both grids
+    coincide (grad, FF.cl:920-961), else centred differences of the interpolated potential
+    with step h (gradPotentialGrid, FF.cl:964-1008) -- then Lennard-Jones plus, per tip
+    charge, Q times the field interpolated at the point shifted by QZ along z
+    (evalLJC_Hartree, FF.cl:860-915).  FE [nz, ny, nx, 4] x-fastest like afm_ff_qzs."""
+    nDim = np.asarray(nDim)
+    lvec = np.asarray(lvec, np.float64)
+    pot = np.asarray(pot_array, np.float32)
+    pot_lvec = np.asarray(pot_lvec, np.float64)
+    npot = np.array(pot.shape)
+    pstep = pot_lvec[1:] / npot[:, None]
+    step = lvec[1:4] / nDim[:, None]
+    f32 = np.float32
+    matching = (np.array_equal(npot, nDim) and (np.abs(pot_lvec[0] - lvec[0]) < 1e-3).all()
+                and (np.abs(np.diag(pstep) * npot - np.diag(lvec[1:4])) < 1e-3).all() and (pstep == np.diag(np.diag(pstep))).all())
+    i, j, k = np.meshgrid(*[np.arange(m, dtype=np.float32) for m in nDim], indexing="ij")
+    so = step.astype(np.float32)
+    o = lvec[0].astype(np.float32)
+    pos = [o[c] + i * so[0, c] + j * so[1, c] + k * so[2, c] for c in range(3)]
+    field = np.zeros(tuple(nDim) + (4,), np.float32)
+    if matching:
+        hs = np.diag(pstep).astype(np.float32)
+        for a in range(3):
+            field[..., a] = -(f32(0.5) * (np.roll(pot, -1, axis=a) - np.roll(pot, 1, axis=a)) / hs[a])
+        field[..., 3] = pot
+    else:
+        Tp = np.linalg.inv(pstep).T.astype(np.float32)
+        hh = f32(h)
+        field[..., 3] = _lerp_b(pot, pot_lvec[0], Tp, pos)
+        for a in range(3):
+            pm = [pos[c] - hh if c == a else pos[c] for c in range(3)]
+            pp = [pos[c] + hh if c == a else pos[c] for c in range(3)]
+            field[..., a] = f32(0.5) * (_lerp_b(pot, pot_lvec[0], Tp, pm) - _lerp_b(pot, pot_lvec[0], Tp, pp)) / hh
+    LJ = afm_ff_qzs(nDim, lvec, xyzs, np.zeros(len(xyzs)), cLJs, np.zeros(4), np.zeros(4), nthreads=nthreads)
+    FE = LJ.transpose(2, 1, 0, 3).copy()
+    T = np.linalg.inv(step).T.astype(np.float32)
+    for Q, QZ in zip(np.asarray(Qs, np.float32), np.asarray(QZs, np.float32)):
+        if Q != 0:
+            FE += Q * _lerp_b(field, lvec[0], T, [pos[0], pos[1], pos[2] + QZ])
+    return FE.transpose(2, 1, 0, 3).copy()
 
 
 def hartree_ff(nDim, lvec, pot_array, pot_lvec, rho_multipole, sigma, xyzs, cLJs, rot_ff, rot_center, nthreads=0):
@@ -670,7 +727,8 @@ class AFMulator:
 
     def eval(self, xyzs, Zs, qs, sample_lvec=None, nthreads=0, return_all=False, pot=None, rho=None, sigma=0.71, rot=np.eye(3)):
         """pot = (array [n0,n1,n2], lvec [4,3]) selects the Hartree route with the multipole tip
-        density rho (dict); otherwise point charges qs."""
+        density rho (dict), or with the point-charge tip when rho is None; otherwise point
+        charges qs."""
         if pot is not None:
             sample_lvec = np.asarray(pot[1])[1:] if sample_lvec is None else sample_lvec
             qs = np.zeros(len(Zs))
@@ -683,7 +741,11 @@ class AFMulator:
         if sum(npbc) > 0:
             Zs, xyzs, qs, cLJs = PBCAtoms3D_np(Zs, xyzs, qs, cLJs, sample_lvec, npbc=npbc)
         xyzs = np.dot(xyzs - rot_center, np.asarray(rot).T) + rot_center
-        if pot is not None:
+        if pot is not None and rho is None:
+            if not np.allclose(rot, np.eye(3)):
+                raise NotImplementedError("the point-charge tip Hartree route has no rotation")
+            FE = hartree_ff_point_charges(self.nDim, self.lvec, pot[0], pot[1], xyzs, cLJs, self.Qs, self.QZs, nthreads=nthreads)
+        elif pot is not None:
             FE = hartree_ff(self.nDim, self.lvec, pot[0], pot[1], rho, sigma, xyzs, cLJs, np.linalg.inv(rot), rot_center, nthreads=nthreads)
         else:
             FE = afm_ff_qzs(self.nDim, self.lvec, xyzs, qs, cLJs, self.Qs, self.QZs, nthreads=nthreads)

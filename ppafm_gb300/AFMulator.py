@@ -29,6 +29,7 @@ from ._lib import AFM_NPARAM, FF_QZS, check, dptr, iptr, lib, stream_handle, tpt
 from .device import DeviceFF, iter_counter, pack_atoms
 from .fieldFFT import FFTGrid
 
+FD_STEP = 0.05  # finite-difference step of the interpolated potential, A (field.py:27)
 VALID_SIZES = np.array([16, 32, 64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048])
 
 
@@ -109,7 +110,9 @@ class AFMulator:
         self._ff = None
         self.rho = None
         self._rho_dev = None
+        self._rho_cache = {}
         self._rho_spectrum_of = None
+        self._efield = None
         self._fft = None
         self.setScanWindow(scan_window, scan_dim, df_steps)
         self.setLvec(lvec, pixPerAngstrome)
@@ -123,9 +126,15 @@ class AFMulator:
         if pixPerAngstrome is not None:
             self.pixPerAngstrome = pixPerAngstrome
         self.lvec = np.asarray(lvec, dtype=np.float64) if lvec is not None else get_lvec(self.scan_window, tipR0=self.tipR0, pixPerAngstrome=self.pixPerAngstrome)
-        self.nDim = common.genFFSampling(self.lvec, pixPerAngstrome=self.pixPerAngstrome)
-        self._ff = None
-        self._rho_dev = None  # the tip density follows the force-field grid
+        nDim = common.genFFSampling(self.lvec, pixPerAngstrome=self.pixPerAngstrome)
+        if getattr(self, "nDim", None) is None or not np.array_equal(nDim, self.nDim) or not np.array_equal(self.lvec[1:], self._cell):
+            self._ff = None
+            self._rho_dev = None  # the tip density follows the force-field grid's shape
+        elif self._ff is not None:  # same grid moved: keep its buffers
+            self._ff.lvec = self.lvec.copy()
+            self._ff.origin = self.lvec[0].copy()
+        self.nDim = nDim
+        self._cell = self.lvec[1:].copy()
 
     def setScanWindow(self, scan_window=None, scan_dim=None, df_steps=None):
         """Scan geometry and the Δf weights (AFMulator.py:211-241)."""
@@ -172,7 +181,15 @@ class AFMulator:
         n = tuple(int(x) for x in self.nDim)
         if self._fft is None or tuple(self._fft.n) != n:
             self._fft = FFTGrid(n)
-        self._rho_spectrum_of = None
+            self._rho_cache = {}
+            self._rho_spectrum_of = None
+        # one device density per tip and grid shape (a generator alternates between tips)
+        tag = ("dict", tuple(sorted(self.rho.items()))) if isinstance(self.rho, dict) else ("grid", id(self.rho))
+        key = (tag, float(self.sigma), self.lvec[1:4].tobytes())
+        hit = self._rho_cache.get(key)
+        if hit is not None and (tag[0] == "dict" or hit[0] is self.rho):
+            self._rho_dev = hit[1]
+            return self._rho_dev
         if isinstance(self.rho, dict):
             # MultipoleTipDensity (field.py:653-700): getProbeDensity on coordinates wrapped
             # around the grid origin
@@ -181,6 +198,9 @@ class AFMulator:
             if tuple(self.rho.shape) != n or not np.allclose(self.rho.lvec[1:], self.lvec[1:]):
                 raise NotImplementedError("the tip density must be given on the force-field grid")
             self._rho_dev = self.rho.device()
+        if len(self._rho_cache) >= 8:
+            self._rho_cache.pop(next(iter(self._rho_cache)))
+        self._rho_cache[key] = (self.rho, self._rho_dev)
         return self._rho_dev
 
     def _hartree_ff(self, pot, atoms_rec, na, rot, rot_center, stream=None):
@@ -188,7 +208,9 @@ class AFMulator:
         interpolated onto it (rotated by the inverse of the atoms' rotation), cross-correlated
         with the tip density, F = -grad E by centred differences, then + Lennard-Jones."""
         if self.rho is None:
-            raise NotImplementedError("the Hartree route needs a tip density (AFMulator(rho=...)); the point-charge tip variant is not supported")
+            if not np.allclose(rot, np.eye(3)):
+                raise NotImplementedError("Force field calculation with rotation for Hartree potential with point charges tip density is not implemented.")
+            return self._hartree_ff_point_charges(pot, atoms_rec, na, stream=stream)
         lv = self.lvec
         if (np.abs(lv[1:4] - np.diag(np.diag(lv[1:4]))) > 0).any():
             raise NotImplementedError("Forcefield calculation via FFT for non-rectangular grids is not implemented.")
@@ -209,6 +231,36 @@ class AFMulator:
         check(lib().ppgpu_grad_fd(tptr(E), iptr(n), dptr(np.ascontiguousarray(np.diag(step_out))), dptr(np.array([-1.0, -1.0, -1.0, 1.0])), tptr(self._ff.FE), 0, stream_handle(stream)))
         zero4 = np.zeros(4)
         self._ff.compute(atoms_rec, na, 0, FF_QZS, Qs=zero4, QZs=zero4, with_E=True, accumulate=True, stream=stream)
+        return self._ff
+
+    def _hartree_ff_point_charges(self, pot, atoms_rec, na, stream=None):
+        """The Hartree route with the point-charge tip (field.py:1168-1317, makeFF :1716-1720):
+        the electric field on the force-field grid -- periodic centred differences of the
+        potential where the two grids coincide, else of the potential interpolated at +-h
+        (h = 0.05 A) -- then Lennard-Jones plus the tip charges Qs at heights QZs in that field."""
+        lv = self.lvec
+        n = np.array(self.nDim, dtype=np.int32)
+        step_out = np.ascontiguousarray(lv[1:4] / n[:, None], dtype=np.float64)
+        pstep = np.ascontiguousarray(pot.step, dtype=np.float64)
+        matching = (
+            tuple(pot.shape) == tuple(n)
+            and (np.abs(pot.origin - lv[0]) < 1e-3).all()
+            and (np.abs(np.diag(pstep) * np.array(pot.shape) - np.diag(lv[1:4])) < 1e-3).all()
+            and (pstep == np.diag(np.diag(pstep))).all()
+        )
+        if self._efield is None or tuple(self._efield.shape[:3]) != tuple(n):
+            self._efield = torch.empty(tuple(int(x) for x in n) + (4,), dtype=torch.float32, device="cuda")
+        if matching:
+            check(lib().ppgpu_grad_fd(tptr(pot.device()), iptr(n), dptr(np.ascontiguousarray(np.diag(pstep))), dptr(np.array([-1.0, -1.0, -1.0, 1.0])), tptr(self._efield), 0, stream_handle(stream)))
+        else:
+            check(lib().ppgpu_grad_potential_grid(tptr(pot.device()), iptr(np.array(pot.shape, dtype=np.int32)), dptr(np.ascontiguousarray(pot.origin, dtype=np.float64)), dptr(pstep),
+                                                  tptr(self._efield), iptr(n), dptr(np.ascontiguousarray(lv[0], dtype=np.float64)), dptr(step_out), dptr(np.full(3, FD_STEP)), stream_handle(stream)))
+        if self._ff is None:
+            self._ff = DeviceFF(self.nDim, self.lvec)
+        zero4 = np.zeros(4)
+        self._ff.compute(atoms_rec, na, 0, FF_QZS, Qs=zero4, QZs=zero4, with_E=True, stream=stream)
+        check(lib().ppgpu_tip_charges_field(tptr(self._efield), iptr(n), dptr(np.ascontiguousarray(lv[0], dtype=np.float64)), dptr(step_out),
+                                            dptr(self.Qs.astype(np.float64)), dptr(self.QZs.astype(np.float64)), tptr(self._ff.FE), 1, stream_handle(stream)))
         return self._ff
 
     # --------------------------------------------------------------- imaging

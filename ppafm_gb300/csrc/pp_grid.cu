@@ -112,17 +112,23 @@ __global__ void __launch_bounds__(256) ffma_kernel(float *sink, int iters) {
 
 // ------------------------------------------------ grids of the AFMulator's Hartree route
 
-// Periodic trilinear interpolation of a scalar grid at point pos (linearInterpB,
+// The voxel of a periodic grid that holds point pos, and the offsets in it (linearInterpB,
 // ppafm/ocl/cl/FF.cl:34-72): lattice coordinate (pos - origin) . T rows, float32.
-__device__ __forceinline__ float lin_interp_b(const float *in, int3 n, float3 o, float3 TA, float3 TB, float3 TC,
-                                              float3 pos) {
+struct LerpCell {
+    long long c[8];  // corners 000, 001, 010, 011, 100, 101, 110, 111 (i, j, k bits)
+    float dx, dy, dz;
+};
+
+__device__ __forceinline__ LerpCell lerp_cell(int3 n, float3 o, float3 TA, float3 TB, float3 TC, float3 pos) {
     const float3 c = make_float3(pos.x - o.x, pos.y - o.y, pos.z - o.z);
     const float3 g = make_float3(c.x * TA.x + c.y * TA.y + c.z * TA.z, c.x * TB.x + c.y * TB.y + c.z * TB.z,
                                  c.x * TC.x + c.y * TC.y + c.z * TC.z);
     const float fx = floorf(g.x), fy = floorf(g.y), fz = floorf(g.z);
+    LerpCell L;
     // fract(): x - floor(x), kept below 1
-    const float dx = fminf(g.x - fx, 0x1.fffffep-1f), dy = fminf(g.y - fy, 0x1.fffffep-1f),
-                dz = fminf(g.z - fz, 0x1.fffffep-1f);
+    L.dx = fminf(g.x - fx, 0x1.fffffep-1f);
+    L.dy = fminf(g.y - fy, 0x1.fffffep-1f);
+    L.dz = fminf(g.z - fz, 0x1.fffffep-1f);
     auto wrap = [](int i, int m) {
         const int r = i % m;
         return r >= 0 ? r : r + m;
@@ -130,11 +136,46 @@ __device__ __forceinline__ float lin_interp_b(const float *in, int3 n, float3 o,
     const int i0 = wrap((int)fx, n.x), j0 = wrap((int)fy, n.y), k0 = wrap((int)fz, n.z);
     const int i1 = (i0 + 1) % n.x, j1 = (j0 + 1) % n.y, k1 = (k0 + 1) % n.z;
     const long long nyz = (long long)n.y * n.z;
-    auto at = [&](int i, int j, int k) { return in[i * nyz + (long long)j * n.z + k]; };
-    return (1 - dx) * (1 - dy) * (1 - dz) * at(i0, j0, k0) + (1 - dx) * (1 - dy) * dz * at(i0, j0, k1) +
-           (1 - dx) * dy * (1 - dz) * at(i0, j1, k0) + (1 - dx) * dy * dz * at(i0, j1, k1) +
-           dx * (1 - dy) * (1 - dz) * at(i1, j0, k0) + dx * (1 - dy) * dz * at(i1, j0, k1) +
-           dx * dy * (1 - dz) * at(i1, j1, k0) + dx * dy * dz * at(i1, j1, k1);
+    const long long I[2] = {i0 * nyz, i1 * nyz}, J[2] = {(long long)j0 * n.z, (long long)j1 * n.z};
+    const int K[2] = {k0, k1};
+#pragma unroll
+    for (int b = 0; b < 8; b++) L.c[b] = I[b >> 2] + J[(b >> 1) & 1] + K[b & 1];
+    return L;
+}
+
+__device__ __forceinline__ float lerp_mix(const LerpCell &L, const float v[8]) {
+    const float dx = L.dx, dy = L.dy, dz = L.dz;
+    return (1 - dx) * (1 - dy) * (1 - dz) * v[0] + (1 - dx) * (1 - dy) * dz * v[1] + (1 - dx) * dy * (1 - dz) * v[2] +
+           (1 - dx) * dy * dz * v[3] + dx * (1 - dy) * (1 - dz) * v[4] + dx * (1 - dy) * dz * v[5] +
+           dx * dy * (1 - dz) * v[6] + dx * dy * dz * v[7];
+}
+
+// Periodic trilinear interpolation of a scalar grid (linearInterpB).
+__device__ __forceinline__ float lin_interp_b(const float *in, int3 n, float3 o, float3 TA, float3 TB, float3 TC,
+                                              float3 pos) {
+    const LerpCell L = lerp_cell(n, o, TA, TB, TC, pos);
+    float v[8];
+#pragma unroll
+    for (int b = 0; b < 8; b++) v[b] = in[L.c[b]];
+    return lerp_mix(L, v);
+}
+
+// The same for a float4 grid, component by component (linearInterpB4, FF.cl:74-113).
+__device__ __forceinline__ float4 lin_interp_b4(const float4 *in, int3 n, float3 o, float3 TA, float3 TB, float3 TC,
+                                                float3 pos) {
+    const LerpCell L = lerp_cell(n, o, TA, TB, TC, pos);
+    float4 q[8];
+#pragma unroll
+    for (int b = 0; b < 8; b++) q[b] = in[L.c[b]];
+    float vx[8], vy[8], vz[8], vw[8];
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        vx[b] = q[b].x;
+        vy[b] = q[b].y;
+        vz[b] = q[b].z;
+        vw[b] = q[b].w;
+    }
+    return make_float4(lerp_mix(L, vx), lerp_mix(L, vy), lerp_mix(L, vz), lerp_mix(L, vw));
 }
 
 struct InterpPrm {
@@ -181,6 +222,65 @@ __global__ void grad_fd_kernel(const float *__restrict__ E, float4 *__restrict__
             f = make_float4(f.x + o.x, f.y + o.y, f.z + o.z, f.w + o.w);
         }
         FE[ind] = f;
+    }
+}
+
+// gradPotentialGrid (ppafm/ocl/cl/FF.cl:964-1008): the electric field -grad V on a target
+// grid by centred differences (step h) of the potential interpolated at the six neighbours;
+// w = V at the point.  C order over the target grid.
+struct GradPotPrm {
+    int3 nin, nout;
+    float3 TA, TB, TC, oin;   // potential lattice transform rows and origin
+    float3 sA, sB, sC, oout;  // target grid steps and origin
+    float3 h;
+};
+
+__global__ void grad_pot_grid_kernel(const float *__restrict__ pot, float4 *__restrict__ field, GradPotPrm P,
+                                     long long nout) {
+    for (long long ind = blockIdx.x * (long long)blockDim.x + threadIdx.x; ind < nout;
+         ind += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(ind / ((long long)P.nout.y * P.nout.z));
+        const int j = (int)((ind / P.nout.z) % P.nout.y);
+        const int k = (int)(ind % P.nout.z);
+        const float3 p = make_float3(P.oout.x + i * P.sA.x + j * P.sB.x + k * P.sC.x, P.oout.y + i * P.sA.y + j * P.sB.y + k * P.sC.y,
+                                     P.oout.z + i * P.sA.z + j * P.sB.z + k * P.sC.z);
+        auto V = [&](float ax, float ay, float az) {
+            return lin_interp_b(pot, P.nin, P.oin, P.TA, P.TB, P.TC, make_float3(p.x + ax, p.y + ay, p.z + az));
+        };
+        const float v0 = V(0.f, 0.f, 0.f);
+        const float vip = V(-P.h.x, 0.f, 0.f), vjp = V(0.f, -P.h.y, 0.f), vkp = V(0.f, 0.f, -P.h.z);
+        const float vin = V(P.h.x, 0.f, 0.f), vjn = V(0.f, P.h.y, 0.f), vkn = V(0.f, 0.f, P.h.z);
+        field[ind] = make_float4(0.5f * (vip - vin) / P.h.x, 0.5f * (vjp - vjn) / P.h.y, 0.5f * (vkp - vkn) / P.h.z, v0);
+    }
+}
+
+// The tip charges' part of evalLJC_Hartree (ppafm/ocl/cl/FF.cl:860-915): at every grid point,
+// FE += sum_q Q_q * field(point + (0, 0, QZ_q)), the field (float4, C order, on the same
+// grid) interpolated periodically.  Charges of zero add nothing and are skipped.
+struct TipQPrm {
+    int3 n;
+    float3 TA, TB, TC, o;  // grid lattice transform rows and origin
+    float3 sA, sB, sC;     // grid steps
+    float Q[4], QZ[4];
+};
+
+__global__ void tip_charges_kernel(const float4 *__restrict__ field, float4 *__restrict__ FE, TipQPrm P, int accumulate,
+                                   long long npts) {
+    for (long long ind = blockIdx.x * (long long)blockDim.x + threadIdx.x; ind < npts;
+         ind += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(ind / ((long long)P.n.y * P.n.z));
+        const int j = (int)((ind / P.n.z) % P.n.y);
+        const int k = (int)(ind % P.n.z);
+        const float3 p = make_float3(P.o.x + P.sA.x * i + P.sB.x * j + P.sC.x * k, P.o.y + P.sA.y * i + P.sB.y * j + P.sC.y * k,
+                                     P.o.z + P.sA.z * i + P.sB.z * j + P.sC.z * k);
+        float4 fe = accumulate ? FE[ind] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (P.Q[q] == 0.f) continue;
+            const float4 e = lin_interp_b4(field, P.n, P.o, P.TA, P.TB, P.TC, make_float3(p.x, p.y, p.z + P.QZ[q]));
+            fe = make_float4(fe.x + P.Q[q] * e.x, fe.y + P.Q[q] * e.y, fe.z + P.Q[q] * e.z, fe.w + P.Q[q] * e.w);
+        }
+        FE[ind] = fe;
     }
 }
 
@@ -253,6 +353,19 @@ extern "C" int ppgpu_ffma_peak(float *scratch, int iters, long long *fma_count, 
 
 static float3 f3(const double *v) { return make_float3((float)v[0], (float)v[1], (float)v[2]); }
 
+// T = inv(step)^T as rows (lattice coordinate = coordinate . T rows); false when singular.
+static bool lattice_transform(const double *m, double T[9]) {
+    const double A = m[4] * m[8] - m[5] * m[7], B = -(m[3] * m[8] - m[5] * m[6]), C = m[3] * m[7] - m[4] * m[6];
+    const double det = m[0] * A + m[1] * B + m[2] * C;
+    if (!(det != 0.0)) return false;
+    const double inv[9] = {A / det, -(m[1] * m[8] - m[2] * m[7]) / det, (m[1] * m[5] - m[2] * m[4]) / det,
+                           B / det, (m[0] * m[8] - m[2] * m[6]) / det, -(m[0] * m[5] - m[2] * m[3]) / det,
+                           C / det, -(m[0] * m[7] - m[1] * m[6]) / det, (m[0] * m[4] - m[1] * m[3]) / det};
+    const double Tt[9] = {inv[0], inv[3], inv[6], inv[1], inv[4], inv[7], inv[2], inv[5], inv[8]};
+    memcpy(T, Tt, sizeof(Tt));
+    return true;
+}
+
 /* interp_at (ppafm/ocl/cl/FF.cl:1010-1046, DataGrid.interp_at, ppafm/ocl/field.py:515-572):
  * out[nout0][nout1][nout2] = periodic trilinear interpolation of in[nin0][nin1][nin2] (lattice
  * origin origin_in, steps step_in rows) at origin_out + i a + j b + k c (step_out rows), rotated
@@ -264,15 +377,8 @@ extern "C" int ppgpu_interp_grid(const float *in, const int *nin, const double *
         return set_error(PPGPU_ERR_ARG, "interp_grid: null argument");
     for (int k = 0; k < 3; k++)
         if (nin[k] <= 0 || nout[k] <= 0) return set_error(PPGPU_ERR_ARG, "interp_grid: sizes must be positive");
-    // T = inv(step_in)^T rows (g = coord . T rows)
-    const double *m = step_in;
-    const double A = m[4] * m[8] - m[5] * m[7], B = -(m[3] * m[8] - m[5] * m[6]), C = m[3] * m[7] - m[4] * m[6];
-    const double det = m[0] * A + m[1] * B + m[2] * C;
-    if (!(det != 0.0)) return set_error(PPGPU_ERR_ARG, "interp_grid: singular input cell");
-    double inv[9] = {A / det, -(m[1] * m[8] - m[2] * m[7]) / det, (m[1] * m[5] - m[2] * m[4]) / det,
-                     B / det, (m[0] * m[8] - m[2] * m[6]) / det, -(m[0] * m[5] - m[2] * m[3]) / det,
-                     C / det, -(m[0] * m[7] - m[1] * m[6]) / det, (m[0] * m[4] - m[1] * m[3]) / det};
-    const double T[9] = {inv[0], inv[3], inv[6], inv[1], inv[4], inv[7], inv[2], inv[5], inv[8]};
+    double T[9];
+    if (!lattice_transform(step_in, T)) return set_error(PPGPU_ERR_ARG, "interp_grid: singular input cell");
     const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, Z[3] = {0, 0, 0};
     const double *R = rot ? rot : I, *rc = rot_center ? rot_center : Z;
     InterpPrm P;
@@ -309,5 +415,71 @@ extern "C" int ppgpu_grad_fd(const float *E, const int *n, const double *step, c
         E, reinterpret_cast<float4 *>(FE), make_int3(n[0], n[1], n[2]), f3(step),
         make_float4((float)scale[0], (float)scale[1], (float)scale[2], (float)scale[3]), accumulate, npts);
     PPGPU_CHECK_LAUNCH("grad_fd_kernel");
+    return set_ok();
+}
+
+/* gradPotentialGrid (ppafm/ocl/cl/FF.cl:964-1008, ppafm/ocl/field.py:1225-1317): field
+ * [nout0][nout1][nout2] float4 = (-dV/dx, -dV/dy, -dV/dz, V) at origin_out + i a + j b + k c
+ * (step_out rows), centred differences with steps h[3] of the periodic trilinear interpolation
+ * of pot[nin0][nin1][nin2] (origin origin_in, steps step_in rows).  float32 like the kernel. */
+extern "C" int ppgpu_grad_potential_grid(const float *pot, const int *nin, const double *origin_in, const double *step_in,
+                                         float *field, const int *nout, const double *origin_out,
+                                         const double *step_out, const double *h, void *stream) {
+    if (!pot || !nin || !origin_in || !step_in || !field || !nout || !origin_out || !step_out || !h)
+        return set_error(PPGPU_ERR_ARG, "grad_potential_grid: null argument");
+    for (int k = 0; k < 3; k++) {
+        if (nin[k] <= 0 || nout[k] <= 0) return set_error(PPGPU_ERR_ARG, "grad_potential_grid: sizes must be positive");
+        if (!(h[k] > 0.0)) return set_error(PPGPU_ERR_ARG, "grad_potential_grid: steps h must be positive");
+    }
+    double T[9];
+    if (!lattice_transform(step_in, T)) return set_error(PPGPU_ERR_ARG, "grad_potential_grid: singular potential cell");
+    GradPotPrm P;
+    P.nin = make_int3(nin[0], nin[1], nin[2]);
+    P.nout = make_int3(nout[0], nout[1], nout[2]);
+    P.TA = f3(T);
+    P.TB = f3(T + 3);
+    P.TC = f3(T + 6);
+    P.oin = f3(origin_in);
+    P.sA = f3(step_out);
+    P.sB = f3(step_out + 3);
+    P.sC = f3(step_out + 6);
+    P.oout = f3(origin_out);
+    P.h = f3(h);
+    const long long n = (long long)nout[0] * nout[1] * nout[2];
+    grad_pot_grid_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(pot, reinterpret_cast<float4 *>(field), P, n);
+    PPGPU_CHECK_LAUNCH("grad_pot_grid_kernel");
+    return set_ok();
+}
+
+/* The tip charges of evalLJC_Hartree (ppafm/ocl/cl/FF.cl:860-915, ppafm/ocl/field.py:1168-1223):
+ * FE[n0][n1][n2] float4 (+)= sum_q Qs[q] * field(p + (0, 0, QZs[q])) at every grid point
+ * p = origin + i a + j b + k c (step rows), field [n0][n1][n2] float4 on the same grid,
+ * interpolated periodically.  accumulate adds to FE (which then holds the Lennard-Jones part,
+ * the reference's order of summation). */
+extern "C" int ppgpu_tip_charges_field(const float *field, const int *n, const double *origin, const double *step,
+                                       const double *Qs, const double *QZs, float *FE, int accumulate, void *stream) {
+    if (!field || !n || !origin || !step || !Qs || !QZs || !FE) return set_error(PPGPU_ERR_ARG, "tip_charges_field: null argument");
+    for (int k = 0; k < 3; k++)
+        if (n[k] <= 0) return set_error(PPGPU_ERR_ARG, "tip_charges_field: sizes must be positive");
+    if (field == FE) return set_error(PPGPU_ERR_ARG, "tip_charges_field: field and FE must be different buffers");
+    double T[9];
+    if (!lattice_transform(step, T)) return set_error(PPGPU_ERR_ARG, "tip_charges_field: singular cell");
+    TipQPrm P;
+    P.n = make_int3(n[0], n[1], n[2]);
+    P.TA = f3(T);
+    P.TB = f3(T + 3);
+    P.TC = f3(T + 6);
+    P.o = f3(origin);
+    P.sA = f3(step);
+    P.sB = f3(step + 3);
+    P.sC = f3(step + 6);
+    for (int q = 0; q < 4; q++) {
+        P.Q[q] = (float)Qs[q];
+        P.QZ[q] = (float)QZs[q];
+    }
+    const long long npts = (long long)n[0] * n[1] * n[2];
+    tip_charges_kernel<<<stream_blocks(npts), GRID_THREADS, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(field), reinterpret_cast<float4 *>(FE), P, accumulate, npts);
+    PPGPU_CHECK_LAUNCH("tip_charges_kernel");
     return set_ok();
 }

@@ -23,6 +23,7 @@ import torch
 
 from .. import common as PPU
 from .. import io
+from ..AFMulator import HartreePotential
 
 
 class InverseAFMtrainer:
@@ -174,21 +175,26 @@ class GeneratorAFMtrainer:
     Xs [n_batch, n_tip, nx, ny, nz_out], Ys [n_batch, n_aux, nx, ny], mols the
     [n_atoms, 5] arrays of the rotated molecules, sws [n_batch, n_tip, 2, 3] the scan windows.
     Each sample dict holds the AFMulator.eval arguments (at least xyzs and Zs).  Simulation
-    types: ``'LJ'`` and ``'LJ+PC'`` (point-charge tip); the Hartree and FDBM types need tip
-    densities, which this library does not provide.  Images are queued on the GPU and copied
-    to the host once per batch, as in InverseAFMtrainer.  Aux maps are callables
-    ``aux_map(xyzqs, Zs, pot, rot) -> [nx, ny]``; one with a ``scan_window`` attribute follows
-    the scan window."""
+    types: ``'LJ'``, ``'LJ+PC'`` (point-charge tip) and ``'LJ+Hartree'`` (the sample's
+    ``qs`` is a HartreePotential; ``rhos`` one tip density per tip -- a multipole dict or a
+    TipDensity on the force-field grid -- or None for the point-charge tip Qs, QZs);
+    ``'FDBM'`` is not supported.  Images are queued on
+    the GPU and copied to the host once per batch, as in InverseAFMtrainer.  Aux maps are
+    callables ``aux_map(xyzqs, Zs, pot, rot) -> [nx, ny]`` (pot the HartreePotential or None);
+    one with a ``scan_window`` attribute follows the scan window."""
 
     def __init__(self, afmulator, aux_maps, sample_generator, sim_type="LJ", batch_size=30, distAbove=5.3, iZPPs=[8], Qs=None, QZs=None, rhos=None, rho_deltas=None, ignore_elements=[], density_cutoff=None):
         self.afmulator = afmulator
         self.aux_maps = aux_maps
         self.sample_generator = sample_generator
         self.sim_type = sim_type.lower()
-        if self.sim_type in ("lj+hartree", "fdbm") or rhos is not None or rho_deltas is not None:
-            raise NotImplementedError(f"simulation type {sim_type!r} needs tip densities, which this library does not provide")
-        if self.sim_type not in ("lj", "lj+pc"):
+        if self.sim_type == "fdbm" or rho_deltas is not None:
+            raise NotImplementedError("the FDBM simulation type is not supported")
+        if self.sim_type not in ("lj", "lj+pc", "lj+hartree"):
             raise ValueError(f"Unknown simulation type `{sim_type}`")
+        if rhos is not None and len(rhos) != len(iZPPs):
+            raise ValueError(f"The length of rhos ({len(rhos)}) does not match the length of iZPPs ({len(iZPPs)})")
+        self.rhos = list(rhos) if rhos is not None else [None] * len(iZPPs)
         self.batch_size = batch_size
         self.distAbove = distAbove
         self.distAboveActive = distAbove
@@ -236,16 +242,19 @@ class GeneratorAFMtrainer:
             rot = self.sample_dict["rot"]
             xyzs = self.sample_dict["xyzs"]
             Zs = self.sample_dict["Zs"]
-            qs = self.sample_dict["qs"]
+            pot = self.sample_dict["qs"] if isinstance(self.sample_dict["qs"], HartreePotential) else None
+            qs = np.zeros(len(Zs)) if pot is not None else self.sample_dict["qs"]
             xyz_center = xyzs.mean(axis=0)
             self.xyzs_rot = np.dot(xyzs - xyz_center, rot.T) + xyz_center
             mols.append(np.concatenate([self.xyzs_rot, qs[:, None], Zs[:, None]], axis=1))
             self.handle_positions()
             self.on_sample_start()
             sws_ = []
-            for i, (iZPP, Q, Qz) in enumerate(zip(self.iZPPs, self.Qs, self.QZs)):
+            for i, (iZPP, Q, Qz, rho) in enumerate(zip(self.iZPPs, self.Qs, self.QZs, self.rhos)):
                 afm.iZPP = iZPP
                 afm.setQs(Q, Qz)
+                if rho is not None:
+                    afm.setRho(rho, sigma=afm.sigma, B_pauli=afm.B_pauli)
                 self.sample_dict["REAs"] = PPU.getAtomsREA(afm.iZPP, self.sample_dict["Zs"], afm.typeParams, alphaFac=-1.0)
                 self.handle_distance()
                 afm.setScanWindow(self.scan_window, self.scan_dim, df_steps=self.df_steps)
@@ -256,7 +265,7 @@ class GeneratorAFMtrainer:
                 afm.evalAFM(out=Xd[s, i])
                 sws_.append(np.array(self.scan_window))
             xyzqs = np.concatenate([xyzs, qs[:, None]], axis=1)
-            Ys.append([aux_map(xyzqs, Zs, None, rot) for aux_map in self.aux_maps])
+            Ys.append([aux_map(xyzqs, Zs, pot, rot) for aux_map in self.aux_maps])
             sws.append(sws_)
         if len(mols) == 0:
             raise StopIteration
@@ -273,9 +282,13 @@ class GeneratorAFMtrainer:
             sample_dict["rho_sample"] = None
         elif ("qs" not in sample_dict) or (sample_dict["qs"] is None):
             raise ValueError("Sample dict does not contain qs, which is required for a simulation with electrostatics")
-        elif not isinstance(sample_dict["qs"], np.ndarray):
-            raise ValueError("qs in sample dict is not a numpy array, which is required for a LJ+PC simulation.")
+        elif self.sim_type == "lj+pc":
+            if not isinstance(sample_dict["qs"], np.ndarray):
+                raise ValueError("qs in sample dict is not a numpy array, which is required for a LJ+PC simulation.")
+            sample_dict["rho_sample"] = None
         else:
+            if not isinstance(sample_dict["qs"], HartreePotential):
+                raise ValueError("qs in sample dict is not a HartreePotential, which is required for a LJ+Hartree simulation.")
             sample_dict["rho_sample"] = None
         if "rot" not in sample_dict:
             sample_dict["rot"] = np.eye(3)

@@ -1,6 +1,7 @@
 """The ML generators on the GPU path: the reference's generator test (batch count and
-shapes, tests/test_generator.py of ppafm) and image-for-image equality with AFMulator.eval
-for both the deferred (one copy per batch) and the per-image host-copy mode."""
+shapes, tests/test_generator.py of ppafm), image-for-image equality with AFMulator.eval
+for both the deferred (one copy per batch) and the per-image host-copy mode, and the
+LJ+Hartree simulation type with one tip density per tip."""
 
 import numpy as np
 import pytest
@@ -47,7 +48,56 @@ def test_generator_afm_trainer_batches(gpulib):
     assert i_batch == 2
     assert aux.scan_window is not None
     with pytest.raises(NotImplementedError):
-        GeneratorAFMtrainer(afmulator, [], generator(), sim_type="LJ+Hartree")
+        GeneratorAFMtrainer(afmulator, [], generator(), sim_type="FDBM")
+
+
+def test_generator_hartree_matches_eval(gpulib, oracle):
+    """LJ+Hartree samples with two tip densities (cached per tip on the device, the spectrum
+    transformed again when the tip changes): every image equals AFMulator.eval with that tip
+    density and scan window; the aux maps get the potential."""
+    from ppafm_gb300.AFMulator import AFMulator, HartreePotential
+    from ppafm_gb300.ml.Generator import GeneratorAFMtrainer
+    from tests.test_gpu_pipeline import _hartree_case
+
+    xyzs, Zs, pot, lvp = _hartree_case(oracle)
+    HP = HartreePotential(pot, lvp)
+    rhos = [{"dz2": -0.1}, {"s": 0.05, "pz": 0.02}]
+    rng = np.random.default_rng(3)
+    seen, pots = [], []
+
+    def rotz(t):
+        c, s_ = np.cos(t), np.sin(t)
+        return np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1.0]])
+
+    def samples():
+        for _ in range(3):
+            yield {"xyzs": xyzs, "Zs": Zs, "qs": HP, "rot": rotz(rng.uniform(0, 0.5))}
+
+    class Recorder(GeneratorAFMtrainer):
+        def on_afm_start(self):
+            a = self.afmulator
+            seen.append((a.iZPP, a.scan_window, a.rho, self.sample_dict["rot"].copy()))
+
+    def aux(xyzqs, Zs_, pot_, rot):
+        pots.append(pot_)
+        return np.zeros((32, 28), dtype=np.float32)
+
+    kw = dict(pixPerAngstrome=10, scan_dim=(32, 28, 24), scan_window=((4.0, 4.0, 7.0), (12.0, 11.0, 9.4)), df_steps=8, npbc=(1, 1, 0))
+    tr = Recorder(AFMulator(**kw), [aux], samples(), sim_type="LJ+Hartree", batch_size=2, iZPPs=[8, 8], rhos=rhos)
+    batches = [b for b in tr]  # (list() would ask the generator for its length)
+    assert [b[0].shape for b in batches] == [(2, 2, 32, 28, 17), (1, 2, 32, 28, 17)]
+    assert all(p is HP for p in pots) and len(pots) == 3
+    assert all(np.array_equal(m[:, 3], np.zeros(len(Zs))) for b in batches for m in b[2])
+    images = [Xs[s, t] for Xs, _, _, _ in batches for s in range(Xs.shape[0]) for t in range(2)]
+    assert len(images) == len(seen) == 6
+    assert [r for _, _, r, _ in seen] == rhos * 3
+    for img, (iZPP, sw, rho, rot) in zip(images, seen):
+        ref = AFMulator(**{**kw, "scan_window": sw}, rho=rho)
+        ref.iZPP = iZPP
+        want = ref.eval(xyzs, Zs, HP, rot=rot)
+        assert np.array_equal(img, want)
+    with pytest.raises(ValueError):
+        next(iter(GeneratorAFMtrainer(AFMulator(**kw), [], iter([{"xyzs": xyzs, "Zs": Zs, "qs": np.zeros(len(Zs))}]), sim_type="LJ+Hartree", iZPPs=[8], rhos=rhos[:1])))
 
 
 def _write_molecules(tmp_path, n, rng):

@@ -85,16 +85,19 @@ def test_afmulator_vs_oracle(gpulib, oracle):
         AFMulator(rho_delta={"s": 1.0})  # FDBM
 
 
-def _hartree_case(oracle):
+def _hartree_case(oracle, grid=None):
+    """Atoms and the Hartree potential of their Gaussian charges, on a 16 x 16 x 20 A cell of
+    48 x 48 x 60 points or on grid = (shape, lvec)."""
     rng = np.random.default_rng(9)
     na = 16
     xyzs = np.column_stack([rng.uniform(5, 11, na), rng.uniform(5, 11, na), rng.uniform(-0.3, 0.3, na)])
     Zs = rng.choice([1, 6, 7, 8], size=na)
     q = rng.uniform(-0.4, 0.4, na)
     q -= q.mean()
-    # Hartree potential of Gaussian charges on a 16 x 16 x 20 A cell, 48 x 48 x 60 points
     lvp = np.array([[0.0, 0, -10.0], [16.0, 0, 0], [0, 16.0, 0], [0, 0, 20.0]])
     n = (48, 48, 60)
+    if grid is not None:
+        n, lvp = tuple(int(x) for x in grid[0]), np.array(grid[1], dtype=np.float64)
     atoms = np.column_stack([xyzs - lvp[0], np.full(na, 0.7), q])
     rho = oracle.gaussian_density(n, lvp, atoms)
     pot = oracle.poisson_hartree(rho, lvp).astype(np.float32)
@@ -132,5 +135,37 @@ def test_afmulator_hartree_vs_oracle(gpulib, oracle, rotate):
     assert (d > 0.1).mean() < 0.01 and np.median(d) < 1e-2
     # the tip's spectrum is transformed once and reused: the same image again
     assert np.array_equal(afm.eval(xyzs, Zs, HartreePotential(pot, lvp), rot=rot), X)
-    with pytest.raises(NotImplementedError):
-        AFMulator(**kw).eval(xyzs, Zs, HartreePotential(pot, lvp))  # no tip density
+    if rotate:
+        with pytest.raises(NotImplementedError):
+            AFMulator(**kw).eval(xyzs, Zs, HartreePotential(pot, lvp), rot=rot)  # point-charge tip: no rotation
+
+
+@pytest.mark.parametrize("matching", [False, True])
+def test_afmulator_hartree_point_charge_tip_vs_oracle(gpulib, oracle, matching):
+    """The Hartree route with the point-charge tip (no tip density): the electric field from
+    the potential -- centred differences on the potential's own grid when it is the force
+    field's grid, else of the interpolated potential -- sampled at the tip charges' heights,
+    plus Lennard-Jones; force field and Δf images against the float32 restatement."""
+    from ppafm_gb300 import species
+    from ppafm_gb300.AFMulator import AFMulator, HartreePotential
+
+    kw = dict(pixPerAngstrome=10, scan_dim=(32, 28, 24), scan_window=((4.0, 4.0, 7.0), (12.0, 11.0, 9.4)), df_steps=8, npbc=(1, 1, 0))
+    afm = AFMulator(**kw)
+    # matching: the potential made on the force-field grid itself
+    xyzs, Zs, pot, lvp = _hartree_case(oracle, (afm.nDim, afm.lvec) if matching else None)
+    X = afm.eval(xyzs, Zs, HartreePotential(pot, lvp))
+    FE = afm.downloadFF()
+    T = species.loadSpecies()
+    FFp = np.array([(r[0], r[1], r[2]) for r in T])
+    Xo, aux = oracle.AFMulator(FFp, **kw).eval(xyzs, Zs, None, pot=(pot, lvp), rho=None, return_all=True)
+    FEo = aux["FE"].transpose(2, 1, 0, 3)
+    assert FE.shape == FEo.shape
+    scale = np.abs(FEo[..., :3].astype(np.float64)).max()
+    m = np.linalg.norm(FEo[..., :3].astype(np.float64), axis=-1) < 10.0
+    assert np.abs(FE[..., :3] - FEo[..., :3])[m].max() <= 1e-4 * min(scale, 10.0) + 1e-5
+    assert np.abs(FE[..., 3] - FEo[..., 3])[m].max() <= 1e-4 * np.abs(FEo[..., 3][m]).max() + 1e-5
+    d = np.abs(X - Xo)
+    assert (d > 0.1).mean() < 0.01 and np.median(d) < 1e-2
+    # the tip charges matter: without them the image differs
+    afm0 = AFMulator(**kw, Qs=[0, 0, 0, 0])
+    assert np.abs(afm0.eval(xyzs, Zs, HartreePotential(pot, lvp)) - X).max() > 0.1
