@@ -297,7 +297,7 @@ class AFMulator:
         if self._ff is None:
             self._ff = DeviceFF(self.nDim, self.lvec)
         R = atoms32[:, :3].astype(np.float64) - self.lvec[0]
-        rec, na, nch = pack_atoms(R, c32.astype(np.float64), atoms32[:, 3].astype(np.float64))
+        rec, na, nch = pack_atoms(R, c32.astype(np.float64), atoms32[:, 3].astype(np.float64), stream=stream)
         self._atoms = rec
         if pot is not None:
             return self._hartree_ff(pot, rec, na, np.asarray(rot, dtype=np.float64), np.asarray(rot_center, dtype=np.float64), stream=stream)

@@ -278,9 +278,9 @@ class Pipeline:
 
     def upload_atoms(self, stream=None):
         """Host -> device copy of the atom records (the inputs of one run)."""
-        self.atoms, _, self.ncharged = pack_atoms(self.Rs0, self.cLJs, self.kqq if self.Q != 0.0 else None)
+        self.atoms, _, self.ncharged = pack_atoms(self.Rs0, self.cLJs, self.kqq if self.Q != 0.0 else None, stream=stream)
         if self.tip != "s" and self.Q != 0.0:
-            self.atoms_el, _, self.nch_el = pack_atoms(self.Rs0, None, self.kqq)
+            self.atoms_el, _, self.nch_el = pack_atoms(self.Rs0, None, self.kqq, stream=stream)
 
     def build_ff(self, stream=None):
         if self.Q == 0.0:

@@ -97,6 +97,8 @@ class BatchPipeline:
             self._keep += [xs, ys, zs, rec]
             self.systems.append(dict(FE=FE, rec=rec, n=n, lvec=lvec, natoms=natoms, ncharged=nch, out=out, scan_shape=(nx, ny, nz), lvecScan=lvecScan))
         self._jobs = jobs
+        if torch.device(device).type == "cuda":
+            torch.cuda.current_stream().synchronize()  # the atom records are on the device before any stream runs
         self.handle = ctypes.c_void_p()
         tun = np.ascontiguousarray(self.tuning, dtype=np.int32)
         W = self.W if self.W is not None else np.zeros(1)

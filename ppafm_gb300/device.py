@@ -39,19 +39,29 @@ def _require_cuda():
         raise RuntimeError("ppafm_gb300 device path needs a CUDA device (no CPU fallback)")
 
 
-def pack_atoms(Rs, cLJs=None, kqq=None, device="cuda"):
+def pack_atoms(Rs, cLJs=None, kqq=None, device="cuda", stream=None):
     """Packs atoms into the 48-byte device records of include/ppgpu.h.
     Rs: [n,3] positions relative to the grid origin (float64); cLJs: [n,2] (c6, c12);
-    kqq: [n] charge coefficients.  Returns (records tensor [n,12] float32, n, ncharged)."""
+    kqq: [n] charge coefficients.  Returns (records tensor [n,12] float32, n, ncharged); the
+    copy to the device is queued on stream (default: the current stream)."""
     _require_cuda()
     Rs = np.ascontiguousarray(Rs, dtype=np.float64).reshape(-1, 3)
     n = len(Rs)
     c = None if cLJs is None else np.ascontiguousarray(cLJs, dtype=np.float64).reshape(-1, 2)
     q = None if kqq is None else np.ascontiguousarray(kqq, dtype=np.float64).reshape(-1)
-    rec = np.zeros((max(n, 1), ATOM_FLOATS), dtype=np.float32)
+    dev = torch.device(device)
+    # packed in pinned memory and copied without a synchronisation: the host can prepare the
+    # next system while the GPU works (the caching host allocator keeps the buffer until the
+    # copy has run)
+    rec_t = torch.zeros((max(n, 1), ATOM_FLOATS), dtype=torch.float32, pin_memory=dev.type == "cuda")
     nch = np.zeros(1, dtype=np.int32)
-    check(lib().ppgpu_pack_atoms(n, dptr(Rs), dptr(c), dptr(q), rec.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), iptr(nch)))
-    return torch.from_numpy(rec).to(device), n, int(nch[0])
+    check(lib().ppgpu_pack_atoms(n, dptr(Rs), dptr(c), dptr(q), ctypes.cast(rec_t.data_ptr(), ctypes.POINTER(ctypes.c_float)), iptr(nch)))
+    if dev.type != "cuda":
+        return rec_t, n, int(nch[0])
+    if stream is None:
+        return rec_t.to(dev, non_blocking=True), n, int(nch[0])
+    with torch.cuda.stream(stream):
+        return rec_t.to(dev, non_blocking=True), n, int(nch[0])
 
 
 def iter_counter(device="cuda"):
