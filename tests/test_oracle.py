@@ -246,3 +246,86 @@ def test_mlp_oracle_gradient_finite_differences():
         d[i] = 1e-6
         fd = (MO.loss_and_grad(P + d, X, T, False)[0] - MO.loss_and_grad(P - d, X, T, False)[0]) / 2e-6
         assert abs(fd - G[i]) <= 1e-5 * (abs(G[i]) + 1e-3)
+
+
+def test_interp_at_known_answers(oracle):
+    """interp_at restatement: node values at nodes, exact on a linear function inside the grid,
+    and the periodic wrap between the last and the first node."""
+    n = (8, 6, 10)
+    lv = np.array([[-1.0, 0.5, 2.0], [4.0, 0, 0], [0, 3.0, 0], [0, 0, 5.0]])
+    h = np.diag(lv[1:]) / n
+    g = np.stack(np.meshgrid(*[lv[0][k] + np.arange(n[k]) * h[k] for k in range(3)], indexing="ij"), axis=-1)
+    lin = (0.3 * g[..., 0] - 0.7 * g[..., 1] + 0.2 * g[..., 2]).astype(np.float32)
+    # at the nodes themselves
+    out = oracle.interp_at(lin, lv, n, lv[0], np.diag(h))
+    assert np.allclose(out, lin, atol=1e-5)
+    # half-way points of the interior: the mean of the neighbours, i.e. the linear function
+    o2 = lv[0] + 0.5 * h
+    out = oracle.interp_at(lin, lv, (7, 5, 9), o2, np.diag(h))
+    want = 0.3 * (g[:7, :5, :9, 0] + 0.5 * h[0]) - 0.7 * (g[:7, :5, :9, 1] + 0.5 * h[1]) + 0.2 * (g[:7, :5, :9, 2] + 0.5 * h[2])
+    assert np.allclose(out, want, atol=1e-5)
+    # periodic wrap: a quarter step before the origin along x mixes node n-1 (1/4) and node 0 (3/4)
+    o3 = lv[0] - np.array([0.25 * h[0], 0, 0])
+    out = oracle.interp_at(lin, lv, (1, n[1], n[2]), o3, np.diag(h))
+    assert np.allclose(out[0], 0.25 * lin[-1] + 0.75 * lin[0], atol=1e-5)
+
+
+def test_hartree_tip_density_plane_wave(oracle):
+    """Hartree route with a tip density: V = cos(G.r) on the force-field grid correlated with an
+    s-density of charge c gives E = c exp(-s^2 |G|^2 / 2) cos(G.r) and F = -grad E by centred
+    differences."""
+    n = (16, 16, 16)
+    L, h, s, c = 8.0, 0.5, 0.7, -0.3
+    lv = np.array([[0.0, 0, 0], [L, 0, 0], [0, L, 0], [0, 0, L]])
+    x = np.arange(n[0]) * h
+    G = 2 * np.pi / L
+    pot = np.broadcast_to(np.cos(G * x)[:, None, None], n).astype(np.float32)
+    FE = oracle.hartree_ff(n, lv, pot, lv, {"s": c}, s, np.zeros((0, 3)), np.zeros((0, 2)), np.eye(3), np.zeros(3))
+    FE = FE.transpose(2, 1, 0, 3)  # -> [nx, ny, nz, 4]
+    damp = c * np.exp(-(s * G) ** 2 / 2)
+    E = damp * np.cos(G * x)
+    Fx = damp * np.sin(G * x) * np.sin(G * h) / h
+    assert np.allclose(FE[:, 3, 5, 3], E, atol=1e-6)
+    assert np.allclose(FE[:, 3, 5, 0], Fx, atol=1e-6)
+    assert np.abs(FE[..., 1:3]).max() < 1e-6
+
+
+def test_hartree_point_charge_tip_known_answers(oracle):
+    """Hartree route with the point-charge tip (no atoms): the field of V on the force-field grid
+    sampled at the tip charges' heights (periodically on the force-field grid).  Same grid:
+    periodic centred differences of a plane-wave potential; other grid: the exact gradient of
+    a linear potential (interpolated at +-0.05 A inside the potential's grid)."""
+    n = (16, 12, 20)
+    lv = np.array([[0.0, 0, 0], [8.0, 0, 0], [0, 6.0, 0], [0, 0, 10.0]])
+    h = 0.5
+    kx, kz = 2 * np.pi / 8.0, 2 * 2 * np.pi / 10.0
+    x, z = np.arange(n[0]) * h, np.arange(n[2]) * h
+    V = (np.sin(kx * x)[:, None, None] + 0.5 * np.cos(kz * z)[None, None, :]) * np.ones(n)
+    Qs, QZs = [1.0, -2.0, 0, 0], [0.0, 1.0, 0, 0]
+    none = (np.zeros((0, 3)), np.zeros((0, 2)))
+    FE = oracle.hartree_ff_point_charges(n, lv, V.astype(np.float32), lv, *none, Qs, QZs).transpose(2, 1, 0, 3)
+
+    def field(zs):
+        ex = -np.cos(kx * x)[:, None, None] * np.sin(kx * h) / h * np.ones(n)
+        ez = 0.5 * np.sin(kz * zs)[None, None, :] * np.sin(kz * h) / h * np.ones(n)
+        w = np.sin(kx * x)[:, None, None] + 0.5 * np.cos(kz * zs)[None, None, :]
+        return ex, ez, w * np.ones(n)
+
+    e0, e1 = field(z), field(z + 1.0)  # QZ = 1 A = two steps (periodic)
+    assert np.allclose(FE[..., 0], e0[0] - 2 * e1[0], atol=1e-5)
+    assert np.abs(FE[..., 1]).max() < 1e-5
+    assert np.allclose(FE[..., 2], e0[1] - 2 * e1[1], atol=1e-5)
+    assert np.allclose(FE[..., 3], e0[2] - 2 * e1[2], atol=1e-5)
+    # a linear potential on a larger grid of its own: field (-a, -b, -c), so F = (1 - 2)(-a, -b, -c)
+    a, b, cz = 0.3, -0.2, 0.5
+    lvp = np.array([[-1.0, -1.0, -2.0], [12.0, 0, 0], [0, 10.0, 0], [0, 0, 16.0]])
+    npot = (24, 20, 32)
+    gp = [lvp[0][k] + np.arange(npot[k]) * 0.5 for k in range(3)]
+    Vp = (a * gp[0][:, None, None] + b * gp[1][None, :, None] + cz * gp[2][None, None, :]).astype(np.float32)
+    FE = oracle.hartree_ff_point_charges(n, lv, Vp, lvp, *none, Qs, QZs).transpose(2, 1, 0, 3)
+    assert np.allclose(FE[..., 0], a, atol=2e-3) and np.allclose(FE[..., 1], b, atol=2e-3) and np.allclose(FE[..., 2], cz, atol=2e-3)
+    # the tip charges sample the field on the force-field grid, periodic over its cell
+    def Vff(zs):
+        return a * x[:, None, None] + b * (np.arange(n[1]) * h)[None, :, None] + cz * zs[None, None, :]
+
+    assert np.allclose(FE[..., 3], Vff(z) - 2 * Vff((z + 1.0) % 10.0), atol=1e-4)
