@@ -129,12 +129,14 @@ __device__ __forceinline__ LerpCell lerp_cell(int3 n, float3 o, float3 TA, float
     L.dx = fminf(g.x - fx, 0x1.fffffep-1f);
     L.dy = fminf(g.y - fy, 0x1.fffffep-1f);
     L.dz = fminf(g.z - fz, 0x1.fffffep-1f);
+    // periodic index; the integer remainder only for points outside the home cell
     auto wrap = [](int i, int m) {
+        if ((unsigned)i < (unsigned)m) return i;
         const int r = i % m;
         return r >= 0 ? r : r + m;
     };
     const int i0 = wrap((int)fx, n.x), j0 = wrap((int)fy, n.y), k0 = wrap((int)fz, n.z);
-    const int i1 = (i0 + 1) % n.x, j1 = (j0 + 1) % n.y, k1 = (k0 + 1) % n.z;
+    const int i1 = i0 + 1 == n.x ? 0 : i0 + 1, j1 = j0 + 1 == n.y ? 0 : j0 + 1, k1 = k0 + 1 == n.z ? 0 : k0 + 1;
     const long long nyz = (long long)n.y * n.z;
     const long long I[2] = {i0 * nyz, i1 * nyz}, J[2] = {(long long)j0 * n.z, (long long)j1 * n.z};
     const int K[2] = {k0, k1};
