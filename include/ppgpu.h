@@ -312,6 +312,26 @@ int ppgpu_grad_potential_grid(const float *pot, const int *nin, const double *or
  * same grid interpolated periodically; accumulate != 0 adds to FE (the Lennard-Jones part). */
 int ppgpu_tip_charges_field(const float *field, const int *n, const double *origin, const double *step,
                             const double *Qs, const double *QZs, float *FE, int accumulate, void *stream);
+/* TipDensity.interp_at (ppafm/ocl/field.py:606-650, kernel interp_tip_at, FF.cl:1049-1093): the
+ * origin-centred tip density in[nin0][nin1][nin2] (grid steps step_in[3][3] rows, cell
+ * cell_in[3][3] rows) resampled onto out[nout0][nout1][nout2] (steps step_out rows); output
+ * indices past the middle are negative positions, points beyond half of the input cell are 0. */
+int ppgpu_interp_tip_grid(const float *in, const int *nin, const double *step_in, const double *cell_in, float *out,
+                          const int *nout, const double *step_out, void *stream);
+/* DataGrid.clamp (ppafm/ocl/field.py:288-340; clamp_hard / clamp_soft, FF.cl:1179-1210):
+ * out = in clipped to [minimum, maximum] (soft = 0) or sigmoid-blended into the bounds over
+ * width (soft = 1); in == out allowed. */
+int ppgpu_scalar_clamp(const float *in, float *out, long long n, double minimum, double maximum, int soft, double width,
+                       void *stream);
+/* DataGrid.add_mult (ppafm/ocl/field.py:342-376; addMult, FF.cl:1213-1223): out = a + scale*b. */
+int ppgpu_scalar_add_mult(const float *a, const float *b, float *out, long long n, double scale, void *stream);
+/* DataGrid.power_positive's normalisation sums (ppafm/ocl/field.py:431-452; normalizeSumReduce,
+ * FF.cl:1108-1150): device sums[0] = sum of all values, sums[1] = sum of the positive ones
+ * (float64). */
+int ppgpu_scalar_sums(const float *in, long long n, double *sums, void *stream);
+/* DataGrid.power_positive's power (ppafm/ocl/field.py:378-429; power, FF.cl:1095-1106):
+ * out = scale * max(0, in)^p; in == out allowed. */
+int ppgpu_scalar_power(const float *in, float *out, long long n, double p, double scale, void *stream);
 /* FE_out = a*FE_a + b*FE_b (float4 grids; E included). */
 int ppgpu_axpby_grid(float *FE_out, const float *FE_a, double a, const float *FE_b, double b, long long npts,
                      void *stream);

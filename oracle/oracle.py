@@ -555,6 +555,31 @@ def interp_at(arr, lvec_in, nout, origin_out, step_out, rot=np.eye(3), rot_cente
     return _lerp_b(arr, lvec_in[0], T, pos)
 
 
+def interp_tip_at(arr, lvec_in, shape_new, lvec_new):
+    """TipDensity.interp_at (interp_tip_at, ppafm/ocl/cl/FF.cl:1049-1093), float32 like the
+    kernel: output indices past the middle wrap to negative positions i*a' + j*b' + k*c'; zero
+    where a fractional coordinate (pos . rows of inv(input cell), the reference's form) exceeds
+    0.5 in magnitude, else the periodic interpolation of the input about origin 0."""
+    arr = np.asarray(arr, np.float32)
+    n = np.array(arr.shape)
+    lvec_in = np.asarray(lvec_in, np.float64)
+    lvec_new = np.asarray(lvec_new, np.float64)
+    T = np.linalg.inv(lvec_in[1:] / n[:, None]).T.astype(np.float32)
+    Linv = np.linalg.inv(lvec_in[1:]).astype(np.float32)
+    so = (lvec_new[1:] / np.array(shape_new)[:, None]).astype(np.float32)
+    idx = []
+    for a in range(3):
+        i = np.arange(shape_new[a])
+        i = np.where(i > shape_new[a] // 2, i - shape_new[a], i)
+        idx.append(i.astype(np.float32))
+    i, j, k = np.meshgrid(*idx, indexing="ij")
+    pos = [i * so[0, c] + j * so[1, c] + k * so[2, c] for c in range(3)]
+    frac = [Linv[a, 0] * pos[0] + Linv[a, 1] * pos[1] + Linv[a, 2] * pos[2] for a in range(3)]
+    out = _lerp_b(arr, np.zeros(3), T, pos)
+    out[(np.abs(frac[0]) > 0.5) | (np.abs(frac[1]) > 0.5) | (np.abs(frac[2]) > 0.5)] = 0.0
+    return out
+
+
 def _lerp_b(arr, origin, T, pos):
     """linearInterpB / linearInterpB4 (ppafm/ocl/cl/FF.cl:34-113) at the float32 points
     pos = [x, y, z] of a periodic grid arr [n0, n1, n2(, 4)] (C order) with lattice origin
@@ -627,9 +652,11 @@ def hartree_ff_point_charges(nDim, lvec, pot_array, pot_lvec, xyzs, cLJs, Qs, QZ
 
 def hartree_ff(nDim, lvec, pot_array, pot_lvec, rho_multipole, sigma, xyzs, cLJs, rot_ff, rot_center, nthreads=0):
     """calc_force_hartree (ppafm/ocl/field.py:1446-1504) restated: the potential interpolated
-    onto the force-field grid, cross-correlated with the multipole tip density by FFT (float64
-    numpy), F = -grad E by periodic centred differences, plus Lennard-Jones (evalLJ form,
-    R2SAFE 1e-6).  FE [nz, ny, nx, 4] x-fastest like afm_ff_qzs."""
+    onto the force-field grid, cross-correlated with the tip density by FFT (float64 numpy),
+    F = -grad E by periodic centred differences, plus Lennard-Jones (evalLJ form, R2SAFE
+    1e-6).  rho_multipole: a multipole dict (the density made on the force-field grid), or
+    (array, lvec) of a tip density on its own grid (resampled by interp_tip_at unless it is on
+    the force-field grid).  FE [nz, ny, nx, 4] x-fastest like afm_ff_qzs."""
     nDim = np.asarray(nDim)
     lvec = np.asarray(lvec, np.float64)
     step = lvec[1:4] / nDim[:, None]
@@ -641,7 +668,12 @@ def hartree_ff(nDim, lvec, pot_array, pot_lvec, rho_multipole, sigma, xyzs, cLJs
         c[c >= L[a] / 2] -= L[a]
         coords.append(c)
     X, Y, Z = np.meshgrid(*coords, indexing="ij")
-    rho = getProbeDensity(np.vstack([np.zeros(3), lvec[1:4]]), X, Y, Z, L / nDim, sigma=sigma, multipole_dict=rho_multipole)
+    if isinstance(rho_multipole, dict):
+        rho = getProbeDensity(np.vstack([np.zeros(3), lvec[1:4]]), X, Y, Z, L / nDim, sigma=sigma, multipole_dict=rho_multipole)
+    else:
+        arr, lv_t = np.asarray(rho_multipole[0], np.float32), np.asarray(rho_multipole[1], np.float64)
+        same = tuple(arr.shape) == tuple(int(x) for x in nDim) and np.allclose(lv_t[1:], lvec[1:4])
+        rho = arr if same else interp_tip_at(arr, lv_t, tuple(int(x) for x in nDim), lvec)
     rho = rho.astype(np.float32).astype(np.float64)
     E = np.real(np.fft.ifftn(np.conj(np.fft.fftn(rho)) * np.fft.fftn(pot_i))) * abs(np.linalg.det(step))
     hs = np.diag(step)

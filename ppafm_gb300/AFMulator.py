@@ -12,11 +12,14 @@ Force fields:
     ppafm/ocl/cl/FF.cl:366-423);
   * Hartree (qs a HartreePotential, a tip density set with ``rho``): the potential
     interpolated onto the force-field grid (interp_at), cross-correlated with the tip density
-    by FFT, differentiated by centred differences, plus Lennard-Jones (calc_force_hartree,
-    ppafm/ocl/field.py:1446-1504).
+    (resampled onto the force-field grid when given on another) by FFT, differentiated by
+    centred differences, plus Lennard-Jones (calc_force_hartree,
+    ppafm/ocl/field.py:1446-1504);
+  * Hartree without a tip density: the potential's electric field sampled at the tip point
+    charges, plus Lennard-Jones (run_gradPotentialGrid + run_evalLJC_Hartree,
+    field.py:1168-1317).
 
-Not provided: the Hartree route with a point-charge tip (no ``rho``), FDBM (``rho_delta``,
-``rho_sample``), tip densities on grids other than the force field's, plotting.
+Not provided: FDBM (``rho_delta``, ``rho_sample``), plotting.
 """
 
 import time
@@ -27,50 +30,11 @@ import torch
 from . import common
 from ._lib import AFM_NPARAM, FF_QZS, check, dptr, iptr, lib, stream_handle, tptr
 from .device import DeviceFF, iter_counter, pack_atoms
+from .field import DataGrid, ElectronDensity, HartreePotential, MultipoleTipDensity, TipDensity  # noqa: F401  (the reference exports them here too)
 from .fieldFFT import FFTGrid
 
 FD_STEP = 0.05  # finite-difference step of the interpolated potential, A (field.py:27)
 VALID_SIZES = np.array([16, 32, 64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048])
-
-
-class DataGrid:
-    """A scalar field on a periodic grid (ppafm/ocl/field.py:115-200): array [n0, n1, n2]
-    float32 (C order, the first axis along the first lattice vector) and lvec [4, 3] (origin,
-    then the lattice vectors)."""
-
-    def __init__(self, array, lvec):
-        self.array = np.ascontiguousarray(array, dtype=np.float32)
-        if self.array.ndim != 3:
-            raise ValueError(f"a scalar grid needs 3 dimensions, got {self.array.ndim}")
-        self.shape = tuple(self.array.shape)
-        self.lvec = np.array(lvec, dtype=np.float64)
-        assert self.lvec.shape == (4, 3), f"lvec should have shape (4, 3), but has shape {self.lvec.shape}"
-        self.origin = self.lvec[0]
-        self._dev = None
-
-    @property
-    def step(self):
-        """Single steps along each lattice vector (rows)."""
-        return np.stack([self.lvec[i + 1] / self.shape[i] for i in range(3)])
-
-    @property
-    def cell_vol(self):
-        a, b, c = self.step
-        return abs(np.cross(a, b).dot(c))
-
-    def device(self):
-        """The array in device memory (uploaded once)."""
-        if self._dev is None:
-            self._dev = torch.from_numpy(self.array).cuda()
-        return self._dev
-
-
-class HartreePotential(DataGrid):
-    """Sample Hartree potential in volts."""
-
-
-class TipDensity(DataGrid):
-    """Tip charge density in e/A^3, centred on the grid origin (wrapped)."""
 
 
 def get_lvec(scan_window, pad=(3.0, 3.0, 5.0), tipR0=(0.0, 0.0, 3.0), pixPerAngstrome=10):
@@ -164,7 +128,8 @@ class AFMulator:
     def setRho(self, rho=None, sigma=0.71, B_pauli=1.0):
         """Tip charge density for the Hartree route (AFMulator.py:243-288): a multipole dict
         (e.g. {"dz2": -0.1}) made on the force-field grid like MultipoleTipDensity, or a
-        TipDensity on that grid; None removes it."""
+        TipDensity (resampled about the origin onto the force-field grid when it is on
+        another); None removes it."""
         if rho is not None and not isinstance(rho, (dict, TipDensity)):
             raise ValueError(f"rho should be a dict or a TipDensity, but got `{type(rho)}`")
         if not np.allclose(B_pauli, 1.0):
@@ -194,10 +159,12 @@ class AFMulator:
             # MultipoleTipDensity (field.py:653-700): getProbeDensity on coordinates wrapped
             # around the grid origin
             self._rho_dev = self._fft.probe_density(np.vstack([np.zeros(3), self.lvec[1:4]]), self.sigma, self.rho)
-        else:
-            if tuple(self.rho.shape) != n or not np.allclose(self.rho.lvec[1:], self.lvec[1:]):
-                raise NotImplementedError("the tip density must be given on the force-field grid")
+        elif tuple(self.rho.shape) == n and np.allclose(self.rho.lvec[1:], self.lvec[1:]):
             self._rho_dev = self.rho.device()
+        else:
+            # another grid: resampled about the origin onto the force-field grid
+            # (prepareBuffers, field.py:957-962 -> TipDensity.interp_at)
+            self._rho_dev = self.rho.interp_at(self.lvec, n).device()
         if len(self._rho_cache) >= 8:
             self._rho_cache.pop(next(iter(self._rho_cache)))
         self._rho_cache[key] = (self.rho, self._rho_dev)

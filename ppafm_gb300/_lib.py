@@ -66,6 +66,11 @@ SIGNATURES = {
     "ppgpu_grad_fd": ([c_void_p, _ip, _dp, _dp, c_void_p, c_int, c_void_p], c_int),
     "ppgpu_grad_potential_grid": ([c_void_p, _ip, _dp, _dp, c_void_p, _ip, _dp, _dp, _dp, c_void_p], c_int),
     "ppgpu_tip_charges_field": ([c_void_p, _ip, _dp, _dp, _dp, _dp, c_void_p, c_int, c_void_p], c_int),
+    "ppgpu_interp_tip_grid": ([c_void_p, _ip, _dp, _dp, c_void_p, _ip, _dp, c_void_p], c_int),
+    "ppgpu_scalar_clamp": ([c_void_p, c_void_p, c_longlong, c_double, c_double, c_int, c_double, c_void_p], c_int),
+    "ppgpu_scalar_add_mult": ([c_void_p, c_void_p, c_void_p, c_longlong, c_double, c_void_p], c_int),
+    "ppgpu_scalar_sums": ([c_void_p, c_longlong, c_void_p, c_void_p], c_int),
+    "ppgpu_scalar_power": ([c_void_p, c_void_p, c_longlong, c_double, c_double, c_void_p], c_int),
     "ppgpu_axpby_grid": ([c_void_p, c_void_p, c_double, c_void_p, c_double, c_longlong, c_void_p], c_int),
     "ppgpu_grid_from_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_void_p], c_int),
     "ppgpu_grid_to_f64": ([c_void_p, c_void_p, c_void_p, c_longlong, c_int, c_void_p], c_int),

@@ -286,6 +286,99 @@ __global__ void tip_charges_kernel(const float4 *__restrict__ field, float4 *__r
     }
 }
 
+// interp_tip_at (ppafm/ocl/cl/FF.cl:1049-1093): a tip density centred on the grid origin
+// resampled onto another grid.  Output indices past the middle wrap to negative positions,
+// points beyond half of the input cell along any lattice vector are zero (the input's
+// fractional coordinate f = pos . Linv rows, Linv = inverse of the input cell, as the
+// reference forms it), the rest interpolated periodically about origin 0.
+struct TipInterpPrm {
+    int3 nin, nout;
+    float3 TA, TB, TC;  // input lattice transform rows
+    float3 LA, LB, LC;  // rows of the inverse input cell
+    float3 sA, sB, sC;  // output grid steps
+};
+
+__global__ void interp_tip_kernel(const float *__restrict__ in, float *__restrict__ out, TipInterpPrm P, long long nout) {
+    for (long long ind = blockIdx.x * (long long)blockDim.x + threadIdx.x; ind < nout;
+         ind += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(ind / ((long long)P.nout.y * P.nout.z));
+        int j = (int)((ind / P.nout.z) % P.nout.y);
+        int k = (int)(ind % P.nout.z);
+        if (i > P.nout.x / 2) i -= P.nout.x;
+        if (j > P.nout.y / 2) j -= P.nout.y;
+        if (k > P.nout.z / 2) k -= P.nout.z;
+        const float3 pos = make_float3(i * P.sA.x + j * P.sB.x + k * P.sC.x, i * P.sA.y + j * P.sB.y + k * P.sC.y,
+                                       i * P.sA.z + j * P.sB.z + k * P.sC.z);
+        const float fa = P.LA.x * pos.x + P.LA.y * pos.y + P.LA.z * pos.z;
+        const float fb = P.LB.x * pos.x + P.LB.y * pos.y + P.LB.z * pos.z;
+        const float fc = P.LC.x * pos.x + P.LC.y * pos.y + P.LC.z * pos.z;
+        if (fabsf(fa) > 0.5f || fabsf(fb) > 0.5f || fabsf(fc) > 0.5f)
+            out[ind] = 0.f;
+        else
+            out[ind] = lin_interp_b(in, P.nin, make_float3(0.f, 0.f, 0.f), P.TA, P.TB, P.TC, pos);
+    }
+}
+
+// Elementwise scalar-grid operations of DataGrid (ppafm/ocl/field.py:288-452; kernels
+// clamp_hard, clamp_soft, addMult, power, normalizeSumReduce of FF.cl:1095-1223).
+__global__ void scalar_clamp_kernel(const float *__restrict__ in, float *__restrict__ out, long long n, float lo, float hi,
+                                    int soft, float width) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float v = in[i];
+        if (!soft) {
+            v = fmaxf(lo, fminf(hi, v));
+        } else {
+            // sigmoid blend towards the bound over the width (clamp_soft)
+            if (hi < INFINITY) v = (v - hi) / (1.f + expf((v - hi) / width)) + hi;
+            if (lo > -INFINITY) v = (v - lo) / (1.f + expf((v - lo) / -width)) + lo;
+        }
+        out[i] = v;
+    }
+}
+
+__global__ void scalar_add_mult_kernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ out,
+                                       long long n, float s) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = a[i] + s * b[i];
+}
+
+// (sum of all values, sum of the positive ones) in float64: block partials, then one atomic
+// add per block.
+__global__ void scalar_sums_kernel(const float *__restrict__ in, long long n, double *sums) {
+    double t = 0.0, p = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float v = in[i];
+        t += v;
+        if (v > 0.f) p += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+        p += __shfl_xor_sync(0xffffffffu, p, o);
+    }
+    __shared__ double st[GRID_THREADS / 32], sp[GRID_THREADS / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        st[w] = t;
+        sp[w] = p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double T = 0.0, Pp = 0.0;
+        for (int k = 0; k < GRID_THREADS / 32; k++) {
+            T += st[k];
+            Pp += sp[k];
+        }
+        atomicAdd(sums, T);
+        atomicAdd(sums + 1, Pp);
+    }
+}
+
+__global__ void scalar_power_kernel(const float *__restrict__ in, float *__restrict__ out, long long n, float p, float scale) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = scale * powf(fmaxf(0.f, in[i]), p);
+}
+
 }  // namespace ppgpu
 
 using namespace ppgpu;
@@ -483,5 +576,82 @@ extern "C" int ppgpu_tip_charges_field(const float *field, const int *n, const d
     tip_charges_kernel<<<stream_blocks(npts), GRID_THREADS, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<const float4 *>(field), reinterpret_cast<float4 *>(FE), P, accumulate, npts);
     PPGPU_CHECK_LAUNCH("tip_charges_kernel");
+    return set_ok();
+}
+
+/* TipDensity.interp_at (ppafm/ocl/field.py:606-650, kernel interp_tip_at, FF.cl:1049-1093):
+ * the tip density in[nin0][nin1][nin2] (grid steps step_in rows, cell cell_in rows), centred
+ * on the origin, resampled onto out[nout0][nout1][nout2] with steps step_out rows; output
+ * indices past the middle are negative positions, points beyond half of the input cell are 0. */
+extern "C" int ppgpu_interp_tip_grid(const float *in, const int *nin, const double *step_in, const double *cell_in,
+                                     float *out, const int *nout, const double *step_out, void *stream) {
+    if (!in || !nin || !step_in || !cell_in || !out || !nout || !step_out)
+        return set_error(PPGPU_ERR_ARG, "interp_tip_grid: null argument");
+    for (int k = 0; k < 3; k++)
+        if (nin[k] <= 0 || nout[k] <= 0) return set_error(PPGPU_ERR_ARG, "interp_tip_grid: sizes must be positive");
+    double T[9], LT[9];
+    if (!lattice_transform(step_in, T) || !lattice_transform(cell_in, LT))
+        return set_error(PPGPU_ERR_ARG, "interp_tip_grid: singular input cell");
+    // lattice_transform gives inv(m)^T as rows; the reference takes the rows of inv(cell)
+    const double L[9] = {LT[0], LT[3], LT[6], LT[1], LT[4], LT[7], LT[2], LT[5], LT[8]};
+    TipInterpPrm P;
+    P.nin = make_int3(nin[0], nin[1], nin[2]);
+    P.nout = make_int3(nout[0], nout[1], nout[2]);
+    P.TA = f3(T);
+    P.TB = f3(T + 3);
+    P.TC = f3(T + 6);
+    P.LA = f3(L);
+    P.LB = f3(L + 3);
+    P.LC = f3(L + 6);
+    P.sA = f3(step_out);
+    P.sB = f3(step_out + 3);
+    P.sC = f3(step_out + 6);
+    const long long n = (long long)nout[0] * nout[1] * nout[2];
+    interp_tip_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(in, out, P, n);
+    PPGPU_CHECK_LAUNCH("interp_tip_kernel");
+    return set_ok();
+}
+
+/* DataGrid.clamp (ppafm/ocl/field.py:288-340; clamp_hard, clamp_soft, FF.cl:1179-1210):
+ * out[i] = in[i] clipped to [minimum, maximum] (soft = 0), or blended into the bounds by a
+ * sigmoid of the given width (soft = 1).  in == out is allowed. */
+extern "C" int ppgpu_scalar_clamp(const float *in, float *out, long long n, double minimum, double maximum, int soft,
+                                  double width, void *stream) {
+    if (!in || !out) return set_error(PPGPU_ERR_ARG, "scalar_clamp: null argument");
+    if (n <= 0) return set_ok();
+    scalar_clamp_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(in, out, n, (float)minimum, (float)maximum,
+                                                                                     soft, (float)width);
+    PPGPU_CHECK_LAUNCH("scalar_clamp_kernel");
+    return set_ok();
+}
+
+/* DataGrid.add_mult (ppafm/ocl/field.py:342-376; addMult, FF.cl:1213-1223): out = a + scale*b. */
+extern "C" int ppgpu_scalar_add_mult(const float *a, const float *b, float *out, long long n, double scale, void *stream) {
+    if (!a || !b || !out) return set_error(PPGPU_ERR_ARG, "scalar_add_mult: null argument");
+    if (n <= 0) return set_ok();
+    scalar_add_mult_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(a, b, out, n, (float)scale);
+    PPGPU_CHECK_LAUNCH("scalar_add_mult_kernel");
+    return set_ok();
+}
+
+/* The normalisation sums of DataGrid.power_positive (ppafm/ocl/field.py:431-452;
+ * normalizeSumReduce, FF.cl:1108-1150): sums[0] = sum of all values, sums[1] = sum of the
+ * positive ones, float64, into the device array sums[2] (cleared here). */
+extern "C" int ppgpu_scalar_sums(const float *in, long long n, double *sums, void *stream) {
+    if (!in || !sums) return set_error(PPGPU_ERR_ARG, "scalar_sums: null argument");
+    PPGPU_CUDA(cudaMemsetAsync(sums, 0, 2 * sizeof(double), (cudaStream_t)stream), "clear sums");
+    if (n <= 0) return set_ok();
+    scalar_sums_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(in, n, sums);
+    PPGPU_CHECK_LAUNCH("scalar_sums_kernel");
+    return set_ok();
+}
+
+/* DataGrid.power_positive's power (ppafm/ocl/field.py:378-429; power, FF.cl:1095-1106):
+ * out[i] = scale * max(0, in[i])^p.  in == out is allowed. */
+extern "C" int ppgpu_scalar_power(const float *in, float *out, long long n, double p, double scale, void *stream) {
+    if (!in || !out) return set_error(PPGPU_ERR_ARG, "scalar_power: null argument");
+    if (n <= 0) return set_ok();
+    scalar_power_kernel<<<stream_blocks(n), GRID_THREADS, 0, (cudaStream_t)stream>>>(in, out, n, (float)p, (float)scale);
+    PPGPU_CHECK_LAUNCH("scalar_power_kernel");
     return set_ok();
 }

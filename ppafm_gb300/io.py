@@ -140,6 +140,33 @@ def loadXSFData(fname, xyz_order=True):
     return F.copy(), lvec, nDim - 1, head
 
 
+def loadXSFGeom(fname):
+    """([Zs, x, y, z, q], grid size, lvec) of an XSF file's PRIMCOORD atoms (atomic numbers)
+    and datagrid header (io.py:229-267); ValueError without a PRIMCOORD block."""
+    e, x, y, z, q = [], [], [], [], []
+    with open(fname) as f:
+        for line in f:
+            if "PRIMCOORD" in line:
+                break
+        else:
+            raise ValueError(f"{fname}: no PRIMCOORD block")
+        n = int(f.readline().split()[0])
+        for _ in range(n):
+            ws = f.readline().split()
+            e.append(int(ws[0]))
+            x.append(float(ws[1]))
+            y.append(float(ws[2]))
+            z.append(float(ws[3]))
+            q.append(0)
+        for line in f:
+            if "BEGIN_DATAGRID_3D" in line or "DATAGRID_3D_DENSITY" in line:
+                break
+        ws = f.readline().split()
+        nDim = [int(ws[0]), int(ws[1]), int(ws[2])]
+        lvec = [[float(w) for w in f.readline().split()[:3]] for _ in range(4)]
+    return [e, x, y, z, q], (nDim[0] - 1, nDim[1] - 1, nDim[2] - 1), lvec
+
+
 def packVecGrid(Fx, Fy, Fz, FF=None):
     if FF is None:
         FF = np.zeros(np.shape(Fx) + (3,))

@@ -329,3 +329,27 @@ def test_hartree_point_charge_tip_known_answers(oracle):
         return a * x[:, None, None] + b * (np.arange(n[1]) * h)[None, :, None] + cz * zs[None, None, :]
 
     assert np.allclose(FE[..., 3], Vff(z) - 2 * Vff((z + 1.0) % 10.0), atol=1e-4)
+
+
+def _gaussian_on(shape, lvec):
+    """A unit-width Gaussian at the origin of a periodic grid (wrapped), the form of the
+    reference's tests/test_datagrid.py make_gaussian."""
+    xyz = np.stack(np.meshgrid(*[np.linspace(-0.5, 0.5, shape[i], endpoint=False) for i in range(3)], indexing="ij"), axis=-1)
+    xyz = xyz.dot(np.asarray(lvec, np.float64)[1:].T)
+    a = np.exp(-0.5 * (xyz**2).sum(axis=-1))
+    return np.roll(a, (-np.array(shape) / 2).astype(int), axis=(0, 1, 2))
+
+
+def test_interp_tip_at_gaussian(oracle):
+    """The tip-density resampling restatement against the analytic Gaussian on the new grid
+    (the reference's test_tip_interp at smaller sizes), and zero beyond half of the input cell."""
+    lv1 = np.array([[0.0, 0, 0], [10, 0, 0], [0, 10, 0], [0, 0, 10]])
+    lv2 = np.array([[0.0, 0, 0], [12, 0, 0], [0, 8, 0], [0, 0, 15]])
+    g1 = _gaussian_on((100, 100, 100), lv1).astype(np.float32)
+    out = oracle.interp_tip_at(g1, lv1, (72, 48, 90), lv2)
+    g2 = _gaussian_on((72, 48, 90), lv2)
+    assert np.allclose(out, g2, atol=3e-3, rtol=3e-3)
+    # beyond |x| > 5 A (half of the 10 A input cell) along x: zero; the 12 A grid has such points
+    x = np.arange(72)
+    x = np.where(x > 36, x - 72, x) * (12 / 72)
+    assert (out[np.abs(x) > 5.0 + 1e-6] == 0).all()
