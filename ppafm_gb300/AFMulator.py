@@ -334,13 +334,20 @@ class AFMulator:
         return X
 
     def eval(self, xyzs, Zs, qs, rho_sample=None, sample_lvec=None, rot=np.eye(3), rot_center=None, REAs=None, X=None, plot_to_dir=None):
-        """Prepare and evaluate the AFM image stack (AFMulator.py:142-173)."""
-        if plot_to_dir:
-            raise NotImplementedError("plotting is not part of this library")
+        """Prepare and evaluate the AFM image stack (AFMulator.py:142-173).  plot_to_dir: the
+        reference plots the images there; this library has no plotting and saves the stack as
+        ``df.npy`` in that directory instead (with a warning)."""
         t0 = time.perf_counter()
         self.prepareFF(xyzs, Zs, qs, rho_sample, sample_lvec, rot, rot_center, REAs)
         X = self.evalAFM(X)
         self.last_timing["eval"] = time.perf_counter() - t0
+        if plot_to_dir:
+            import os
+            import warnings
+
+            os.makedirs(plot_to_dir, exist_ok=True)
+            np.save(os.path.join(plot_to_dir, "df.npy"), X)
+            warnings.warn(f"plotting is not part of this library; the df stack is saved as {os.path.join(plot_to_dir, 'df.npy')}")
         return X
 
     def __call__(self, *args, **kwargs):

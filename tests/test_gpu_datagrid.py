@@ -141,3 +141,11 @@ def test_afmulator_tip_density_on_other_grid_vs_oracle(gpulib, oracle):
     assert np.abs(FE[..., :3] - FEo[..., :3])[m].max() <= 1e-4 * min(scale, 10.0) + 1e-5
     d = np.abs(X_gpu - Xo)
     assert (d > 0.1).mean() < 0.01 and np.median(d) < 1e-2
+    # plot_to_dir: no plotting here; the stack is saved instead, the result unchanged
+    import os
+    import tempfile
+
+    out_dir = tempfile.mkdtemp()
+    with pytest.warns(UserWarning):
+        X2 = afm.eval(xyzs, Zs, HartreePotential(pot, lvp), plot_to_dir=out_dir)
+    assert np.array_equal(X2, X_gpu) and np.array_equal(np.load(os.path.join(out_dir, "df.npy")), X2)
