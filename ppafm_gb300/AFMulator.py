@@ -353,6 +353,159 @@ class AFMulator:
     def __call__(self, *args, **kwargs):
         return self.eval(*args, **kwargs)
 
+    def eval_(self, mol):
+        """eval of an object with xyzs, Zs and qs attributes (AFMulator.py:181-182)."""
+        return self.eval(mol.xyzs, mol.Zs, mol.qs)
+
     def downloadFF(self):
         """The force field as [nx, ny, nz, 4] float32 (Fx, Fy, Fz, E)."""
         return self._ff.grid4.cpu().numpy()
+
+    # ------------------------------------------------------------ parameter files
+
+    @classmethod
+    def from_params(cls, file_path="./params.ini"):
+        """An AFMulator configured from a params.ini (or .toml) file (AFMulator.py:483-494)."""
+        parameters, sample_lvec = _get_params(file_path)
+        afm = cls(**parameters)
+        afm.sample_lvec = sample_lvec
+        return afm
+
+    def load_params(self, file_path="./params.ini"):
+        """Updates this AFMulator from a parameter file (AFMulator.py:496-520)."""
+        parameters, sample_lvec = _get_params(file_path)
+        if parameters["tipStiffness"] is not None:
+            self.setStiffness(parameters["tipStiffness"])
+        self.iZPP = parameters["iZPP"]
+        self.tipR0 = np.array(parameters["tipR0"], dtype=np.float64)
+        self.f0Cantilever = parameters["f0Cantilever"]
+        self.kCantilever = parameters["kCantilever"]
+        self.npbc = parameters["npbc"]
+        self.A_pauli = parameters["A_pauli"]
+        self.setScanWindow(parameters["scan_window"], parameters["scan_dim"], parameters["df_steps"])
+        self.setLvec(parameters["lvec"], parameters["pixPerAngstrome"])
+        if self.rho is None or isinstance(self.rho, dict):
+            self.setRho(parameters["rho"], parameters["sigma"])
+        else:
+            import warnings
+
+            warnings.warn(f'Using existing tip density with exponent {parameters["B_pauli"]}, instead of parameters from params.ini file.')
+            self.setRho(self.rho, sigma=parameters["sigma"], B_pauli=parameters["B_pauli"])
+        self.sample_lvec = sample_lvec
+        self.colorscale = parameters["colorscale"]
+
+    def save_params(self, file_path="./params.ini"):
+        """Writes this AFMulator's parameters as a params.ini file (AFMulator.py:522-565)."""
+        import warnings
+
+        k = self.stiffness * -common.eVA_Nm
+        scan_step = (
+            (self.scan_window[1][0] - self.scan_window[0][0]) / (self.scan_dim[0] - 1),
+            (self.scan_window[1][1] - self.scan_window[0][1]) / (self.scan_dim[1] - 1),
+            (self.scan_window[1][2] - self.scan_window[0][2]) / self.scan_dim[2],
+        )
+        with open(file_path, "w") as f:
+            f.write(f"probeType {self.iZPP}\n")
+            if isinstance(self.rho, dict):
+                if len(self.rho) > 1:
+                    warnings.warn("More than one tip multipole type specified. Only writing the first one into params.ini.")
+                tip = list(self.rho)[0]
+                f.write(f"tip {tip}\n")
+                f.write(f"charge {self.rho[tip]}\n")
+                f.write(f"sigma {self.sigma}\n")
+            f.write(f"stiffness {k[0]} {k[1]} {k[3]}\n")
+            f.write(f"r0Probe {self.tipR0[0]} {self.tipR0[1]} {self.tipR0[2]}\n")
+            f.write(f"PBC {(np.array(self.npbc) > 0).any()}\n")
+            f.write(f"nPBC {self.npbc[0]} {self.npbc[1]} {self.npbc[2]}\n")
+            if self.sample_lvec is not None:
+                sl = np.asarray(self.sample_lvec)
+                for name, row in zip(("gridA", "gridB", "gridC"), sl):
+                    f.write(f"{name} {row[0]} {row[1]} {row[2]}\n")
+            for name, row in zip(("FFgrid0", "FFgridA", "FFgridB", "FFgridC"), self.lvec):
+                f.write(f"{name} {row[0]} {row[1]} {row[2]}\n")
+            f.write(f"gridN {self.nDim[0]} {self.nDim[1]} {self.nDim[2]}\n")
+            f.write(f"scanMin {self.scan_window[0][0]} {self.scan_window[0][1]} {self.scan_window[0][2]}\n")
+            f.write(f"scanMax {self.scan_window[1][0]} {self.scan_window[1][1]} {self.scan_window[1][2]}\n")
+            f.write(f"scanStep {scan_step[0]} {scan_step[1]} {scan_step[2]}\n")
+            f.write(f"kCantilever {self.kCantilever}\n")
+            f.write(f"f0Cantilever {self.f0Cantilever}\n")
+            f.write(f"Amplitude {self.amplitude}\n")
+            f.write(f"Apauli {self.A_pauli}\n")
+            f.write(f"Bpauli {self.B_pauli}\n")
+
+    # ------------------------------------------------------------ debugging aids
+
+    def saveFF(self, prefix="./"):
+        """The force field's components, |F| clamped to 10 eV/A, as XSF files FF_x/y/z.xsf
+        (AFMulator.py:569-583)."""
+        FF = self.downloadFF()
+        F = FF[..., :3].astype(np.float64)
+        Fr = np.sqrt((F**2).sum(axis=-1))
+        k = np.where(Fr > 10.0, 10.0 / np.where(Fr > 0, Fr, 1.0), 1.0)
+        for c, name in enumerate("xyz"):
+            self.saveDebugXSF_FF(f"{prefix}FF_{name}.xsf", F[..., c] * k)
+
+    def saveDebugXSF_FF(self, fname, F):
+        from . import io
+
+        io.saveXSFData(fname, F, self.lvec)
+
+    def check_scan_window(self):
+        """Warns when the scan window comes within 0.3 A of a non-periodic edge of the
+        force-field grid (AFMulator.py:589-607)."""
+        import warnings
+
+        for i, dim in enumerate("xyz"):
+            if self.npbc[i]:
+                continue
+            lo = self.lvec[0, i]
+            hi = lo + self.lvec[i + 1, i]
+            s0 = self.scan_window[0][i] - 0.3
+            s1 = self.scan_window[1][i] + 0.3
+            if i == 2:
+                s0 -= self.tipR0[2]
+                s1 -= self.tipR0[2]
+            if s0 < lo or s1 > hi:
+                warnings.warn(
+                    f"The edge of the scan window in {dim} dimension is very close or extends over the boundary of the force-field grid "
+                    f"which is not periodic in {dim} dimension. If you get artifacts in the images, please check the boundary conditions "
+                    "and the size of the scan window and the force field grid."
+                )
+
+
+def _get_params(file_path):
+    """AFMulator arguments from a parameter file (AFMulator.py:642-699).  A file with PBC False
+    gives npbc (0, 0, 0)."""
+    import warnings
+
+    from .species import SYMBOL_TO_Z
+
+    p = common.PpafmParameters.from_file(file_path)
+    lvec = np.array([p.FFgrid0, p.FFgridA, p.FFgridB, p.FFgridC], dtype=np.float64)
+    if (lvec < 0).any():
+        lvec = None
+    sample_lvec = np.array([p.gridA, p.gridB, p.gridC], dtype=np.float64)
+    if (np.array(p.gridN) == 0).any() or lvec is None:
+        pix = 10
+    else:
+        rx, ry, rz = (round(p.gridN[i] / np.linalg.norm(lvec[i + 1])) for i in range(3))
+        if np.allclose([rx, ry], rz):
+            pix = rx
+        else:
+            pix = int(np.max([rx, ry, rz]))
+            warnings.warn(f"Unequal grid densities in x, y, z directions is not supported by the AFMulator. Using the maximum of x, y, z directions, {pix}, for grid point density.")
+    scan_window = (tuple(p.scanMin), tuple(p.scanMax))
+    scan_dim = (
+        round((scan_window[1][0] - scan_window[0][0]) / p.scanStep[0]) + 1,
+        round((scan_window[1][1] - scan_window[0][1]) / p.scanStep[1]) + 1,
+        round((scan_window[1][2] - scan_window[0][2]) / p.scanStep[2]),
+    )
+    iZPP = SYMBOL_TO_Z[p.probeType] if p.probeType in SYMBOL_TO_Z else int(p.probeType)
+    stiff = p.stiffness
+    stiff = [0.25, 0.25, 0.0, 30.0] if (np.array(stiff) < 0).any() else list(np.insert(np.array(stiff, dtype=np.float64), 2, 0.0))
+    params = dict(
+        lvec=lvec, pixPerAngstrome=pix, scan_dim=scan_dim, scan_window=scan_window, iZPP=iZPP, rho={p.tip: p.charge}, sigma=p.sigma,
+        A_pauli=p.Apauli, B_pauli=p.Bpauli, df_steps=round(p.Amplitude / p.scanStep[2]), tipR0=p.r0Probe, tipStiffness=stiff,
+        npbc=tuple(p.nPBC) if p.PBC else (0, 0, 0), f0Cantilever=p.f0Cantilever, kCantilever=p.kCantilever, colorscale=p.colorscale,
+    )
+    return params, sample_lvec

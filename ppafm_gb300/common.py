@@ -19,6 +19,133 @@ atom2iZ = _species.atom2iZ
 atoms2iZs = _species.atoms2iZs
 
 
+# ------------------------------------------------------------------ parameters
+
+# Defaults of PpafmParameters (common.py:26-78), in the reference's order.
+_PARAM_DEFAULTS = dict(
+    PBC=True, nPBC=[1, 1, 1], gridN=[-1, -1, -1], gridO=[0.0, 0.0, 0.0], gridA=[20.0, 0.0, 0.0], gridB=[0.0, 20.0, 0.0], gridC=[0.0, 0.0, 20.0],
+    FFgrid0=[-1.0, -1.0, -1.0], FFgridA=[-1.0, -1.0, -1.0], FFgridB=[-1.0, -1.0, -1.0], FFgridC=[-1.0, -1.0, -1.0], moleculeShift=[0.0, 0.0, 0.0],
+    probeType="O", charge=0.00, Apauli=18.0, Bpauli=1.0, ffModel="LJ", Rcore=0.7, r0Probe=[0.00, 0.00, 4.00], stiffness=[-1.0, -1.0, -1.0],
+    klat=0.5, krad=20.00, tip="s", sigma=0.7, scanStep=[0.10, 0.10, 0.10], scanMin=[0.0, 0.0, 5.0], scanMax=[20.0, 20.0, 8.0],
+    scanTilt=[0.0, 0.0, -0.1], tiltedScan=False, kCantilever=1800.0, f0Cantilever=30300.0, Amplitude=1.0, plotSliceFrom=16, plotSliceTo=22,
+    plotSliceBy=1, imageInterpolation="bicubic", colorscale="gray", colorscale_kpfm="seismic", ddisp=0.05, aMorse=-1.6, Rtip=30.0,
+    permit=0.00552634959, vdWDampKind=2, Vbias=0.0,
+)
+
+
+class PpafmParameters:
+    """Simulation parameters with the reference's names and defaults (common.py:26-160):
+    attributes, ``from_file`` for params.ini (``load_ini``: one ``key value...`` per line,
+    ``#`` comments, values typed like the defaults) and params.toml, ``to_file`` for toml.
+    Every function here that takes ``parameters`` accepts this object or a dict."""
+
+    def __init__(self, **kw):
+        for k, v in _PARAM_DEFAULTS.items():
+            setattr(self, k, list(v) if isinstance(v, list) else v)
+        self.apply_options(kw)
+
+    def __setattr__(self, key, value):
+        if key not in _PARAM_DEFAULTS:
+            raise AttributeError(f"Parameter {key} is not known")
+        object.__setattr__(self, key, value)
+
+    @classmethod
+    def from_file(cls, file_path="params.ini"):
+        from pathlib import Path
+
+        file_path = Path(file_path)
+        obj = cls()
+        try:
+            with open(file_path, "rb" if file_path.suffix == ".toml" else "r") as f:
+                if file_path.suffix == ".ini":
+                    obj.load_ini(f.readlines())
+                elif file_path.suffix == ".toml":
+                    import tomllib
+
+                    obj.apply_options(tomllib.load(f))
+                else:
+                    raise ValueError(f"Unsupported file extension: {file_path.suffix}")
+        except FileNotFoundError:
+            raise ValueError(f"File {file_path} not found")
+        return obj
+
+    def apply_options(self, obj):
+        for key, value in obj.items():
+            if key in _PARAM_DEFAULTS and value is not None:
+                setattr(self, key, value)
+
+    def model_dump(self):
+        return {k: getattr(self, k) for k in _PARAM_DEFAULTS}
+
+    def __eq__(self, other):
+        return isinstance(other, PpafmParameters) and self.model_dump() == other.model_dump()
+
+    def __repr__(self):
+        return "PpafmParameters(" + ", ".join(f"{k}={v!r}" for k, v in self.model_dump().items()) + ")"
+
+    def to_file(self, file_path="params.toml"):
+        """Writes the parameters as toml (flat keys; strings, numbers, booleans, lists)."""
+        from pathlib import Path
+
+        file_path = Path(file_path)
+        if file_path.suffix != ".toml":
+            raise ValueError(f"Unsupported file extension: {file_path.suffix}")
+
+        def fmt(v):
+            if isinstance(v, bool):
+                return "true" if v else "false"
+            if isinstance(v, str):
+                return '"' + v.replace("\\", "\\\\").replace('"', '\\"') + '"'
+            if isinstance(v, (list, tuple)):
+                return "[" + ", ".join(fmt(x) for x in v) + "]"
+            return repr(float(v)) if isinstance(v, float) else str(int(v))
+
+        with open(file_path, "w") as f:
+            for k, v in self.model_dump().items():
+                f.write(f"{k} = {fmt(v)}\n")
+
+    def load_ini(self, lines):
+        """params.ini lines (common.py:119-160): bools by their first letter, lists of three
+        numbers (a string and a number for a tip list), gridN from the cell when not given."""
+        for line in lines:
+            words = line.split("#")[0].strip().split()
+            if len(words) < 2:
+                continue
+            key = words[0]
+            if key not in _PARAM_DEFAULTS:
+                raise ValueError(f"Parameter {key} is not known")
+            val = getattr(self, key)
+            try:
+                if isinstance(val, bool):
+                    setattr(self, key, words[1].strip()[0] in "Tt")
+                elif isinstance(val, float):
+                    setattr(self, key, float(words[1]))
+                elif isinstance(val, int):
+                    setattr(self, key, int(words[1]))
+                elif isinstance(val, str):
+                    setattr(self, key, words[1])
+                elif isinstance(val, list):
+                    if isinstance(val[0], float):
+                        setattr(self, key, [float(words[1]), float(words[2]), float(words[3])])
+                    elif isinstance(val[0], int):
+                        setattr(self, key, [int(words[1]), int(words[2]), int(words[3])])
+                    else:
+                        setattr(self, key, [str(words[1]), float(words[2])])
+            except (ValueError, IndexError):
+                raise ValueError(f"Error parsing parameters on line: {line}") from None
+        if self.gridN[0] <= 0:
+            autoGridN(self)
+        if isinstance(self.tip, str):
+            self.tip = self.tip.replace('"', "").replace("'", "")
+
+
+def autoGridN(parameters):
+    """Grid size at 10 points per A of each cell vector (common.py:518-522)."""
+    for k, v in enumerate((parameters.gridA, parameters.gridB, parameters.gridC)):
+        parameters.gridN[k] = round(np.linalg.norm(v) * 10)
+    return parameters.gridN
+
+
 # ------------------------------------------------------------------ Δf weights
 
 

@@ -3,7 +3,7 @@
 Run where the reference checkout exists (it is read only):
 
     python tests/golden/make_golden.py [/root/reference]           # all fixtures
-    python tests/golden/make_golden.py /root/reference extras      # xsf/ and tilt.npz only
+    python tests/golden/make_golden.py /root/reference extras      # xsf/, tilt.npz, params/ only
 
 The script copies the reference's ``ppafm`` package to a temporary directory, compiles
 its two C++ modules there from their own sources with g++ (ProbeParticle, GridUtils; the
@@ -44,6 +44,7 @@ def main(ref_root="/root/reference", only=None):
         try:
             make_xsf(tmp)
             make_tilt(tmp)
+            make_params(ref_root)
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         return
@@ -231,6 +232,23 @@ def make_tilt(tmp):
         cases[f"df_{i}"] = PPU.Fz2df_tilt(F, d, k0=1800.0, f0=30300.0, amplitude=amp)
     np.savez_compressed(os.path.join(HERE, "tilt.npz"), F=F, **cases)
     print("tilt fixture written")
+
+
+def make_params(ref_root):
+    """PpafmParameters (common.py:26-160) of the reference's own test file
+    (tests/data/test_params.ini) and its defaults, parsed by the reference -> tests/golden/params/."""
+    import json
+
+    import ppafm.common as PPU
+
+    out = os.path.join(HERE, "params")
+    os.makedirs(out, exist_ok=True)
+    shutil.copyfile(os.path.join(ref_root, "tests", "data", "test_params.ini"), os.path.join(out, "test_params.ini"))
+    parsed = PPU.PpafmParameters.from_file(os.path.join(out, "test_params.ini")).model_dump()
+    default = PPU.PpafmParameters().model_dump()
+    with open(os.path.join(out, "parsed.json"), "w") as f:
+        json.dump({"parsed": parsed, "default": default}, f, indent=1)
+    print("params fixtures written")
 
 
 if __name__ == "__main__":

@@ -149,3 +149,14 @@ def test_afmulator_tip_density_on_other_grid_vs_oracle(gpulib, oracle):
     with pytest.warns(UserWarning):
         X2 = afm.eval(xyzs, Zs, HartreePotential(pot, lvp), plot_to_dir=out_dir)
     assert np.array_equal(X2, X_gpu) and np.array_equal(np.load(os.path.join(out_dir, "df.npy")), X2)
+    # eval_ of a molecule object, and the force field saved as XSF (|F| clamped to 10 eV/A)
+    from types import SimpleNamespace
+
+    assert np.array_equal(afm.eval_(SimpleNamespace(xyzs=xyzs, Zs=Zs, qs=HartreePotential(pot, lvp))), X_gpu)
+    afm.saveFF(prefix=os.path.join(out_dir, ""))
+    from ppafm_gb300.io import loadXSFData
+
+    Fz, _, _, _ = loadXSFData(os.path.join(out_dir, "FF_z.xsf"))
+    F = afm.downloadFF()[..., :3].astype(np.float64)
+    k = np.minimum(1.0, 10.0 / np.maximum(np.linalg.norm(F, axis=-1), 1e-30))
+    assert np.allclose(Fz, F[..., 2] * k, rtol=1e-5, atol=1e-5)

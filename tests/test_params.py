@@ -1,0 +1,91 @@
+"""Simulation parameters (common.PpafmParameters, restating ppafm/common.py:26-160): the
+reference's own test (tests/test_common.py test_ppafm_parameters) on its parameter file, with
+the parsed values and the defaults compared to what the reference itself produced
+(tests/golden/params/, made by tests/golden/make_golden.py)."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden", "params")
+
+
+def test_ppafm_parameters(tmp_path):
+    from ppafm_gb300 import common
+
+    ref = json.load(open(os.path.join(GOLD, "parsed.json")))
+    p_default = common.PpafmParameters()
+    assert p_default.model_dump() == ref["default"]
+    assert p_default.PBC is True and p_default.nPBC == [1, 1, 1] and p_default.probeType == "O"
+    assert p_default.gridN == [-1, -1, -1] and np.isclose(p_default.klat, 0.5) and p_default.vdWDampKind == 2
+
+    p_ini = common.PpafmParameters.from_file(os.path.join(GOLD, "test_params.ini"))
+    assert p_ini.model_dump() == ref["parsed"]
+    assert p_ini.PBC is False and p_ini.nPBC == [2, 3, 4] and p_ini.probeType == "Xe"
+    assert np.isclose(p_ini.charge, 0.5) and p_ini.ffModel == "Morse" and np.isclose(p_ini.gridN, [10, 20, 30]).all()
+    assert np.isclose(p_ini.scanStep, [0.1, 0.2, 0.3]).all() and np.isclose(p_ini.Amplitude, 8.0) and p_ini.vdWDampKind == 3
+
+    p_ini.to_file(tmp_path / "test_params.toml")
+    assert common.PpafmParameters.from_file(tmp_path / "test_params.toml") == p_ini
+
+    # gridN from the cell when the file does not give it; unknown keys and bad values raise
+    (tmp_path / "a.ini").write_text("gridA 12.0 0 0\ngridB 0 8.5 0\ngridC 0 0 20.0\n")
+    assert common.PpafmParameters.from_file(tmp_path / "a.ini").gridN == [120, 85, 200]
+    (tmp_path / "b.ini").write_text("nosuchkey 1\n")
+    with pytest.raises(ValueError):
+        common.PpafmParameters.from_file(tmp_path / "b.ini")
+    (tmp_path / "c.ini").write_text("scanMin 1.0 2.0\n")
+    with pytest.raises(ValueError):
+        common.PpafmParameters.from_file(tmp_path / "c.ini")
+    with pytest.raises(ValueError):
+        common.PpafmParameters.from_file(tmp_path / "missing.ini")
+
+
+def test_parameters_drive_the_host_helpers():
+    """A PpafmParameters object where the pipeline functions take parameters (attribute access)."""
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import common
+
+    p = common.PpafmParameters(probeType="8", charge=-0.05, r0Probe=[0.0, 0.0, 4.0], klat=0.25, krad=20.0)
+    assert HL._get(p, "probeType") == "8" and HL._get(p, "charge") == -0.05
+    v = HL.tip_vector(p, dict(maxIters=300, convF2=1e-8, dt=0.5, damping=0.1))
+    assert np.isfinite(v).all()
+
+
+def test_afmulator_parameter_files(tmp_path):
+    """AFMulator.from_params / save_params / load_params (AFMulator.py:483-565): the values a
+    params.ini sets, a save and reload, and the scan-window check (no GPU work involved)."""
+    import warnings
+
+    from ppafm_gb300.AFMulator import AFMulator
+
+    (tmp_path / "params.ini").write_text(
+        "probeType 8\ntip dz2\ncharge -0.1\nsigma 0.71\nstiffness 0.25 0.25 20.0\nr0Probe 0.0 0.0 3.0\n"
+        "PBC True\nnPBC 1 1 0\ngridA 16.0 0 0\ngridB 0 16.0 0\ngridC 0 0 20.0\n"
+        "scanMin 2.0 2.0 7.0\nscanMax 14.0 14.0 10.0\nscanStep 0.1 0.1 0.1\nAmplitude 1.0\n"
+    )
+    afm = AFMulator.from_params(tmp_path / "params.ini")
+    assert afm.iZPP == 8 and afm.rho == {"dz2": -0.1} and np.isclose(afm.sigma, 0.71)
+    assert afm.scan_dim == (121, 121, 30) and afm.df_steps == 10 and tuple(afm.npbc) == (1, 1, 0)
+    assert np.allclose(afm.sample_lvec, np.diag([16.0, 16.0, 20.0]))
+    assert np.allclose(afm.stiffness * -16.0217662, [0.25, 0.25, 0.0, 20.0], rtol=1e-6)
+    afm.save_params(tmp_path / "saved.ini")
+    b = AFMulator.from_params(tmp_path / "saved.ini")
+    assert b.scan_dim == afm.scan_dim and b.df_steps == afm.df_steps and b.rho == afm.rho
+    assert np.allclose(b.lvec, afm.lvec) and np.array_equal(b.nDim, afm.nDim)
+    assert np.allclose(b.stiffness, afm.stiffness, rtol=1e-6) and np.allclose(b.tipR0, afm.tipR0)
+    c = AFMulator()
+    c.load_params(tmp_path / "saved.ini")
+    assert c.scan_dim == afm.scan_dim and np.allclose(c.lvec, afm.lvec) and c.rho == afm.rho
+    # scan window reaching past the non-periodic z edge of the force-field grid
+    c.setScanWindow(((2.0, 2.0, 7.0), (14.0, 14.0, 60.0)), (121, 121, 30))
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        c.check_scan_window()
+    assert any("boundary of the force-field grid" in str(x.message) for x in w)
+    # a symbol as probe type
+    (tmp_path / "xe.ini").write_text("probeType Xe\n")
+    assert AFMulator.from_params(tmp_path / "xe.ini").iZPP == 54
