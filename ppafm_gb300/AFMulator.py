@@ -302,9 +302,19 @@ class AFMulator:
         nw = len(self.dfWeight)
         nout = nz - nw + 1
         dev = ff.FE.device
-        if self._out is None:
-            self._points = torch.from_numpy(self._scan_points().reshape(-1, 4)).to(dev)
+        if self._out is None or self._out["X"].shape != (npix, nout) or self._out["FEs"].shape[1] != nz:
             self._out = dict(FEs=torch.empty((npix, nz, 4), dtype=torch.float32, device=dev), X=torch.empty((npix, nout), dtype=torch.float32, device=dev))
+        key = (tuple(map(tuple, self.scan_window)), tuple(self.scan_dim), tuple(self.lvec[0]))
+        if getattr(self, "_points_key", None) != key:
+            # tip positions of this scan window: packed in pinned memory and copied without a
+            # synchronisation, so a generator's next image is prepared while the GPU works
+            pts = torch.from_numpy(self._scan_points().reshape(-1, 4)).pin_memory()
+            if stream is None:
+                self._points = pts.to(dev, non_blocking=True)
+            else:
+                with torch.cuda.stream(stream):
+                    self._points = pts.to(dev, non_blocking=True)
+            self._points_key = key
         if want_paths and "paths" not in self._out:
             self._out["paths"] = torch.empty((npix, nz, 4), dtype=torch.float32, device=dev)
         if want_iters and "iters" not in self._out:

@@ -20,7 +20,7 @@ import torch
 
 from . import common as PPU
 from . import core
-from .device import DeviceFF, iter_counter, pack_atoms, relax_params, relax_scan, relax_strokes
+from .device import DeviceFF, iter_counter, pack_atoms, relax_params, relax_scan, relax_strokes, upload_f64
 from .device import tip_spline as tip_spline_ctx
 from .fieldFFT import FFTGrid
 from ._lib import FF_COULOMB, FF_LJ, FF_LJC
@@ -244,6 +244,17 @@ def computeELFF_pointCharge_atoms(Zs, Rs, Qs, lvec, gridN, parameters, tip="s", 
 # ------------------------------------------------------------------- pipeline
 
 
+def _scan_coords(self, stream=None):
+    """The pipeline's tip coordinates (xs, ys, zs) as device tensors, uploaded again only when
+    the host arrays change."""
+    host = (self.xs, self.ys, self.zs)
+    cached = getattr(self, "_coords", None)
+    if cached is None or not all(np.array_equal(a, b) for a, b in zip(cached[0], host)):
+        dev = self.ff.FE.device
+        self._coords = (tuple(np.array(v, dtype=np.float64) for v in host), tuple(upload_f64(v, dev, stream) for v in host))
+    return self._coords[1]
+
+
 class Pipeline:
     """The reference CPU pipeline (computeLJ + computeELFF_pointCharge with the default
     clamp, perform_relaxation, Fz2df) as device-resident stages.  Build once per system,
@@ -295,8 +306,10 @@ class Pipeline:
             self.ff.axpby(1.0, self.ff_el, self.Q, stream=stream)
         return self.ff
 
+    _scan_coords = _scan_coords
+
     def relax(self, stream=None):
-        self.out = relax_scan(self.ff, self.prm, self.xs, self.ys, self.zs, pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
+        self.out = relax_scan(self.ff, self.prm, *self._scan_coords(stream), pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
         return self.out
 
     def run(self, stream=None):
@@ -397,8 +410,10 @@ class DensityOverlapPipeline:
             g.potential2forces(self.V, self.rho_t, self.lvec, FE=self.ff.FE, scale=self.Q / self.Ne, with_E=True, accumulate=True, stream=stream)
         return self.ff
 
+    _scan_coords = _scan_coords
+
     def relax(self, stream=None):
-        self.out = relax_scan(self.ff, self.prm, self.xs, self.ys, self.zs, pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
+        self.out = relax_scan(self.ff, self.prm, *self._scan_coords(stream), pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
         return self.out
 
     def run(self, stream=None):

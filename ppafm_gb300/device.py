@@ -206,14 +206,25 @@ def relax_strokes(ff, prm, rTips, probeStart=1, relaxAlg=1, iters=False, counter
     return rs, fs, itrsum, it
 
 
+def upload_f64(v, dev, stream=None):
+    """A float64 device tensor of v: device tensors pass through; host arrays go through pinned
+    memory without a synchronisation, on stream (default: the current stream)."""
+    if isinstance(v, torch.Tensor) and v.is_cuda:
+        return v.to(torch.float64).contiguous()
+    t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).pin_memory()
+    if stream is None:
+        return t.to(dev, non_blocking=True)
+    with torch.cuda.stream(stream):
+        return t.to(dev, non_blocking=True)
+
+
 def relax_scan(ff, prm, xs, ys, zs, pos_offset=(0.0, 0.0, 0.0), df_weights=None, want_fzs=True, want_ppos=True, want_iters=False, counter=None, out=None, stream=None):
     """Regular scan with relaxedScan3D_omp semantics: tips at (xs[ix], ys[iy], zs[iz])
-    relative to the grid origin, zs in approach order (descending).  Outputs ascending z.
+    relative to the grid origin, zs in approach order (descending); host arrays or float64
+    device tensors.  Outputs ascending z.
     df_weights (already scaled, np.convolve orientation) adds the fused Δf epilogue."""
     dev = ff.FE.device
-    xs_d = torch.as_tensor(np.ascontiguousarray(xs, dtype=np.float64)).to(dev)
-    ys_d = torch.as_tensor(np.ascontiguousarray(ys, dtype=np.float64)).to(dev)
-    zs_d = torch.as_tensor(np.ascontiguousarray(zs, dtype=np.float64)).to(dev)
+    xs_d, ys_d, zs_d = (upload_f64(v, dev, stream) for v in (xs, ys, zs))
     nx, ny, nz = len(xs), len(ys), len(zs)
     out = {} if out is None else out
     need_fzs = want_fzs or df_weights is not None
