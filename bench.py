@@ -174,19 +174,24 @@ class PointChargeJob:
         self.nch = self.pl.ncharged
         self.ff_name = "ff_kernel<LJC> (force field)" if self.pl.Q != 0.0 else "ff_kernel<LJ> (force field)"
         self.launches_per_step = 2
-        self.rec_pinned = torch.empty(self.pl.atoms.shape, dtype=self.pl.atoms.dtype, pin_memory=True)
+        self.rec_pinned = [torch.empty(self.pl.atoms.shape, dtype=self.pl.atoms.dtype, pin_memory=True) for _ in range(2)]
         self.host_in = {k: np.asarray(w[k]).copy() for k in ("Zs", "Rs", "Qs")}
 
-    def e2e_inputs(self):
-        """Host prep (PBC images, LJ mixing, packing) + H2D of the atom records; bytes copied."""
+    def e2e_host(self, slot=0):
+        """Host prep of one step (PBC images, LJ mixing, packing into pinned slot `slot`);
+        returns the bytes e2e_h2d copies."""
         from ppafm_gb300.device import pack_atoms
 
         pl = self.pl
         Rs0, cLJs, kqq = self.HL.prepare_atoms(self.host_in["Zs"], self.host_in["Rs"], self.host_in["Qs"], pl.lvec, self.w)
         rec, _, _ = pack_atoms(Rs0, cLJs, kqq if pl.Q != 0.0 else None, device="cpu")
-        self.rec_pinned.copy_(rec)
-        pl.atoms.copy_(self.rec_pinned, non_blocking=True)
-        return int(self.rec_pinned.numel() * self.rec_pinned.element_size())
+        pin = self.rec_pinned[slot]
+        pin.copy_(rec)
+        return int(pin.numel() * pin.element_size())
+
+    def e2e_h2d(self, slot=0):
+        """H2D of the atom records of pinned slot `slot` (on the current stream)."""
+        self.pl.atoms.copy_(self.rec_pinned[slot], non_blocking=True)
 
     def ff_roofline(self, t_ff, peak_fp32):
         if self.pl.Q != 0.0:
@@ -217,7 +222,12 @@ class OverlapJob:
         for h, d in zip(self.host, (self.pl.rho_s, self.pl.rho_q, self.pl.rho_t)):
             h.copy_(d)
 
-    def e2e_inputs(self):
+    def e2e_host(self, slot=0):
+        """Nothing to prepare: the density grids are pinned host arrays; returns their bytes."""
+        return int(sum(h.numel() * h.element_size() for h in self.host))
+
+    def e2e_h2d(self, slot=0):
+        """H2D of the three density grids (on the current stream)."""
         for h, d in zip(self.host, (self.pl.rho_s, self.pl.rho_q, self.pl.rho_t)):
             d.copy_(h, non_blocking=True)
         return int(sum(h.numel() * h.element_size() for h in self.host))
@@ -261,6 +271,7 @@ class BatchBench:
         self.w = systems[0]
         self.systems = systems
         self.torch = torch
+        self.HL = HL
         if tuning is None:
             self.tuning, self.tune_ms = BT.autotune(systems, self.w, relax, reps=2)
         else:
@@ -273,33 +284,42 @@ class BatchBench:
         self.launches_per_step = 1
         self.BT = BT
         self.relax = relax
-        pin = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s["out"].items()} for s in self.pl.systems]
-        self.pin_out = pin
+        # two pinned slots of inputs and outputs (double-buffered end-to-end steps)
+        self.pin_out = [[{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s["out"].items()} for s in self.pl.systems] for _ in range(2)]
+        self.rec_pin = [[torch.empty(s["rec"].shape, dtype=s["rec"].dtype, pin_memory=True) for s in self.pl.systems] for _ in range(2)]
+        self._done = [None, None]
+        self._k = 0
 
     def step(self):
         self.pl.replay()
 
     def e2e_step(self):
-        """Public API end to end: host atoms of every molecule -> packed records (H2D) ->
-        the batched launch -> outputs to pinned host memory (D2H)."""
+        """Public API end to end, double-buffered: host atoms of every molecule -> packed
+        records in pinned slot k % 2 (H2D) -> the batched launch -> outputs to pinned slot
+        k % 2 (D2H).  The host prepares step k while the GPU runs step k-1, waiting only for
+        step k-2's outputs before it reuses their slot."""
         from ppafm_gb300.device import pack_atoms
 
+        slot = self._k % 2
+        if self._done[slot] is not None:
+            self._done[slot].synchronize()
         h2d = 0
-        for s, w in zip(self.pl.systems, self.systems):
+        for s, w, pin in zip(self.pl.systems, self.systems, self.rec_pin[slot]):
             Rs0, cLJs, kqq = self.HL.prepare_atoms(w["Zs"], w["Rs"], w["Qs"], w["lvec"], self.w)
             rec, _, _ = pack_atoms(Rs0, cLJs, kqq, device="cpu")
-            s.setdefault("rec_pin", self.torch.empty(rec.shape, dtype=rec.dtype, pin_memory=True))
-            s["rec_pin"].copy_(rec)
+            pin.copy_(rec)
             h2d += rec.numel() * rec.element_size()
-        for s in self.pl.systems:
-            s["rec"].copy_(s["rec_pin"], non_blocking=True)
+        for s, pin in zip(self.pl.systems, self.rec_pin[slot]):
+            s["rec"].copy_(pin, non_blocking=True)
         self.pl.replay()
         d2h = 0
-        for s, pin in zip(self.pl.systems, self.pin_out):
+        for s, pin in zip(self.pl.systems, self.pin_out[slot]):
             for k, v in s["out"].items():
                 pin[k].copy_(v, non_blocking=True)
                 d2h += v.numel() * v.element_size()
-        self.torch.cuda.current_stream().synchronize()
+        self._done[slot] = self.torch.cuda.Event()
+        self._done[slot].record()
+        self._k += 1
         return h2d, d2h
 
     def learned(self, args, plain_loop_ms, steps=120000, lr=1e-3):
@@ -399,7 +419,6 @@ def run_batch(args, rank, world, local):
     relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
     tuning = [int(x) for x in args.tuning.split(",")] if args.tuning else None
     job = BatchBench(systems, relax, HL, torch, tuning=tuning)
-    job.HL = HL
     st = torch.cuda.current_stream()
 
     def barrier():
@@ -430,6 +449,7 @@ def run_batch(args, rank, world, local):
     for _ in range(max(1, args.warmup)):
         job.e2e_step()
     barrier()
+    torch.cuda.synchronize()  # the first timed step's host work falls inside the interval
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
     a.record(st)
@@ -562,18 +582,50 @@ def run_ours(args, rank, world, local):
     iters_total = int(pl.counter.item())
     _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
 
-    # ---------------- end to end through the host API
-    pin_out = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in pl.out.items()}
+    # ---------------- end to end through the host API.  Every step copies its own inputs in
+    # and its outputs out, through pinned slot k % 2.  The copies run on two more streams: the
+    # inputs of step k go in once step k-1's force field has read its inputs (during step
+    # k-1's relaxation), the outputs of step k come out while step k+1's force field runs
+    # (step k+1's relaxation waits for them); the host prepares step k while the GPU works and
+    # waits only for step k-2's outputs before reusing their slot.
+    pin_out = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in pl.out.items()} for _ in range(2)]
+    cs = torch.cuda.Stream()  # host -> device
+    ds = torch.cuda.Stream()  # device -> host
+    done = [None, None]
+    last = {"ff": None, "d2h": None}
     h2d = [0]
+    kstep = [0]
 
     def e2e_step():
+        slot = kstep[0] % 2
+        if done[slot] is not None:
+            done[slot].synchronize()
+        h2d[0] = job.e2e_host(slot)
+        with torch.cuda.stream(cs):
+            if last["ff"] is not None:
+                cs.wait_event(last["ff"])
+            job.e2e_h2d(slot)
+            inputs_in = torch.cuda.Event()
+            inputs_in.record(cs)
+        st.wait_event(inputs_in)
         if flush is not None:
             flush.zero_()
-        h2d[0] = job.e2e_inputs()
-        pl.run()
-        for k, v in pl.out.items():
-            pin_out[k].copy_(v, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+        pl.build_ff()
+        last["ff"] = torch.cuda.Event()
+        last["ff"].record(st)
+        if last["d2h"] is not None:
+            st.wait_event(last["d2h"])
+        pl.relax()
+        relaxed = torch.cuda.Event()
+        relaxed.record(st)
+        with torch.cuda.stream(ds):
+            ds.wait_event(relaxed)
+            for k, v in pl.out.items():
+                pin_out[slot][k].copy_(v, non_blocking=True)
+            done[slot] = torch.cuda.Event()
+            done[slot].record(ds)
+        last["d2h"] = done[slot]
+        kstep[0] += 1
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -584,11 +636,12 @@ def run_ours(args, rank, world, local):
     a.record(st)
     for _ in range(args.steps):
         e2e_step()
+    st.wait_stream(ds)  # the last outputs are on the host before the interval ends
     b.record(st)
     b.synchronize()
     barrier()
     t_e2e = a.elapsed_time(b) * 1e-3
-    d2h = int(sum(v.numel() * v.element_size() for v in pin_out.values()))
+    d2h = int(sum(v.numel() * v.element_size() for v in pin_out[0].values()))
 
     # ---------------- max over ranks
     from ppafm_gb300.ranks import max_over_ranks
