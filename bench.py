@@ -276,7 +276,7 @@ class BatchBench:
             self.tuning, self.tune_ms = BT.autotune(systems, self.w, relax, reps=2)
         else:
             self.tuning, self.tune_ms = tuple(tuning), None
-        self.pl = BT.BatchPipeline(systems, self.w, relax=relax, want_ppos=True, tuning=self.tuning)
+        self.pl = BT.BatchPipeline(systems, self.w, relax=relax, want_ppos=True, tuning=self.tuning, out_sets=2)
         self.pl.capture()
         self.units = self.pl.pixel_z
         self.npts = int(sum(np.prod(s["n"]) for s in self.pl.systems))
@@ -284,22 +284,28 @@ class BatchBench:
         self.launches_per_step = 1
         self.BT = BT
         self.relax = relax
-        # two pinned slots of inputs and outputs (double-buffered end-to-end steps)
+        # two slots of pinned inputs and outputs and of device outputs (pipelined end-to-end
+        # steps); the output copies run on their own stream
         self.pin_out = [[{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s["out"].items()} for s in self.pl.systems] for _ in range(2)]
         self.rec_pin = [[torch.empty(s["rec"].shape, dtype=s["rec"].dtype, pin_memory=True) for s in self.pl.systems] for _ in range(2)]
         self._done = [None, None]
         self._k = 0
+        self.d2h_stream = torch.cuda.Stream()
 
     def step(self):
         self.pl.replay()
 
     def e2e_step(self):
-        """Public API end to end, double-buffered: host atoms of every molecule -> packed
-        records in pinned slot k % 2 (H2D) -> the batched launch -> outputs to pinned slot
-        k % 2 (D2H).  The host prepares step k while the GPU runs step k-1, waiting only for
-        step k-2's outputs before it reuses their slot."""
+        """Public API end to end, pipelined: host atoms of every molecule -> packed records in
+        pinned slot k % 2 (H2D, in stream order: the launch before reads the records) -> the
+        batched launch into device output set k % 2 -> those outputs to pinned slot k % 2 on
+        the copy stream while the next launch writes the other set.  The host prepares step k
+        while the GPU runs step k-1, waiting only for step k-2's outputs before it reuses
+        their slots."""
         from ppafm_gb300.device import pack_atoms
 
+        torch = self.torch
+        st = torch.cuda.current_stream()
         slot = self._k % 2
         if self._done[slot] is not None:
             self._done[slot].synchronize()
@@ -311,16 +317,27 @@ class BatchBench:
             h2d += rec.numel() * rec.element_size()
         for s, pin in zip(self.pl.systems, self.rec_pin[slot]):
             s["rec"].copy_(pin, non_blocking=True)
-        self.pl.replay()
+        if self._done[slot] is not None:
+            st.wait_event(self._done[slot])  # device output set `slot` has been copied out
+        self.pl.replay(slot)
+        ran = torch.cuda.Event()
+        ran.record(st)
         d2h = 0
-        for s, pin in zip(self.pl.systems, self.pin_out[slot]):
-            for k, v in s["out"].items():
-                pin[k].copy_(v, non_blocking=True)
-                d2h += v.numel() * v.element_size()
-        self._done[slot] = self.torch.cuda.Event()
-        self._done[slot].record()
+        ds = self.d2h_stream
+        with torch.cuda.stream(ds):
+            ds.wait_event(ran)
+            for s, pin in zip(self.pl.systems, self.pin_out[slot]):
+                for k, v in s["outs"][slot].items():
+                    pin[k].copy_(v, non_blocking=True)
+                    d2h += v.numel() * v.element_size()
+            self._done[slot] = torch.cuda.Event()
+            self._done[slot].record(ds)
         self._k += 1
         return h2d, d2h
+
+    def e2e_drain(self):
+        """The current stream waits for the output copies still in flight."""
+        self.torch.cuda.current_stream().wait_stream(self.d2h_stream)
 
     def learned(self, args, plain_loop_ms, steps=120000, lr=1e-3):
         """Config-4 line: train the warm-start network on plain-FIRE pairs of a held-out batch
@@ -455,6 +472,7 @@ def run_batch(args, rank, world, local):
     a.record(st)
     for _ in range(args.steps):
         h2d, d2h = job.e2e_step()
+    job.e2e_drain()
     b.record(st)
     b.synchronize()
     t_e2e = a.elapsed_time(b) * 1e-3

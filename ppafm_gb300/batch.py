@@ -38,9 +38,13 @@ class BatchPipeline:
     """A batch of systems: each a dict with Zs, Rs, Qs, lvec (orthogonal cell), gridN and
     its scan (scanMin, scanMax, scanStep).  Probe, FIRE and Δf settings come from
     ``parameters`` (shared by the batch).  Buffers stay in device memory; ``run()`` is one
-    launch (plus a counter reset), ``capture()`` records it in a CUDA graph."""
+    launch (plus a counter reset), ``capture()`` records it in a CUDA graph.
+    out_sets > 1 keeps that many sets of output buffers (``systems[j]["outs"][slot]``), each
+    with its own launch handle and graph (``run(slot=...)``, ``replay(slot)``,
+    ``outputs(j, slot)``), so one set can be copied to the host while the next run writes
+    another; force fields and atom records are shared."""
 
-    def __init__(self, systems, parameters, relax=None, with_df=True, want_ppos=True, want_iters=False, tuning=None, FFparams=None, device="cuda"):
+    def __init__(self, systems, parameters, relax=None, with_df=True, want_ppos=True, want_iters=False, tuning=None, FFparams=None, device="cuda", out_sets=1):
         self.p = parameters
         self.device = device
         self.Q = float(_get(parameters, "charge", 0.0))
@@ -69,14 +73,19 @@ class BatchPipeline:
             ys = np.ascontiguousarray(yT - lvec[0, 1])
             zs = np.ascontiguousarray(zT[::-1] - lvec[0, 2])
             nx, ny, nz = len(xs), len(ys), len(zs)
-            out = {}
-            out["fzs"] = torch.empty((nx, ny, nz), dtype=torch.float32, device=device)
-            if want_ppos:
-                out["ppos"] = torch.empty((nx, ny, nz, 3), dtype=torch.float32, device=device)
-            if want_iters:
-                out["iters"] = torch.empty((nx, ny, nz), dtype=torch.int32, device=device)
-            if self.W is not None:
-                out["df"] = torch.empty((nx, ny, nz - len(self.W) + 1), dtype=torch.float32, device=device)
+
+            def new_out():
+                o = {"fzs": torch.empty((nx, ny, nz), dtype=torch.float32, device=device)}
+                if want_ppos:
+                    o["ppos"] = torch.empty((nx, ny, nz, 3), dtype=torch.float32, device=device)
+                if want_iters:
+                    o["iters"] = torch.empty((nx, ny, nz), dtype=torch.int32, device=device)
+                if self.W is not None:
+                    o["df"] = torch.empty((nx, ny, nz - len(self.W) + 1), dtype=torch.float32, device=device)
+                return o
+
+            outs = [new_out() for _ in range(max(1, int(out_sets)))]
+            out = outs[0]
             J = jobs[j]
             J.FE = FE.data_ptr()
             J.atoms = rec.data_ptr()
@@ -95,22 +104,37 @@ class BatchPipeline:
             J.df = out["df"].data_ptr() if "df" in out else None
             J.iters = out["iters"].data_ptr() if "iters" in out else None
             self._keep += [xs, ys, zs, rec]
-            self.systems.append(dict(FE=FE, rec=rec, n=n, lvec=lvec, natoms=natoms, ncharged=nch, out=out, scan_shape=(nx, ny, nz), lvecScan=lvecScan))
-        self._jobs = jobs
+            self.systems.append(dict(FE=FE, rec=rec, n=n, lvec=lvec, natoms=natoms, ncharged=nch, out=out, outs=outs, scan_shape=(nx, ny, nz), lvecScan=lvecScan))
+        self._jobs = [jobs]
+        for slot in range(1, len(self.systems[0]["outs"]) if self.systems else 1):
+            js = (BatchJob * len(systems))()
+            ctypes.memmove(js, jobs, ctypes.sizeof(jobs))
+            for j, sysd in enumerate(self.systems):
+                o = sysd["outs"][slot]
+                js[j].fzs = o["fzs"].data_ptr()
+                js[j].ppos = o["ppos"].data_ptr() if "ppos" in o else None
+                js[j].df = o["df"].data_ptr() if "df" in o else None
+                js[j].iters = o["iters"].data_ptr() if "iters" in o else None
+            self._jobs.append(js)
         if torch.device(device).type == "cuda":
             torch.cuda.current_stream().synchronize()  # the atom records are on the device before any stream runs
-        self.handle = ctypes.c_void_p()
         tun = np.ascontiguousarray(self.tuning, dtype=np.int32)
         W = self.W if self.W is not None else np.zeros(1)
-        check(lib().ppgpu_batch_create(ctypes.cast(jobs, ctypes.c_void_p), len(systems), _dp(np.ascontiguousarray(self.prm, dtype=np.float64)), self.Q, Fmax_DEFAULT, 0 if self.W is None else len(self.W), _dp(W), tun.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), ctypes.byref(self.handle)))
+        self.handles = []
+        for js in self._jobs:
+            h = ctypes.c_void_p()
+            self.handles.append(h)
+            check(lib().ppgpu_batch_create(ctypes.cast(js, ctypes.c_void_p), len(systems), _dp(np.ascontiguousarray(self.prm, dtype=np.float64)), self.Q, Fmax_DEFAULT, 0 if self.W is None else len(self.W), _dp(W), tun.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), ctypes.byref(h)))
+        self.handle = self.handles[0]
         info = (ctypes.c_longlong * 4)()
         check(lib().ppgpu_batch_info(self.handle, info))
         self.ff_items, self.strokes, self.ctas, _ = list(info)
+        self.graphs = [None] * len(self.handles)
         self.graph = None
 
     # --------------------------------------------------------------- running
-    def run(self, stream=None):
-        check(lib().ppgpu_batch_run(self.handle, stream_handle(stream)))
+    def run(self, stream=None, slot=0):
+        check(lib().ppgpu_batch_run(self.handles[slot], stream_handle(stream)))
 
     def run_layered(self, net=None, record=None, stream=None):
         """Height-synchronous run: with a WarmStartNet the learned warm start, without it plain
@@ -121,8 +145,17 @@ class BatchPipeline:
 
     def capture(self, fn=None):
         """Records one run (or fn(), e.g. lambda: self.run_layered(net)) in a CUDA graph;
-        replay() launches it."""
-        fn = fn or self.run
+        replay() launches it.  Without fn, every output set gets its graph (replay(slot))."""
+        if fn is None:
+            for slot in range(len(self.handles)):
+                self.graphs[slot] = self._capture(lambda: self.run(slot=slot))
+            self.graph = self.graphs[0]
+            return self.graph
+        self.graph = self._capture(fn)
+        self.graphs[0] = self.graph
+        return self.graph
+
+    def _capture(self, fn):
         torch.cuda.synchronize()
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
@@ -130,15 +163,15 @@ class BatchPipeline:
             fn()  # warm-up outside the capture (lazy module loading, first-use buffers)
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph):
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
             fn()
-        return self.graph
+        return graph
 
-    def replay(self):
-        if self.graph is None:
+    def replay(self, slot=0):
+        if self.graphs[slot] is None:
             self.capture()
-        self.graph.replay()
+        self.graphs[slot].replay()
 
     def iterations(self):
         v = ctypes.c_ulonglong(0)
@@ -149,13 +182,15 @@ class BatchPipeline:
     def pixel_z(self):
         return int(sum(np.prod(s["scan_shape"]) for s in self.systems))
 
-    def outputs(self, j):
-        return self.systems[j]["out"]
+    def outputs(self, j, slot=0):
+        return self.systems[j]["outs"][slot]
 
     def close(self):
-        if getattr(self, "handle", None) is not None and self.handle.value:
-            lib().ppgpu_batch_destroy(self.handle)
-            self.handle = ctypes.c_void_p()
+        for h in getattr(self, "handles", []):
+            if h is not None and h.value:
+                lib().ppgpu_batch_destroy(h)
+        self.handles = []
+        self.handle = ctypes.c_void_p()
 
     def __del__(self):
         try:

@@ -95,6 +95,34 @@ def test_batch_graph_replay(gpulib):
             assert v.equal(first[j][k]), (j, k)
 
 
+def test_batch_output_sets(gpulib):
+    """Two output sets: each slot's launch (and graph) writes its own buffers, equal to the
+    one-set pipeline's; running one slot leaves the other untouched."""
+    import torch
+
+    from ppafm_gb300.batch import BatchPipeline
+
+    systems, params, relax = _batch(nmol=3, seed=9)
+    ref = BatchPipeline(systems, params, relax=relax, want_iters=True)
+    ref.run()
+    bp = BatchPipeline(systems, params, relax=relax, want_iters=True, out_sets=2)
+    bp.run(slot=1)
+    torch.cuda.synchronize()
+    for j in range(len(systems)):
+        assert all(v.data_ptr() != w.data_ptr() for v, w in zip(bp.outputs(j, 0).values(), bp.outputs(j, 1).values()))
+        for k, v in bp.outputs(j, 1).items():
+            assert v.equal(ref.outputs(j)[k]), (j, k)
+        for v in bp.outputs(j, 0).values():
+            v.zero_()
+    bp.capture()
+    bp.replay(0)
+    torch.cuda.synchronize()
+    for j in range(len(systems)):
+        for k, v in bp.outputs(j, 0).items():
+            assert v.equal(ref.outputs(j)[k]), (j, k)
+    bp.close()
+
+
 def test_batch_system_vs_oracle(gpulib, oracle):
     from ppafm_gb300.batch import BatchPipeline
     from tests.conftest import rel_err
