@@ -238,7 +238,77 @@ def computeELFF_pointCharge_atoms(Zs, Rs, Qs, lvec, gridN, parameters, tip="s", 
     if device:
         return ff
     F, E = ff.to_host()
-    return F, (E if computeVpot else None)
+    V = None
+    if computeVpot:
+        V = E
+        if Vmax_DEFAULT is not None:
+            V[V > Vmax_DEFAULT] = Vmax_DEFAULT
+    return F, V
+
+
+# ------------------------------------------------------ file-based stage functions
+
+
+def _load_stage_geometry(geomFile, geometry_format, parameters, FFparams):
+    from . import io
+
+    elem_dict = PPU.getFFdict(FFparams)
+    atoms, nDim, lvec = io.loadGeometry(geomFile, format=geometry_format, parameters=parameters)
+    head = io.primcoords2Xsf(PPU.atoms2iZs(atoms[0], elem_dict), [atoms[1], atoms[2], atoms[3]], lvec)
+    iZs, Rs, Qs = PPU.parseAtoms(atoms, elem_dict, autogeom=False, PBC=parameters.PBC, lvec=lvec, parameters=parameters)
+    n = PPU.autoGridN(parameters) if parameters.gridN[0] <= 0 else parameters.gridN
+    return atoms, nDim, lvec, head, elem_dict, iZs, Rs, Qs, np.array(n, dtype=np.int32)
+
+
+def _finish_stage(ff, computeVpot, Fmax, Vmax, names, save_format, lvec, head, atoms):
+    from . import io
+
+    if Fmax is not None:
+        ff.clamp(Fmax)
+    F, E = ff.to_host()
+    V = None
+    if computeVpot:
+        V = E
+        if Vmax is not None:
+            V[V > Vmax] = Vmax
+    if save_format is not None:
+        io.save_vec_field(names[0], F, lvec, data_format=save_format, head=head, atomic_info=(atoms[:4], lvec))
+        if computeVpot:
+            io.save_scal_field(names[1], V, lvec, data_format=save_format, head=head, atomic_info=(atoms[:4], lvec))
+    return F, V
+
+
+def computeLJ(geomFile, speciesFile, geometry_format=None, save_format=None, computeVpot=False, Fmax=Fmax_DEFAULT, Vmax=Vmax_DEFAULT, ffModel="LJ", parameters=None):
+    """The Lennard-Jones stage of the command-line pipeline (HighLevel.py:260-307): geometry
+    from a file (io.loadGeometry: xyz, xsf, POSCAR, FHI-aims .in), species from speciesFile
+    (the built-in table when it does not exist), in-plane images when PBC, the grid on the GPU,
+    |F| and V clamped, saved as FFLJ_x/y/z (and ELJ) when save_format is 'xsf' or 'npy'.
+    Returns (FF [n0, n1, n2, 3], V or None, grid size, lvec), float64.  Only ffModel 'LJ' (the
+    Morse and vdW models are not part of this library).  parameters: a PpafmParameters; its
+    grid is set from the geometry like the reference's."""
+    if ffModel != "LJ":
+        raise NotImplementedError(f"force-field model {ffModel!r} is not part of this library")
+    FFparams = PPU.loadSpecies(speciesFile)
+    atoms, nDim, lvec, head, elem_dict, iZs, Rs, Qs, n = _load_stage_geometry(geomFile, geometry_format, parameters, FFparams)
+    iPP = PPU.atom2iZ(parameters.probeType, elem_dict)
+    cLJs = PPU.getAtomsLJ(iPP, iZs, FFparams)
+    rec, na, _ = pack_atoms(Rs - lvec[0], cLJs, None)
+    ff = DeviceFF(n, lvec).compute(rec, na, 0, FF_LJ, with_E=computeVpot)
+    F, V = _finish_stage(ff, computeVpot, Fmax, Vmax, ("FF" + ffModel, "E" + ffModel), save_format, lvec, head, atoms)
+    return F, V, nDim, lvec
+
+
+def computeELFF_pointCharge(geomFile, geometry_format=None, tip="s", save_format=None, computeVpot=False, Fmax=Fmax_DEFAULT, Vmax=Vmax_DEFAULT, parameters=None):
+    """The point-charge electrostatics stage (HighLevel.py:353-387): charges from the geometry
+    file, Coulomb grid of the s / pz / dz2 tip on the GPU, clamped, saved as FFel_x/y/z (and
+    Vel).  Returns (FF, V or None, grid size, lvec)."""
+    tipKind = TIP_KINDS[tip]
+    FFparams = PPU.loadSpecies()
+    atoms, nDim, lvec, head, elem_dict, iZs, Rs, Qs, n = _load_stage_geometry(geomFile, geometry_format, parameters, FFparams)
+    rec, na, nch = pack_atoms(Rs - lvec[0], None, Qs * PPU.CoulombConst)
+    ff = DeviceFF(n, lvec).compute(rec, na, nch, FF_COULOMB, kind=tipKind, with_E=computeVpot)
+    F, V = _finish_stage(ff, computeVpot, Fmax, Vmax, ("FFel", "Vel"), save_format, lvec, head, atoms)
+    return F, V, nDim, lvec
 
 
 # ------------------------------------------------------------------- pipeline

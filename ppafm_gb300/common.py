@@ -226,13 +226,33 @@ def Fz2df_tilt(F, d, k0, f0, amplitude=1.0, units=16.0217656):
 # ------------------------------------------------------------- atoms and LJ
 
 
-def PBCAtoms(Zs, Rs, Qs, avec, bvec, na=1, nb=1):
+def PBCAtoms(Zs, Rs, Qs, avec, bvec, na=None, nb=None, parameters=None):
     """In-plane periodic images (common.py:608-628): images ordered i (along a) outer,
-    j (along b) inner, atoms innermost; z unchanged."""
+    j (along b) inner, atoms innermost; z unchanged.  na, nb default to the parameters' nPBC
+    (1, 1 without parameters)."""
+    if na is None:
+        na = parameters.nPBC[0] if parameters is not None else 1
+    if nb is None:
+        nb = parameters.nPBC[1] if parameters is not None else 1
     Rs = np.asarray(Rs, dtype=np.float64)
     shifts = [(i, j) for i in range(-na, na + 1) for j in range(-nb, nb + 1)]
     Rs_ = np.concatenate([np.column_stack([Rs[:, 0] + i * avec[0] + j * bvec[0], Rs[:, 1] + i * avec[1] + j * bvec[1], Rs[:, 2]]) for i, j in shifts])
     return np.tile(np.asarray(Zs), len(shifts)), Rs_, np.tile(np.asarray(Qs, dtype=np.float64), len(shifts))
+
+
+def parseAtoms(atoms, elem_dict, PBC=True, autogeom=False, lvec=None, parameters=None):
+    """(iZs, Rs [n, 3], Qs) of loadGeometry's atom lists (common.py:828-848), replicated in the
+    plane when PBC (cell from lvec, else the parameters' gridA/gridB).  autogeom (the
+    reference's re-centring of the cell on the atoms) is not provided."""
+    if autogeom:
+        raise NotImplementedError("autogeom is not provided")
+    Rs = np.array([atoms[1], atoms[2], atoms[3]], dtype=np.float64).T.copy()
+    iZs = np.zeros(len(atoms[0])) if elem_dict is None else atoms2iZs(atoms[0], elem_dict)
+    Qs = np.array(atoms[4], dtype=np.float64)
+    if PBC:
+        avec, bvec = (lvec[1], lvec[2]) if lvec is not None else (parameters.gridA, parameters.gridB)
+        iZs, Rs, Qs = PBCAtoms(iZs, Rs, Qs, avec=avec, bvec=bvec, parameters=parameters)
+    return iZs, Rs, Qs
 
 
 def PBCAtoms3D_np(Zs, Rs, Qs, cLJs, REAs, lvec, npbc=(1, 1, 1)):

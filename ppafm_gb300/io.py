@@ -69,6 +69,165 @@ def saveXYZ(fname, xyzs, Zs, qs=None, comment="", append=False):
             f.write(line + "\n")
 
 
+def parseLvecASE(comment):
+    """Lattice vectors of an ASE extended-xyz comment line (Lattice="ax ay az bx ... cz"),
+    origin zero, as float32 values like io.py:506-525; None without them."""
+    m = re.match('.*Lattice="\\s*((?:[+-]?(?:[0-9]*\\.)?[0-9]+\\s*){9})"', comment)
+    if not m:
+        return None
+    lvec = np.zeros(12, dtype=np.float32)
+    lvec[3:] = np.array([float(x) for x in m.group(1).split()], dtype=np.float32)
+    return lvec.reshape(4, 3)
+
+
+def loadPOSCAR(file_path):
+    """(xyzs, Zs, lvec) of a VASP POSCAR/CONTCAR file (io.py:154-192): scale, lattice, element
+    names and counts, optional selective-dynamics line, cartesian or direct coordinates."""
+    with open(file_path) as f:
+        f.readline()
+        scale = float(f.readline())
+        lvec = np.zeros((4, 3))
+        for i in range(3):
+            lvec[i + 1] = [float(v) for v in f.readline().split()[:3]]
+        elems = [SYMBOL_TO_Z[e] for e in f.readline().split()]
+        Zs = []
+        for e, n in zip(elems, f.readline().split()):
+            Zs += [e] * int(n)
+        Zs = np.array(Zs, dtype=np.int32)
+        line = f.readline()
+        if line[0] in "Ss":
+            line = f.readline()
+        cartesian = line[0] in "CcKk"
+        xyzs = np.array([[float(v) for v in f.readline().split()[:3]] for _ in range(len(Zs))])
+        lvec *= scale
+        if cartesian:
+            xyzs *= scale
+        else:
+            xyzs = np.outer(xyzs[:, 0], lvec[1]) + np.outer(xyzs[:, 1], lvec[2]) + np.outer(xyzs[:, 2], lvec[3])
+    return xyzs, Zs, lvec
+
+
+def loadGeometryIN(fname):
+    """(xyzs, Zs, lvec or None) of an FHI-aims geometry.in (io.py:126-151)."""
+    Zs, xyzs, lvec = [], [], []
+    with open(fname) as f:
+        for line in f:
+            ws = line.strip().split()
+            if len(ws) == 0 or ws[0][0] == "#":
+                continue
+            if ws[0] == "atom":
+                xyzs.append([float(ws[1]), float(ws[2]), float(ws[3])])
+                Zs.append(SYMBOL_TO_Z[ws[4]])
+            elif ws[0] == "lattice_vector":
+                lvec.append([float(ws[1]), float(ws[2]), float(ws[3])])
+            elif ws[0] == "atom_frac" and len(lvec) == 3:
+                xyzs.append(np.array([float(ws[1]), float(ws[2]), float(ws[3])]) @ np.array(lvec))
+                Zs.append(SYMBOL_TO_Z[ws[4]])
+            elif ws[0] == "trust_radius":
+                break
+    lv = np.stack([[0.0, 0.0, 0.0]] + lvec, axis=0) if lvec else None
+    return np.array(xyzs), np.array(Zs, dtype=np.int32), lv
+
+
+def loadGeometry(fname=None, format=None, parameters=None):
+    """(atoms [Zs, x, y, z, q] lists, grid size, lvec [4, 3]) of a geometry file (io.py:398-503):
+    xyz (with ASE lattice), xsf (PRIMCOORD), POSCAR/CONTCAR or FHI-aims .in.  A missing lattice
+    comes from the parameters; a zero lattice vector becomes one that encloses the scan window
+    (probe offset included) with 3 A of padding and switches PBC off; a grid size that is not
+    positive becomes 10 points per A.  The parameters' grid (gridO/A/B/C, gridN) is set to the
+    result, as in the reference.  CUBE and npy geometries are not read here."""
+    import copy
+
+    if fname is None:
+        raise ValueError("Please provide the name of the file with coordinates")
+    if parameters is None:
+        raise ValueError("Please provide the parameters dictionary here")
+    fname = str(fname)
+    if format is None or format == "":
+        low = fname.lower()
+        for ext, fmt in ((".xyz", "xyz"), (".cube", "cube"), (".xsf", "xsf"), (".npy", "npy")):
+            if low.endswith(ext):
+                format = fmt
+        if low.endswith(".in") or low.endswith(".in.next_step"):
+            format = "in"
+        base = fname.replace("\\", "/").split("/")[-1]
+        if base.startswith("POSCAR") or base.startswith("CONTCAR"):
+            format = "poscar"
+    else:
+        format = format.lower()
+    xyzs = Zs = qs = None
+    nDim = None
+    if format == "xyz":
+        xyzs, Zs, qs, comment = loadXYZ(fname)
+        lvec = parseLvecASE(comment)
+    elif format == "xsf":
+        atoms, nDim, lvec = loadXSFGeom(fname)
+    elif format == "poscar":
+        xyzs, Zs, lvec = loadPOSCAR(fname)
+    elif format == "in":
+        xyzs, Zs, lvec = loadGeometryIN(fname)
+    elif format in ("cube", "npy"):
+        raise NotImplementedError(f"{format} geometries are not read by this library")
+    elif format is None:
+        raise ValueError("ERROR!!! Input geometry format was neither specified nor could it be determined automatically.")
+    else:
+        raise ValueError("ERROR!!! Unknown format %s of input geometry." % (format))
+    if xyzs is not None:
+        if qs is None:
+            qs = np.zeros(len(Zs))
+        atoms = [list(Zs), list(xyzs[:, 0]), list(xyzs[:, 1]), list(xyzs[:, 2]), list(qs)]
+        nDim = np.array(parameters.gridN)
+    nDim = np.array(nDim)
+    if lvec is None or len(lvec) == 0:
+        lvec = np.zeros((4, 3))
+        lvec[0, :] = copy.copy(parameters.gridO)
+        lvec[1, :] = copy.copy(parameters.gridA)
+        lvec[2, :] = copy.copy(parameters.gridB)
+        lvec[3, :] = copy.copy(parameters.gridC)
+    else:
+        lvec = [list(v) for v in lvec]
+        if len(lvec) == 1:
+            lvec.append(list(parameters.gridA))
+        if len(lvec) == 2:
+            lvec.append(list(parameters.gridB))
+        if len(lvec) == 3:
+            lvec.append(list(parameters.gridC))
+    lvec = np.array(lvec, dtype=np.float64)
+    probe_min = np.array(parameters.scanMin, dtype=np.float64)
+    probe_max = np.array(parameters.scanMax, dtype=np.float64)
+    r0 = parameters.r0Probe
+    probe_min += (r0[0], r0[1], -r0[2])
+    probe_max += (r0[0], r0[1], -r0[2])
+    pad, default_grid_step = 3.0, 0.1
+    for i in range(3):
+        if np.allclose(lvec[i + 1, :], 0):
+            parameters.PBC = False
+            lvec[i + 1, i] = probe_max[i] - probe_min[i] + 2 * pad
+            lvec[0, i] = probe_min[i] - pad
+        if not nDim[i] > 0:
+            nDim[i] = round(np.linalg.norm(lvec[i + 1, :]) / default_grid_step)
+    for i in range(3):
+        parameters.gridO[i] = lvec[0][i]
+        parameters.gridA[i] = lvec[1][i]
+        parameters.gridB[i] = lvec[2][i]
+        parameters.gridC[i] = lvec[3][i]
+    parameters.gridN = nDim
+    return atoms, nDim, lvec
+
+
+def primcoords2Xsf(iZs, xyzs, lvec):
+    """The XSF header (cell and PRIMCOORD atoms) the command-line stages write in front of their
+    grids (io.py:323-346)."""
+    lines = ["CRYSTAL", "PRIMVEC"]
+    lines += [f"{lvec[k][0]:f} {lvec[k][1]:f} {lvec[k][2]:f}" for k in (1, 2, 3)]
+    lines += ["CONVVEC"]
+    lines += [f"{lvec[k][0]:f} {lvec[k][1]:f} {lvec[k][2]:f}" for k in (1, 2, 3)]
+    lines += ["PRIMCOORD", "%i 1" % len(iZs)]
+    lines += ["%i %5.6f %5.6f %5.6f" % (iZs[i], xyzs[0][i], xyzs[1][i], xyzs[2][i]) for i in range(len(iZs))]
+    lines += ["", "BEGIN_BLOCK_DATAGRID_3D", "some_datagrid", "BEGIN_DATAGRID_3D_whatever"]
+    return "\n".join(lines) + "\n"
+
+
 # --------------------------------------------------------------------- grid files
 # XSF datagrids and npz grids of ppafm/io.py:563-620, 716-880: the files the reference's
 # command-line stages hand to each other (force fields, Fz and Δf stacks).  A datagrid has

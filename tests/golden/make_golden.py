@@ -45,6 +45,7 @@ def main(ref_root="/root/reference", only=None):
             make_xsf(tmp)
             make_tilt(tmp)
             make_params(ref_root)
+            make_stages(tmp)
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         return
@@ -249,6 +250,64 @@ def make_params(ref_root):
     with open(os.path.join(out, "parsed.json"), "w") as f:
         json.dump({"parsed": parsed, "default": default}, f, indent=1)
     print("params fixtures written")
+
+
+def make_stages(tmp):
+    """The file-based force-field stages (HighLevel.computeLJ, computeELFF_pointCharge,
+    io.loadGeometry) of the reference on small seeded inputs -> tests/golden/stages/: an xyz
+    molecule with charges, a POSCAR and an FHI-aims geometry.in, the parameters, the grids the
+    stages return and what loadGeometry parses."""
+    import json
+
+    import ppafm.common as PPU
+    import ppafm.HighLevel as HL
+    import ppafm.io as pio
+
+    out = os.path.join(HERE, "stages")
+    os.makedirs(out, exist_ok=True)
+    rng = np.random.default_rng(31)
+    n = 14
+    xyz = np.column_stack([rng.uniform(2.5, 6.5, n), rng.uniform(2.5, 6.5, n), rng.uniform(-0.3, 0.3, n)])
+    Zs = rng.choice([1, 6, 7, 8], n)
+    q = rng.uniform(-0.3, 0.3, n)
+    q -= q.mean()
+    sym = {1: "H", 6: "C", 7: "N", 8: "O"}
+    with open(os.path.join(out, "mol.xyz"), "w") as f:
+        f.write(f"{n}\nseeded molecule\n")
+        for i in range(n):
+            f.write(f"{sym[int(Zs[i])]} {xyz[i,0]:.6f} {xyz[i,1]:.6f} {xyz[i,2]:.6f} {q[i]:.6f}\n")
+    ini = "probeType 8\ncharge -0.05\ngridA 9.0 0.0 0.0\ngridB 0.0 9.6 0.0\ngridC 0.0 0.0 8.0\ngridO 0.0 0.0 -3.0\ngridN 24 26 20\nnPBC 1 1 0\nscanMin 1.0 1.0 5.0\nscanMax 8.0 8.0 7.0\n"
+    with open(os.path.join(out, "params.ini"), "w") as f:
+        f.write(ini)
+    cwd = os.getcwd()
+    os.chdir(tmp)
+    try:
+        p = PPU.PpafmParameters.from_file(os.path.join(out, "params.ini"))
+        FF, V, nDim, lvec = HL.computeLJ(os.path.join(out, "mol.xyz"), None, computeVpot=True, parameters=p)
+        FF, V = FF.copy(), V.copy()
+        p = PPU.PpafmParameters.from_file(os.path.join(out, "params.ini"))
+        FE, VE, _, _ = HL.computeELFF_pointCharge(os.path.join(out, "mol.xyz"), tip="dz2", computeVpot=True, parameters=p)
+        FE, VE = FE.copy(), VE.copy()
+    finally:
+        os.chdir(cwd)
+    f32 = np.float32  # the GPU grids are float32; float32 copies keep the fixture small
+    np.savez_compressed(os.path.join(out, "grids.npz"), F_lj=FF.astype(f32), E_lj=V.astype(f32), F_el=FE.astype(f32), E_el=VE.astype(f32), nDim=np.array(nDim), lvec=np.array(lvec))
+    # geometry files: POSCAR (direct coordinates) and geometry.in, parsed by the reference
+    with open(os.path.join(out, "POSCAR"), "w") as f:
+        f.write("seeded cell\n1.5\n4.0 0.0 0.0\n0.5 5.0 0.0\n0.0 0.0 6.0\nC O H\n2 1 1\nDirect\n")
+        for r in rng.uniform(0, 1, (4, 3)):
+            f.write(f"{r[0]:.6f} {r[1]:.6f} {r[2]:.6f}\n")
+    with open(os.path.join(out, "geometry.in"), "w") as f:
+        f.write("# seeded\nlattice_vector 7.0 0.0 0.0\nlattice_vector 0.0 8.0 0.0\nlattice_vector 0.0 0.0 9.0\n")
+        f.write("atom 1.0 2.0 3.0 C\natom 2.5 2.0 3.0 O\natom_frac 0.5 0.25 0.1 N\n")
+    parsed = {}
+    for name in ("POSCAR", "geometry.in", "mol.xyz"):
+        p = PPU.PpafmParameters.from_file(os.path.join(out, "params.ini"))
+        atoms, nD, lv = pio.loadGeometry(os.path.join(out, name), format="poscar" if name == "POSCAR" else None, parameters=p)
+        parsed[name] = {"atoms": [[float(x) for x in a] for a in atoms], "nDim": [int(x) for x in nD], "lvec": np.asarray(lv, dtype=np.float64).tolist(), "PBC": bool(p.PBC), "gridN": [int(x) for x in p.gridN]}
+    with open(os.path.join(out, "geometry.json"), "w") as f:
+        json.dump(parsed, f, indent=1)
+    print("stage fixtures written")
 
 
 if __name__ == "__main__":

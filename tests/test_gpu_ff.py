@@ -203,3 +203,33 @@ def test_bad_arguments_raise(gpulib):
         ff.compute(atoms, na, 0, D.FF_COULOMB, kind=7)
     with pytest.raises(PPGPUError):
         D.DeviceFF((8, 8, 8), np.zeros((3, 3))).compute(atoms, na, 0, D.FF_LJ)
+
+
+def test_file_stages_vs_reference(gpulib, tmp_path, monkeypatch):
+    """HighLevel.computeLJ / computeELFF_pointCharge from a geometry file (HighLevel.py:260-307,
+    353-387) against the reference's own stages on the same xyz and parameters
+    (tests/golden/stages), and the files they save."""
+    import os
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import common, io
+
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "stages")
+    g = np.load(os.path.join(gold, "grids.npz"))
+    monkeypatch.chdir(tmp_path)  # the stages save into the working directory, like the reference
+    p = common.PpafmParameters.from_file(os.path.join(gold, "params.ini"))
+    F, V, nDim, lvec = HL.computeLJ(os.path.join(gold, "mol.xyz"), None, save_format="xsf", computeVpot=True, parameters=p)
+    assert tuple(nDim) == tuple(g["nDim"]) and np.allclose(lvec, g["lvec"])
+    ok = np.linalg.norm(g["F_lj"], axis=-1) < 1e30
+    assert rel_err(F[ok], g["F_lj"][ok].astype(np.float64), FLOOR) < TOL
+    assert np.abs(V - g["E_lj"]).max() <= 1e-4 * max(1.0, np.abs(g["E_lj"]).max())
+    p = common.PpafmParameters.from_file(os.path.join(gold, "params.ini"))
+    F, V, _, _ = HL.computeELFF_pointCharge(os.path.join(gold, "mol.xyz"), tip="dz2", save_format="npy", computeVpot=True, parameters=p)
+    assert rel_err(F, g["F_el"].astype(np.float64), FLOOR) < TOL
+    assert np.abs(V - g["E_el"]).max() <= 1e-4 * max(1.0, np.abs(g["E_el"]).max())
+    Fx, lv, _, _ = io.loadXSFData("FFLJ_x.xsf")
+    assert Fx.shape == tuple(g["nDim"]) and np.allclose(lv, g["lvec"], atol=1e-6)
+    atoms, _, _ = io.loadXSFGeom("ELJ.xsf")  # the header: the file's atoms (without images)
+    assert len(atoms[0]) == 14
+    d = np.load("FFel.npz")
+    assert np.allclose(d["FF"], F)

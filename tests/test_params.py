@@ -89,3 +89,29 @@ def test_afmulator_parameter_files(tmp_path):
     # a symbol as probe type
     (tmp_path / "xe.ini").write_text("probeType Xe\n")
     assert AFMulator.from_params(tmp_path / "xe.ini").iZPP == 54
+
+
+def test_load_geometry_vs_reference():
+    """io.loadGeometry (io.py:398-503) on an xyz with charges, a POSCAR in direct coordinates and
+    an FHI-aims geometry.in: atoms, grid size, lattice and the parameters it sets, as the
+    reference parsed them (tests/golden/stages/geometry.json)."""
+    from ppafm_gb300 import common, io
+
+    gold = os.path.join(HERE, "golden", "stages")
+    ref = json.load(open(os.path.join(gold, "geometry.json")))
+    for name, r in ref.items():
+        p = common.PpafmParameters.from_file(os.path.join(gold, "params.ini"))
+        atoms, nD, lv = io.loadGeometry(os.path.join(gold, name), parameters=p)
+        assert [int(z) for z in atoms[0]] == [int(z) for z in r["atoms"][0]], name
+        for k in range(1, 5):
+            assert np.allclose(atoms[k], r["atoms"][k], rtol=1e-12, atol=1e-12), (name, k)
+        assert list(nD) == r["nDim"] and np.allclose(lv, r["lvec"], rtol=1e-7) and p.PBC == r["PBC"], name
+        assert [int(x) for x in p.gridN] == r["gridN"]
+        assert np.allclose([p.gridO, p.gridA, p.gridB, p.gridC], r["lvec"], rtol=1e-7)
+    # a zero cell vector: made to enclose the scan window with 3 A padding, PBC off
+    p = common.PpafmParameters.from_file(os.path.join(gold, "params.ini"))
+    p.gridC = [0.0, 0.0, 0.0]
+    _, nD, lv = io.loadGeometry(os.path.join(gold, "mol.xyz"), parameters=p)
+    assert p.PBC is False and np.isclose(lv[3, 2], (7.0 - 4.0) - (5.0 - 4.0) + 6.0) and np.isclose(lv[0, 2], 5.0 - 4.0 - 3.0)
+    head = io.primcoords2Xsf([6, 8], [[0.0, 1.0], [0.5, 1.5], [0.25, 0.75]], lv)
+    assert "PRIMCOORD\n2 1\n6 0.000000 0.500000 0.250000\n8 1.000000 1.500000 0.750000\n" in head
