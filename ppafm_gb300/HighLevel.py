@@ -311,6 +311,36 @@ def computeELFF_pointCharge(geomFile, geometry_format=None, tip="s", save_format
     return F, V, nDim, lvec
 
 
+def computeElFF(V, lvec, nDim, tip, computeVpot=False, tilt=0.0, sigma=None, deleteV=True, parameters=None):
+    """Electrostatic force field of a Hartree potential V [n0, n1, n2] and the tip charge
+    density (HighLevel.py:390-411) by FFT on the GPU: tip a multipole name ('s', 'pz', 'dz2',
+    ...) or dict (Gaussian of width sigma, the parameters' sigma by default), a density array
+    on V's grid, or an XSF file of the tip's electron density (negated into a charge density).
+    Returns (FF [n0, n1, n2, 3], V_out or None), float64."""
+    from . import fieldFFT as fFFT
+    from . import io
+
+    rho = None
+    multipole = None
+    if sigma is None:
+        sigma = _get(parameters, "sigma", 0.7)
+    if isinstance(tip, (list, np.ndarray)):
+        rho = tip
+    elif isinstance(tip, dict):
+        multipole = tip
+    elif tip in {"s", "px", "py", "pz", "dx2", "dy2", "dz2", "dxy", "dxz", "dyz"}:
+        multipole = {tip: 1.0}
+    elif str(tip).endswith(".xsf"):
+        rho, _, nDim_tip, _ = io.loadXSFData(tip)
+        if any(np.asarray(nDim_tip) != np.asarray(nDim)):
+            raise ValueError("Input file for tip charge density has been specified, but the dimensions are incompatible with the Hartree potential file!")
+        rho = -rho  # charge density from the electron density
+    else:
+        raise ValueError(f"unknown tip {tip!r}")
+    Fx, Fy, Fz, Vout = fFFT.potential2forces_mem(V, lvec, nDim, rho=rho, sigma=sigma, multipole=multipole, doPot=computeVpot, tilt=tilt, deleteV=deleteV)
+    return io.packVecGrid(Fx, Fy, Fz), Vout
+
+
 # ------------------------------------------------------------------- pipeline
 
 

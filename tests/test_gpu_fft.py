@@ -86,6 +86,22 @@ def test_potential2forces_mem_dropin(gpulib, golden):
     assert e is None and _close(fz, g["skew_odd_mFz"])[0]
     with pytest.raises(ValueError):
         fieldFFT.potential2forces_mem(V[:-1], lv, np.array(V.shape), rho=rho)
+    # HighLevel.computeElFF (HighLevel.py:390-411): the same with a density array, a multipole
+    # dict and an XSF tip-density file (its electron density negated)
+    import os
+    import tempfile
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import io
+
+    FF, E = HL.computeElFF(V, lv, np.array(V.shape), rho, computeVpot=True)
+    assert _close(FF[..., 2], g["skew_odd_Fz"])[0] and _close(E, g["skew_odd_E"])[0]
+    FF, E = HL.computeElFF(V, lv, np.array(V.shape), {"s": 1.0, "dz2": -0.3}, sigma=0.7)
+    assert E is None and _close(FF[..., 2], g["skew_odd_mFz"])[0]
+    d = tempfile.mkdtemp()
+    io.saveXSFData(os.path.join(d, "tip.xsf"), -rho, lv)
+    FF, _ = HL.computeElFF(V, lv, np.array(V.shape), os.path.join(d, "tip.xsf"))
+    assert np.abs(FF[..., 2] - g["skew_odd_Fz"]).max() <= 1e-4 * np.abs(g["skew_odd_Fz"]).max()  # the file keeps 6 digits
 
 
 @pytest.mark.parametrize("mp", [None, {"s": 1.0}, {"px": 1.0}, {"py": 0.7}, {"pz": -1.0}, {"dz2": 1.0}, {"dx2": 0.5}, {"dy2": 0.5}, {"dxy": 1.0}, {"dxz": 1.0}, {"dyz": 1.0}, {"s": 1.0, "dz2": -0.3}])
