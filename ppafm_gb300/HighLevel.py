@@ -159,6 +159,10 @@ def perform_relaxation(lvec, FFLJ, FFel=None, FFpauli=None, FFboltz=None, FFkpfm
         FF += FFpauli * _get(parameters, "Apauli")
     if FFboltz is not None:
         FF += FFboltz
+    if bFFtotDebug:
+        from . import io
+
+        io.save_vec_field("FFtotDebug", FF, lvec)
     ff = DeviceFF(FF.shape[:3], lvec).from_host_f64(FF.reshape(-1, 3))
     prm = tip_vector(parameters, relax)
     with tip_spline_ctx(tip_spline):
