@@ -139,6 +139,16 @@ class AFMulator:
         self.B_pauli = B_pauli
         self._rho_dev = None
 
+    def setBPauli(self, B_pauli=1.0):
+        """Pauli density exponent (AFMulator.py:286-288): only 1 here (other exponents belong
+        to FDBM)."""
+        self.setRho(self.rho, sigma=self.sigma, B_pauli=B_pauli)
+
+    def setRhoDelta(self, rho_delta=None):
+        """FDBM tip delta density (AFMulator.py:290-307): not supported; None is accepted."""
+        if rho_delta is not None:
+            raise NotImplementedError("tip delta densities (FDBM) are not supported")
+
     def _tip_density(self):
         """The tip density on the force-field grid (device, cached)."""
         if self._rho_dev is not None:
@@ -370,6 +380,21 @@ class AFMulator:
     def downloadFF(self):
         """The force field as [nx, ny, nz, 4] float32 (Fx, Fy, Fz, E)."""
         return self._ff.grid4.cpu().numpy()
+
+    def plot_images(self, X, outdir="afm_images", prefix="df", **plot_kwargs):
+        """The reference plots the Δf stack into outdir (AFMulator.py:609-640); this library has
+        no plotting and saves it as <prefix>.npz there instead (X with heights top-down, the tip
+        heights at mid-oscillation and the image extent, as the plots are labelled), with a
+        warning."""
+        import os
+        import warnings
+
+        os.makedirs(outdir, exist_ok=True)
+        zTips = np.linspace(self.scan_window[0][2], self.scan_window[1][2] - self.df_steps * self.dz, self.scan_dim[2] - self.df_steps + 1) + self.amplitude / 2
+        extent = [self.scan_window[0][0], self.scan_window[1][0], self.scan_window[0][1], self.scan_window[1][1]]
+        path = os.path.join(outdir, f"{prefix}.npz")
+        np.savez(path, X=np.asarray(X)[:, :, ::-1], zTips=zTips, extent=np.array(extent))
+        warnings.warn(f"plotting is not part of this library; the images are saved as {path}")
 
     # ------------------------------------------------------------ parameter files
 

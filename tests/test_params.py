@@ -89,6 +89,18 @@ def test_afmulator_parameter_files(tmp_path):
     # a symbol as probe type
     (tmp_path / "xe.ini").write_text("probeType Xe\n")
     assert AFMulator.from_params(tmp_path / "xe.ini").iZPP == 54
+    # no plotting: plot_images saves the stack (heights top-down) with its tip heights
+    X = np.arange(121 * 121 * 21, dtype=np.float32).reshape(121, 121, 21)
+    with warnings.catch_warnings(record=True):
+        warnings.simplefilter("always")
+        afm.plot_images(X, outdir=str(tmp_path / "img"))
+    z = np.load(tmp_path / "img" / "df.npz")
+    assert np.array_equal(z["X"], X[:, :, ::-1]) and len(z["zTips"]) == 21 and np.isclose(z["zTips"][0], 7.0 + afm.amplitude / 2)
+    afm.setRhoDelta(None)
+    with pytest.raises(NotImplementedError):
+        afm.setRhoDelta({"s": 1.0})
+    with pytest.raises(NotImplementedError):
+        afm.setBPauli(1.2)
 
 
 def test_load_geometry_vs_reference():
