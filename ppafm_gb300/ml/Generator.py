@@ -329,6 +329,10 @@ class GeneratorAFMtrainer:
         sw = self.scan_window
         self.scan_window = ((sw[0][0], sw[0][1], z_min), (sw[1][0], sw[1][1], z_min + self.scan_size[2]))
 
+    def set_fdbm_parameters(self, A_pauli, B_pauli):
+        """FDBM Pauli parameters (ppafm/ml/Generator.py:617-635); the reference does nothing
+        unless the simulation type is FDBM, which this library does not provide."""
+
     def randomize_df_steps(self, minimum=4, maximum=20):
         """Random number of Δf steps, keeping the output z size and the z step."""
         self.df_steps = np.random.randint(minimum, maximum + 1)
