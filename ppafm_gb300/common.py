@@ -223,6 +223,84 @@ def Fz2df_tilt(F, d, k0, f0, amplitude=1.0, units=16.0217656):
     return (comps[0] * d[0] + comps[1] * d[1] + comps[2] * d[2]) * units * f0 / k0
 
 
+# ------------------------------------------------------------------ rotations
+
+
+def rotation_matrix(axis, theta):
+    """Counterclockwise rotation by theta about axis (common.py:448-466), from the unit
+    quaternion (cos(theta/2), -axis sin(theta/2)) in the reference's sign convention."""
+    axis = np.asarray(axis, dtype=np.float64)
+    axis = axis / np.sqrt(np.dot(axis, axis))
+    a = np.cos(theta / 2.0)
+    b, c, d = -axis * np.sin(theta / 2.0)
+    return np.array(
+        [
+            [a * a + b * b - c * c - d * d, 2 * (b * c + a * d), 2 * (b * d - a * c)],
+            [2 * (b * c - a * d), a * a + c * c - b * b - d * d, 2 * (c * d + a * b)],
+            [2 * (b * d + a * c), 2 * (c * d - a * b), a * a + d * d - b * b - c * c],
+        ]
+    )
+
+
+def makeRotJitter(n=10, maxAngle=0.3):
+    """50 random small rotations, angle up to maxAngle about random axes (common.py:469-476;
+    like the reference, n is not used)."""
+    r = (np.random.rand(50, 4) - 0.5) * 2
+    return [rotation_matrix(r[i, :3] / np.sqrt(np.dot(r[i, :3], r[i, :3])), r[i, 3] * maxAngle) for i in range(50)]
+
+
+def genRotations(axis, thetas):
+    return np.array([rotation_matrix(axis, t) for t in thetas])
+
+
+def sphereTangentSpace(n=100):
+    """n orthonormal frames whose third rows are a golden-angle spiral over the sphere, the
+    first row horizontal (common.py:483-497)."""
+    theta = np.pi * (3.0 - np.sqrt(5.0)) * np.arange(n)
+    z = np.linspace(1.0 - 1.0 / n, 1.0 / n - 1.0, n)
+    r = np.sqrt(1.0 - z * z)
+    c, s_ = np.cos(theta), np.sin(theta)
+    rots = np.zeros((n, 3, 3))
+    rots[:, 2] = np.stack([r * c, r * s_, z], axis=-1)
+    rots[:, 0, 0] = -s_
+    rots[:, 0, 1] = c
+    rots[:, 1, :] = np.cross(rots[:, 2, :], rots[:, 0, :])
+    return rots
+
+
+def maxAlongDir(atoms, hdir):
+    """(index, height) of the atom highest along hdir (common.py:500-503)."""
+    x = np.dot(atoms[:, :3], np.asarray(hdir)[:, None])
+    i = np.argmax(x)
+    return i, x[i][0]
+
+
+def maxAlongDirEntropy(atoms, hdir, beta=1.0):
+    """maxAlongDir plus sum exp(beta (x - x_max)) over the atoms (common.py:506-510)."""
+    x = np.dot(atoms[:, :3], np.asarray(hdir)[:, None])
+    i = np.argmax(x)
+    return i, x[i][0], np.sum(np.exp(beta * (x - x[i])))
+
+
+def multRot(Zs, Rs, Qs, cLJs, rots, cog=(0, 0, 0)):
+    """The atoms once per rotation about cog, rotations outer (common.py:779-802)."""
+    Rs = np.asarray(Rs, dtype=np.float64)
+    cog = np.asarray(cog, dtype=np.float64)
+    R = np.concatenate([(Rs - cog) @ np.asarray(rot, dtype=np.float64).T + cog for rot in rots])
+    m = len(rots)
+    return np.tile(np.asarray(Zs), m), R, np.tile(np.asarray(Qs), m), np.tile(np.asarray(cLJs), (m, 1))
+
+
+def wrapAtomsCell(Rs, da, db, avec, bvec):
+    """Wraps Rs in place into the in-plane cell (avec, bvec), shifted by (da, db) cell
+    fractions (common.py:596-605)."""
+    M = np.array((avec[:2], bvec[:2]), dtype=np.float64)
+    AB = np.dot(Rs[:, :2], np.linalg.inv(M))
+    AB[:, 0] = (AB[:, 0] + 10 + da) % 1.0
+    AB[:, 1] = (AB[:, 1] + 10 + db) % 1.0
+    Rs[:, :2] = np.dot(AB, M)
+
+
 # ------------------------------------------------------------- atoms and LJ
 
 
@@ -253,6 +331,31 @@ def parseAtoms(atoms, elem_dict, PBC=True, autogeom=False, lvec=None, parameters
         avec, bvec = (lvec[1], lvec[2]) if lvec is not None else (parameters.gridA, parameters.gridB)
         iZs, Rs, Qs = PBCAtoms(iZs, Rs, Qs, avec=avec, bvec=bvec, parameters=parameters)
     return iZs, Rs, Qs
+
+
+def PBCAtoms3D(Zs, Rs, Qs, cLJs, lvec, npbc=(1, 1, 1)):
+    """3-D periodic images (common.py:631-664): the atoms, then every other image (a outer, c
+    inner).  Like the reference, the returned cLJs hold the images only (not the home cell)."""
+    Rs = np.asarray(Rs, dtype=np.float64)
+    lvec = np.asarray(lvec, dtype=np.float64)
+    shifts = [(a, b, c) for a in range(-npbc[0], npbc[0] + 1) for b in range(-npbc[1], npbc[1] + 1) for c in range(-npbc[2], npbc[2] + 1) if (a, b, c) != (0, 0, 0)]
+    R = np.concatenate([Rs] + [Rs + (a * lvec[0] + b * lvec[1] + c * lvec[2]) for a, b, c in shifts])
+    m = len(shifts)
+    cl = np.tile(np.asarray(cLJs), (m, 1)) if m else np.zeros((0, np.shape(cLJs)[1]))
+    return np.tile(np.asarray(Zs), m + 1), R, np.tile(np.asarray(Qs), m + 1), cl
+
+
+def getSampleAtomsREA(iZs, FFparams):
+    """(R, E, alpha) of every atom's species (common.py:895-896)."""
+    return np.array([(FFparams[i - 1][0], FFparams[i - 1][1], FFparams[i - 1][2]) for i in iZs])
+
+
+def getAtomsRE(iZprobe, iZs, FFparams):
+    """(R_ij, sqrt(E_i E_j)) pair parameters of the Morse model (common.py:899-905)."""
+    Rpp, Epp = FFparams[iZprobe - 1][0], FFparams[iZprobe - 1][1]
+    REs = np.array([(Rpp + FFparams[z - 1][0], Epp * FFparams[z - 1][1]) for z in iZs])
+    REs[:, 1] = np.sqrt(REs[:, 1])
+    return REs
 
 
 def PBCAtoms3D_np(Zs, Rs, Qs, cLJs, REAs, lvec, npbc=(1, 1, 1)):
@@ -315,8 +418,16 @@ def REA2LJ(cREAs, cLJs=None):
     return cLJs
 
 
-def prepareScanGrids(scanMin, scanMax, scanStep, r0Probe):
-    """Tip positions and the scan-output lattice (common.py:922-946)."""
+def prepareScanGrids(scanMin=None, scanMax=None, scanStep=None, r0Probe=None, parameters=None):
+    """Tip positions and the scan-output lattice (common.py:922-946).  Called like the
+    reference with the parameters object (``prepareScanGrids(parameters)`` or
+    ``prepareScanGrids(parameters=p)``: its scanMin, scanMax, scanStep, r0Probe), or with the
+    four values."""
+    if parameters is None and scanMax is None and scanMin is not None and not np.ndim(scanMin):
+        parameters, scanMin = scanMin, None  # prepareScanGrids(parameters)
+    if parameters is not None:
+        g = (lambda k: parameters[k]) if isinstance(parameters, dict) else (lambda k: getattr(parameters, k))
+        scanMin, scanMax, scanStep, r0Probe = g("scanMin"), g("scanMax"), g("scanStep"), g("r0Probe")
     xTips = np.arange(scanMin[0], scanMax[0] + 0.5 * scanStep[0], scanStep[0])
     yTips = np.arange(scanMin[1], scanMax[1] + 0.5 * scanStep[1], scanStep[1])
     zTips = np.arange(scanMin[2], scanMax[2] + 0.5 * scanStep[2], scanStep[2])
@@ -329,6 +440,18 @@ def prepareScanGrids(scanMin, scanMax, scanStep, r0Probe):
         ]
     )
     return xTips, yTips, zTips, lvecScan
+
+
+def lvec2params(parameters, lvec):
+    """The cell vectors of lvec [4, 3] into the parameters' gridA/B/C (common.py:949-952)."""
+    parameters.gridA = np.array(lvec[1, :], dtype=np.float64)
+    parameters.gridB = np.array(lvec[2, :], dtype=np.float64)
+    parameters.gridC = np.array(lvec[3, :], dtype=np.float64)
+
+
+def params2lvec(parameters):
+    """lvec [4, 3] with origin 0 and the parameters' gridA/B/C (common.py:955-964)."""
+    return np.array([[0.0, 0.0, 0.0], parameters.gridA, parameters.gridB, parameters.gridC], dtype=np.float64)
 
 
 def genFFSampling(lvec, pixPerAngstrome=10):

@@ -355,16 +355,8 @@ class GeneratorAFMtrainer:
         """Run before every image."""
 
 
-def maxAlongDirEntropy(atoms, hdir, beta=1.0):
-    """(index, height, entropy) of the atoms' projection on hdir (common.py:506-510)."""
-    xdir = np.dot(atoms[:, :3], hdir[:, None])
-    imin = np.argmax(xdir)
-    entropy = np.sum(np.exp(beta * (xdir - xdir[imin])))
-    return imin, xdir[imin][0], entropy
-
-
 def sortRotationsByEntropy(xyzs, rotations):
-    scored = [(maxAlongDirEntropy(xyzs, np.asarray(rot)[2].ravel().copy())[2], rot) for rot in rotations]
+    scored = [(PPU.maxAlongDirEntropy(xyzs, np.asarray(rot)[2].ravel().copy())[2], rot) for rot in rotations]
     scored.sort(key=lambda item: -item[0])
     return [rot for _, rot in scored]
 

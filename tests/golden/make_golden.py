@@ -46,6 +46,7 @@ def main(ref_root="/root/reference", only=None):
             make_tilt(tmp)
             make_params(ref_root)
             make_stages(tmp)
+            make_helpers(tmp)
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         return
@@ -308,6 +309,44 @@ def make_stages(tmp):
     with open(os.path.join(out, "geometry.json"), "w") as f:
         json.dump(parsed, f, indent=1)
     print("stage fixtures written")
+
+
+def make_helpers(tmp):
+    """Host helpers of ppafm/common.py (rotations, sphere frames, image replication, wrapping,
+    pair parameters) on seeded inputs -> tests/golden/helpers.npz."""
+    import ppafm.common as PPU
+
+    rng = np.random.default_rng(55)
+    n = 7
+    Zs = rng.choice([1, 6, 7, 8, 17], n)
+    Rs = rng.uniform(-3, 3, (n, 3))
+    Qs = rng.uniform(-0.3, 0.3, n)
+    FF = PPU.loadSpecies()
+    cLJs = PPU.getAtomsLJ(8, Zs, FF)
+    lvec3 = np.array([[5.0, 0.0, 0.0], [1.0, 6.0, 0.0], [0.0, 0.5, 7.0]])
+    axis = np.array([0.3, -0.4, 0.8])
+    thetas = np.array([0.1, 1.2, -2.5])
+    rots = PPU.genRotations(axis, thetas)
+    out = dict(Zs=Zs, Rs=Rs, Qs=Qs, cLJs=cLJs, lvec3=lvec3, axis=axis, thetas=thetas)
+    out["rot"] = PPU.rotation_matrix(axis, 0.7)
+    out["rots"] = rots
+    out["sphere"] = PPU.sphereTangentSpace(11)
+    hdir = np.array([0.1, 0.2, 0.97])
+    out["hdir"] = hdir
+    i, h = PPU.maxAlongDir(Rs, hdir)
+    i2, h2, e2 = PPU.maxAlongDirEntropy(Rs, hdir, beta=0.7)
+    out["maxdir"] = np.array([i, h, i2, h2, e2])
+    z, r, q, c = PPU.multRot(Zs, Rs, Qs, cLJs, rots, cog=(0.5, -0.5, 0.2))
+    out.update(mr_Z=z, mr_R=r, mr_Q=q, mr_c=c)
+    z, r, q, c = PPU.PBCAtoms3D(Zs, Rs, Qs, cLJs, lvec3, npbc=[1, 1, 0])
+    out.update(p3_Z=z, p3_R=r, p3_Q=q, p3_c=c)
+    W = Rs.copy()
+    PPU.wrapAtomsCell(W, 0.25, -0.1, lvec3[0], lvec3[1])
+    out["wrapped"] = W
+    out["sREA"] = PPU.getSampleAtomsREA(Zs, FF)
+    out["RE"] = PPU.getAtomsRE(8, Zs, FF)
+    np.savez(os.path.join(HERE, "helpers.npz"), **out)
+    print("helper fixtures written")
 
 
 if __name__ == "__main__":

@@ -127,3 +127,35 @@ def test_load_geometry_vs_reference():
     assert p.PBC is False and np.isclose(lv[3, 2], (7.0 - 4.0) - (5.0 - 4.0) + 6.0) and np.isclose(lv[0, 2], 5.0 - 4.0 - 3.0)
     head = io.primcoords2Xsf([6, 8], [[0.0, 1.0], [0.5, 1.5], [0.25, 0.75]], lv)
     assert "PRIMCOORD\n2 1\n6 0.000000 0.500000 0.250000\n8 1.000000 1.500000 0.750000\n" in head
+
+
+def test_common_helpers_vs_reference():
+    """Rotations, sphere frames, image replication, wrapping and pair parameters of
+    ppafm/common.py against the reference's own outputs (tests/golden/helpers.npz), and the
+    reference's test_sphere_tangent_space vectors."""
+    from ppafm_gb300 import common as C
+
+    g = np.load(os.path.join(HERE, "golden", "helpers.npz"))
+    FF = C.loadSpecies()
+    assert np.allclose(C.rotation_matrix(g["axis"], 0.7), g["rot"], rtol=0, atol=1e-14)
+    rots = C.genRotations(g["axis"], g["thetas"])
+    assert np.allclose(rots, g["rots"], rtol=0, atol=1e-14)
+    assert np.allclose(C.sphereTangentSpace(11), g["sphere"], rtol=0, atol=1e-14)
+    assert np.allclose(
+        C.sphereTangentSpace(2),
+        [[[-0.0, 1.0, 0.0], [-0.5, -0.0, 0.8660254], [0.8660254, 0.0, 0.5]], [[-0.67549029, -0.73736888, 0.0], [-0.36868444, 0.33774515, 0.8660254], [-0.63858018, 0.58499175, -0.5]]],
+    )
+    i, h = C.maxAlongDir(g["Rs"], g["hdir"])
+    i2, h2, e2 = C.maxAlongDirEntropy(g["Rs"], g["hdir"], beta=0.7)
+    assert np.allclose([i, h, i2, h2, e2], g["maxdir"], rtol=1e-14)
+    z, r, q, c = C.multRot(g["Zs"], g["Rs"], g["Qs"], g["cLJs"], rots, cog=(0.5, -0.5, 0.2))
+    assert np.array_equal(z, g["mr_Z"]) and np.allclose(r, g["mr_R"], rtol=0, atol=1e-13) and np.array_equal(q, g["mr_Q"]) and np.array_equal(c, g["mr_c"])
+    z, r, q, c = C.PBCAtoms3D(g["Zs"], g["Rs"], g["Qs"], g["cLJs"], g["lvec3"], npbc=[1, 1, 0])
+    assert np.array_equal(z, g["p3_Z"]) and np.allclose(r, g["p3_R"], rtol=0, atol=1e-13) and np.array_equal(q, g["p3_Q"]) and np.array_equal(c, g["p3_c"])
+    W = g["Rs"].copy()
+    C.wrapAtomsCell(W, 0.25, -0.1, g["lvec3"][0], g["lvec3"][1])
+    assert np.allclose(W, g["wrapped"], rtol=0, atol=1e-12)
+    assert np.array_equal(C.getSampleAtomsREA(g["Zs"], FF), g["sREA"])
+    assert np.array_equal(C.getAtomsRE(8, g["Zs"], FF), g["RE"])
+    R = np.array(C.makeRotJitter())
+    assert R.shape == (50, 3, 3) and np.allclose(R @ R.transpose(0, 2, 1), np.eye(3), atol=1e-12)
