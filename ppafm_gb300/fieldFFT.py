@@ -128,7 +128,61 @@ def potential2forces_mem(V, lvec, nDim, sigma=0.7, rho=None, multipole=None, doF
     return Fx, Fy, Fz, E
 
 
-def getProbeDensity(lvec, nDim, sigma=0.7, multipole_dict=None):
-    """fieldFFT.py:99-118 on the GPU (tilt 0): the tip density on the rolled grid."""
+def getSampleDimensions(lvec):
+    """The cell rows of lvec (fieldFFT.py:17-19)."""
+    return np.matrix(np.asarray(lvec)[1:])
+
+
+def getSize(inp_axis, dims, sampleSize):
+    """(|cell vector|, its length per grid step) along 'x', 'y' or 'z' (fieldFFT.py:22-29)."""
+    a = {"x": 0, "y": 1, "z": 2}[inp_axis]
+    size = np.linalg.norm(np.asarray(sampleSize)[a])
+    return size, size / dims[a]
+
+
+def getMGrid(dims, dd):
+    """Coordinate arrays X, Y, Z of the rolled grid the FFT route works on, the origin at index
+    0 and negative coordinates past the middle (fieldFFT.py:32-48)."""
+    out = []
+    for a in range(3):
+        n = int(dims[a])
+        shift = n // 2
+        shift_ = shift + (1.0 if n % 2 else 0.0)
+        idx = np.arange(n, dtype=np.float64)
+        line = dd[a] * np.roll(idx - shift_, shift)
+        shape = [1, 1, 1]
+        shape[a] = n
+        out.append(np.broadcast_to(line.reshape(shape), tuple(int(x) for x in dims)).copy())
+    return out[0], out[1], out[2]
+
+
+def getProbeDensity(lvec, nDim=None, Z=None, dd=None, *args, sigma=0.7, multipole_dict=None, tilt=0.0, **kw):
+    """The normalised Gaussian tip density with multipoles (fieldFFT.py:99-118) on the GPU, tilt
+    0, on the rolled grid: ``getProbeDensity(lvec, nDim, sigma=..., multipole_dict=...)``, or
+    the reference's form ``getProbeDensity(sampleSize, X, Y, Z, dd, sigma, multipole_dict,
+    tilt)`` with X, Y, Z from getMGrid (the only coordinates the GPU makes)."""
+    if isinstance(nDim, np.ndarray) and nDim.ndim == 3:  # the reference's (sampleSize, X, Y, Z, dd, ...)
+        X, Y, Zc = nDim, Z, dd
+        dd = args[0] if args else kw.pop("dd")
+        rest = list(args[1:])
+        if rest:
+            sigma = rest.pop(0)
+        if rest:
+            multipole_dict = rest.pop(0)
+        if rest:
+            tilt = rest.pop(0)
+        dims = X.shape
+        Xg, Yg, Zg = getMGrid(dims, dd)
+        if not (np.allclose(X, Xg) and np.allclose(Y, Yg) and np.allclose(Zc, Zg)):
+            raise ValueError("the GPU makes the density on getMGrid's coordinates; X, Y, Z differ from them")
+        cell = np.asarray(lvec, dtype=np.float64)
+        lvec = np.vstack([np.zeros(3), cell[-3:]])
+        nDim = dims
+    elif Z is not None:
+        sigma = Z
+        if dd is not None:
+            multipole_dict = dd
+    if tilt != 0.0:
+        raise NotImplementedError("tilted tip densities are not supported")
     g = FFTGrid(nDim)
     return g.probe_density(lvec, sigma, multipole_dict).cpu().numpy().astype(np.float64)

@@ -300,3 +300,23 @@ def test_density_overlap_pipeline_vs_oracle(gpulib, overlap_case, f64):
     assert abs(itg.mean() - it.mean()) < 0.05 * it.mean() + 0.5
     dfz = np.abs(out["fzs"].cpu().numpy() - fzs)[~flips].max()
     assert dfz < (1e-4 if f64 else 2e-3), dfz
+
+
+def test_get_probe_density_reference_signature(gpulib, oracle):
+    """fieldFFT.getProbeDensity called like the reference (sampleSize, X, Y, Z, dd, sigma,
+    multipole_dict) with getMGrid coordinates equals the (lvec, nDim) form and the oracle."""
+    from ppafm_gb300 import fieldFFT as F
+
+    lv = np.array([[0.0, 0, 0], [6.0, 0, 0], [1.2, 5.5, 0], [0, 0.4, 4.3]])
+    dims = (15, 16, 17)
+    dd = [F.getSize(a, dims, F.getSampleDimensions(lv))[1] for a in "xyz"]
+    X, Y, Z = F.getMGrid(dims, dd)
+    mp = {"s": 1.0, "dz2": -0.3}
+    a = F.getProbeDensity(F.getSampleDimensions(lv), X, Y, Z, dd, 0.7, mp)
+    b = F.getProbeDensity(lv, dims, sigma=0.7, multipole_dict=mp)
+    assert np.array_equal(a, b)
+    Xo, Yo, Zo = oracle.getMGrid(dims, dd)
+    ref = oracle.getProbeDensity(lv, Xo, Yo, Zo, dd, sigma=0.7, multipole_dict=mp)
+    assert np.abs(a - ref).max() <= 1e-5 * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        F.getProbeDensity(F.getSampleDimensions(lv), X + 0.1, Y, Z, dd, 0.7, mp)
