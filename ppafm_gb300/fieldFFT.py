@@ -129,8 +129,9 @@ def potential2forces_mem(V, lvec, nDim, sigma=0.7, rho=None, multipole=None, doF
 
 
 def getSampleDimensions(lvec):
-    """The cell rows of lvec (fieldFFT.py:17-19)."""
-    return np.matrix(np.asarray(lvec)[1:])
+    """The cell rows of lvec (fieldFFT.py:17-19; a plain array where the reference returns the
+    deprecated numpy matrix)."""
+    return np.array(np.asarray(lvec, dtype=np.float64)[1:])
 
 
 def getSize(inp_axis, dims, sampleSize):
