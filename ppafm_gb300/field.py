@@ -92,18 +92,22 @@ class DataGrid:
 
     @classmethod
     def from_file(cls, file_path, scale=1.0):
-        """(grid, xyzs, Zs) from an XSF datagrid (io.py loadXSFData + loadXSFGeom); values
-        times scale."""
+        """(grid, xyzs, Zs) from a cube file or an XSF datagrid (io.py loadCUBE + loadAtomsCUBE,
+        loadXSFData + loadXSFGeom); values times scale."""
         file_path = str(file_path)
-        if not file_path.endswith(".xsf"):
+        if file_path.endswith(".cube"):
+            data, lvec, _, _ = io.loadCUBE(file_path, xyz_order=True)
+            Zs, x, y, z, _ = io.loadAtomsCUBE(file_path)
+        elif file_path.endswith(".xsf"):
+            data, lvec, _, _ = io.loadXSFData(file_path, xyz_order=True)
+            try:
+                (Zs, x, y, z, _), _, _ = io.loadXSFGeom(file_path)
+            except ValueError:
+                warnings.warn(f"Could not read geometry from {file_path} in DataGrid.from_file.")
+                Zs = np.zeros(1)
+                x = y = z = np.zeros((1, 1))
+        else:
             raise ValueError(f"Unsupported file format in file `{file_path}`")
-        data, lvec, _, _ = io.loadXSFData(file_path, xyz_order=True)
-        try:
-            (Zs, x, y, z, _), _, _ = io.loadXSFGeom(file_path)
-        except ValueError:
-            warnings.warn(f"Could not read geometry from {file_path} in DataGrid.from_file.")
-            Zs = np.zeros(1)
-            x = y = z = np.zeros((1, 1))
         if not np.allclose(scale, 1.0):
             data = data * scale
         return cls(data, lvec), np.stack([np.asarray(x).ravel(), np.asarray(y).ravel(), np.asarray(z).ravel()], axis=1), np.array(Zs)

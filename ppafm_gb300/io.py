@@ -69,6 +69,114 @@ def saveXYZ(fname, xyzs, Zs, qs=None, comment="", append=False):
             f.write(line + "\n")
 
 
+# Gaussian cube units (io.py:13-14)
+bohrRadius2angstroem = 0.5291772109217
+Hartree2eV = 27.211396132
+
+
+def _cube_header(fname):
+    with open(fname) as f:
+        f.readline()
+        f.readline()
+        h = [f.readline().split() for _ in range(4)]
+    return h
+
+
+def loadCellCUBE(fname):
+    """[origin, a, b, c] of a cube file in A (io.py:350-379): the voxel vectors times their
+    counts, converted from bohr."""
+    h = _cube_header(fname)
+    b = bohrRadius2angstroem
+    cell = [[float(v) * b for v in h[0][1:4]]]
+    for k in (1, 2, 3):
+        n = int(h[k][0])
+        cell.append([float(v) * n * b for v in h[k][1:4]])
+    return cell
+
+
+def loadNCUBE(fname):
+    """Voxel counts of a cube file (io.py:382-395)."""
+    h = _cube_header(fname)
+    return [int(h[1][0]), int(h[2][0]), int(h[3][0])]
+
+
+def loadAtomsCUBE(fname):
+    """[Zs, x, y, z, q] of a cube file's atoms, coordinates in A, charges 0 (io.py:291-320)."""
+    e, x, y, z, q = [], [], [], [], []
+    with open(fname) as f:
+        f.readline()
+        f.readline()
+        natoms = int(f.readline().split()[0])
+        for _ in range(3):
+            f.readline()
+        for _ in range(natoms):
+            w = f.readline().split()
+            e.append(int(w[0]))
+            x.append(float(w[2]) * bohrRadius2angstroem)
+            y.append(float(w[3]) * bohrRadius2angstroem)
+            z.append(float(w[4]) * bohrRadius2angstroem)
+            q.append(0.0)
+    return [e, x, y, z, q]
+
+
+def loadCUBE(fname, xyz_order=False):
+    """(data, lvec [4, 3], grid size, header) of a Gaussian cube file (io.py:643-675): values
+    converted from Hartree to eV (x slowest in the file); x, y, z order with xyz_order, else
+    reversed like an XSF grid."""
+    h = _cube_header(fname)
+    nDim = np.array([int(h[1][0]), int(h[2][0]), int(h[3][0])])
+    lvec = np.array(loadCellCUBE(fname), dtype=np.float64)
+    natoms = abs(int(h[0][0]))
+    with open(fname) as f:
+        for _ in range(6 + natoms):
+            f.readline()
+        vals = np.array(f.read().split()[: int(np.prod(nDim))], dtype=np.float64)
+    if vals.size != int(np.prod(nDim)):
+        raise ValueError(f"{fname}: {vals.size} grid values, expected {int(np.prod(nDim))}")
+    F = vals.reshape(nDim)
+    if not xyz_order:
+        F = F.transpose((2, 1, 0)).copy()
+        nDim = [nDim[2], nDim[1], nDim[0]]
+    F *= Hartree2eV
+    head = ["BEGIN_BLOCK_DATAGRID_3D \n", "g98_3D_unknown \n", "DATAGRID_3D_g98Cube \n"]
+    return F, lvec, nDim, head
+
+
+def saveGeomXSF(fname, elems, xyzs, primvec, convvec=None, bTransposed=False):
+    """An XSF geometry: CRYSTAL, PRIMVEC, CONVVEC (primvec when not given), PRIMCOORD atoms
+    (io.py:203-226; xyzs [n, 3], or [3, n] with bTransposed)."""
+    convvec = primvec if convvec is None else convvec
+    xyzs = np.asarray(xyzs)
+    if bTransposed:
+        xyzs = xyzs.T
+    with open(fname, "w") as f:
+        f.write("CRYSTAL\nPRIMVEC\n")
+        for v in primvec:
+            f.write("".join(" %f " % x for x in v) + "\n")
+        f.write("CONVVEC\n")
+        for v in convvec:
+            f.write("".join(" %f " % x for x in v) + "\n")
+        f.write("PRIMCOORD\n%i %i\n" % (len(elems), 1))
+        for i in range(len(elems)):
+            f.write(f"{elems[i]} {xyzs[i][0]:10.10f} {xyzs[i][1]:10.10f} {xyzs[i][2]:10.10f}\n")
+        f.write("\n")
+
+
+def getFromHead_PRIMCOORD(head):
+    """(Zs, Rs) of the PRIMCOORD block in a list of XSF header lines (io.py:623-637)."""
+    Zs = Rs = None
+    for i, line in enumerate(head):
+        if "PRIMCOORD" in line:
+            n = int(head[i + 1].split()[0])
+            Zs = np.zeros(n, dtype="int32")
+            Rs = np.zeros((n, 3))
+            for j in range(n):
+                w = head[i + j + 2].split()
+                Zs[j] = int(w[0])
+                Rs[j] = [float(w[1]), float(w[2]), float(w[3])]
+    return Zs, Rs
+
+
 def parseLvecASE(comment):
     """Lattice vectors of an ASE extended-xyz comment line (Lattice="ax ay az bx ... cz"),
     origin zero, as float32 values like io.py:506-525; None without them."""
@@ -131,11 +239,12 @@ def loadGeometryIN(fname):
 
 def loadGeometry(fname=None, format=None, parameters=None):
     """(atoms [Zs, x, y, z, q] lists, grid size, lvec [4, 3]) of a geometry file (io.py:398-503):
-    xyz (with ASE lattice), xsf (PRIMCOORD), POSCAR/CONTCAR or FHI-aims .in.  A missing lattice
+    xyz (with ASE lattice), xsf (PRIMCOORD), cube, POSCAR/CONTCAR or FHI-aims .in.  A missing lattice
     comes from the parameters; a zero lattice vector becomes one that encloses the scan window
     (probe offset included) with 3 A of padding and switches PBC off; a grid size that is not
     positive becomes 10 points per A.  The parameters' grid (gridO/A/B/C, gridN) is set to the
-    result, as in the reference.  CUBE and npy geometries are not read here."""
+    result, as in the reference.  CUBE files give their atoms and cell; npy geometries are not
+    read here."""
     import copy
 
     if fname is None:
@@ -166,8 +275,12 @@ def loadGeometry(fname=None, format=None, parameters=None):
         xyzs, Zs, lvec = loadPOSCAR(fname)
     elif format == "in":
         xyzs, Zs, lvec = loadGeometryIN(fname)
-    elif format in ("cube", "npy"):
-        raise NotImplementedError(f"{format} geometries are not read by this library")
+    elif format == "cube":
+        atoms = loadAtomsCUBE(fname)
+        lvec = loadCellCUBE(fname)
+        nDim = loadNCUBE(fname)
+    elif format == "npy":
+        raise NotImplementedError("npy geometries are not read by this library")
     elif format is None:
         raise ValueError("ERROR!!! Input geometry format was neither specified nor could it be determined automatically.")
     else:

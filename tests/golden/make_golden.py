@@ -47,6 +47,7 @@ def main(ref_root="/root/reference", only=None):
             make_params(ref_root)
             make_stages(tmp)
             make_helpers(tmp)
+            make_cube(tmp)
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         return
@@ -347,6 +348,40 @@ def make_helpers(tmp):
     out["RE"] = PPU.getAtomsRE(8, Zs, FF)
     np.savez(os.path.join(HERE, "helpers.npz"), **out)
     print("helper fixtures written")
+
+
+def make_cube(tmp):
+    """A small Gaussian cube file (skewed voxels, three atoms) and what the reference's readers
+    make of it (io.loadCUBE in both orders, loadAtomsCUBE, loadCellCUBE, loadNCUBE, loadGeometry)
+    -> tests/golden/cube/."""
+    import ppafm.common as PPU
+    import ppafm.io as pio
+
+    out = os.path.join(HERE, "cube")
+    os.makedirs(out, exist_ok=True)
+    rng = np.random.default_rng(77)
+    n = (5, 4, 6)
+    vox = np.array([[0.4, 0.0, 0.0], [0.1, 0.45, 0.0], [0.0, 0.05, 0.5]])
+    data = rng.normal(size=n)
+    path = os.path.join(out, "dens.cube")
+    with open(path, "w") as f:
+        f.write("seeded cube\nsecond comment line\n")
+        f.write("%5d %12.6f %12.6f %12.6f\n" % (3, -1.0, 0.5, 2.0))
+        for k in range(3):
+            f.write("%5d %12.6f %12.6f %12.6f\n" % (n[k], *vox[k]))
+        for Z, p in ((6, (1.0, 1.5, 2.0)), (8, (2.2, 0.3, -0.4)), (1, (0.0, 0.0, 0.0))):
+            f.write("%5d %12.6f %12.6f %12.6f %12.6f\n" % (Z, 0.0, *p))
+        vals = data.ravel()
+        for i in range(0, vals.size, 6):
+            f.write(" ".join("%13.5e" % v for v in vals[i : i + 6]) + "\n")
+    F, lvec, nD, _ = pio.loadCUBE(path)
+    Fx, _, nDx, _ = pio.loadCUBE(path, xyz_order=True)
+    atoms = pio.loadAtomsCUBE(path)
+    p = PPU.PpafmParameters()
+    g_atoms, g_n, g_lvec = pio.loadGeometry(path, parameters=p)
+    np.savez(os.path.join(out, "parsed.npz"), F=F, lvec=lvec, nD=np.array(nD), Fx=Fx, nDx=np.array(nDx), atoms=np.array(atoms, dtype=np.float64),
+             cell=np.array(pio.loadCellCUBE(path)), ncube=np.array(pio.loadNCUBE(path)), g_atoms=np.array(g_atoms, dtype=np.float64), g_n=np.array(g_n), g_lvec=np.array(g_lvec))
+    print("cube fixtures written")
 
 
 if __name__ == "__main__":

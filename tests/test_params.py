@@ -159,3 +159,33 @@ def test_common_helpers_vs_reference():
     assert np.array_equal(C.getAtomsRE(8, g["Zs"], FF), g["RE"])
     R = np.array(C.makeRotJitter())
     assert R.shape == (50, 3, 3) and np.allclose(R @ R.transpose(0, 2, 1), np.eye(3), atol=1e-12)
+
+
+def test_cube_and_xsf_geometry_files(tmp_path):
+    """Gaussian cube reading (io.py:291-395, 643-675) against the reference's readers on a
+    skewed-voxel file (tests/golden/cube/), loadGeometry of it, and the XSF geometry writer
+    with the PRIMCOORD header parser."""
+    from ppafm_gb300 import common, io
+
+    gold = os.path.join(HERE, "golden", "cube")
+    g = np.load(os.path.join(gold, "parsed.npz"))
+    path = os.path.join(gold, "dens.cube")
+    F, lvec, nD, head = io.loadCUBE(path)
+    assert np.array_equal(F, g["F"]) and np.array_equal(lvec, g["lvec"]) and list(nD) == list(g["nD"])
+    Fx, _, nDx, _ = io.loadCUBE(path, xyz_order=True)
+    assert np.array_equal(Fx, g["Fx"]) and list(nDx) == list(g["nDx"])
+    assert np.array_equal(np.array(io.loadAtomsCUBE(path), dtype=np.float64), g["atoms"])
+    assert np.array_equal(np.array(io.loadCellCUBE(path)), g["cell"]) and io.loadNCUBE(path) == list(g["ncube"])
+    p = common.PpafmParameters()
+    atoms, n, lv = io.loadGeometry(path, parameters=p)
+    assert np.array_equal(np.array(atoms, dtype=np.float64), g["g_atoms"]) and np.array_equal(np.array(n), g["g_n"]) and np.array_equal(lv, g["g_lvec"])
+    # XSF geometry: written, read back by loadXSFGeom and by the header parser
+    xyz = np.array([[0.5, 1.0, 1.5], [2.0, -1.0, 0.25]])
+    cell = np.diag([6.0, 7.0, 8.0])
+    io.saveGeomXSF(str(tmp_path / "g.xsf"), [6, 8], xyz, cell)
+    with open(tmp_path / "g.xsf", "a") as f:
+        f.write("BEGIN_BLOCK_DATAGRID_3D\nx\nBEGIN_DATAGRID_3D_x\n2 2 2\n0 0 0\n6 0 0\n0 7 0\n0 0 8\n")
+    (Zs, x, y, z, _), _, _ = io.loadXSFGeom(str(tmp_path / "g.xsf"))
+    assert Zs == [6, 8] and np.allclose(np.column_stack([x, y, z]), xyz)
+    Zh, Rh = io.getFromHead_PRIMCOORD(open(tmp_path / "g.xsf").read().split("\n"))
+    assert list(Zh) == [6, 8] and np.allclose(Rh, xyz)
