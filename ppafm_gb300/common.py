@@ -14,6 +14,7 @@ eVA_Nm = 16.0217662
 CoulombConst = 14.399645
 
 loadSpecies = _species.loadSpecies
+loadSpeciesLines = _species.loadSpeciesLines
 getFFdict = _species.getFFdict
 atom2iZ = _species.atom2iZ
 atoms2iZs = _species.atoms2iZs

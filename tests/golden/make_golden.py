@@ -251,6 +251,8 @@ def make_params(ref_root):
     default = PPU.PpafmParameters().model_dump()
     with open(os.path.join(out, "parsed.json"), "w") as f:
         json.dump({"parsed": parsed, "default": default}, f, indent=1)
+    sp = PPU.loadSpecies()  # the reference's default species table
+    np.savez(os.path.join(out, "species.npz"), rmin=sp["rmin"], epsilon=sp["epsilon"], alpha=sp["alpha"], atom=sp["atom"], symbol=sp["symbol"])
     print("params fixtures written")
 
 

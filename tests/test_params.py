@@ -189,3 +189,17 @@ def test_cube_and_xsf_geometry_files(tmp_path):
     assert Zs == [6, 8] and np.allclose(np.column_stack([x, y, z]), xyz)
     Zh, Rh = io.getFromHead_PRIMCOORD(open(tmp_path / "g.xsf").read().split("\n"))
     assert list(Zh) == [6, 8] and np.allclose(Rh, xyz)
+
+
+def test_species_table_is_the_reference_default():
+    """The built-in per-element table equals the reference's defaults/atomtypes.ini as the
+    reference loads it (all 118 species), and loadSpeciesLines reads the same format."""
+    from ppafm_gb300 import common
+
+    g = np.load(os.path.join(HERE, "golden", "params", "species.npz"))
+    sp = common.loadSpecies()
+    for k in ("rmin", "epsilon", "alpha", "atom", "symbol"):
+        assert np.array_equal(sp[k], g[k]), k
+    lines = [f"{r} {e} {a} {z} {s.decode()}\n" for r, e, a, z, s in zip(g["rmin"], g["epsilon"], g["alpha"], g["atom"], g["symbol"])]
+    sp2 = common.loadSpeciesLines(lines + ["short line\n"])
+    assert len(sp2) == len(sp) and np.array_equal(sp2["rmin"], sp["rmin"]) and np.array_equal(sp2["symbol"], sp["symbol"])
