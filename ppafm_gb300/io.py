@@ -460,6 +460,24 @@ def limit_vec_field(FF, Fmax=100.0):
         FF[..., k].flat[mask] *= Fmax / FR[mask]
 
 
+def saveWSxM_2D(name_file, data, Xs, Ys):
+    """One image as a WSxM ASCII XYZ file: header lines, then x, y, value per point
+    (io.py:680-692)."""
+    out = np.column_stack([np.asarray(Xs).ravel(), np.asarray(Ys).ravel(), np.asarray(data).ravel()])
+    with open(name_file, "w") as f:
+        f.write("WSxM file copyright Nanotec Electronica\nWSxM ASCII XYZ file\nX[A]  Y[A]  df[Hz]\n\n")
+        np.savetxt(f, out)
+
+
+def saveWSxM_3D(prefix, data, extent, slices=None):
+    """The z slices of data [nx, ny, nz] as <prefix>_NNN.xyz WSxM files over extent
+    (xmin, xmax, ymin, ymax) (io.py:695-706)."""
+    nx, ny, nz = np.shape(data)
+    Xs, Ys = np.meshgrid(np.linspace(extent[0], extent[1], nx), np.linspace(extent[2], extent[3], ny))
+    for i in range(nz) if slices is None else slices:
+        saveWSxM_2D(prefix + "_%03d.xyz" % i, data[:, :, i], Xs, Ys)
+
+
 def saveNpy(fname, data, lvec, atomic_info):
     np.savez(fname + ".npz", data=data, lvec=lvec, atoms=atomic_info[0], lvec0=atomic_info[1])
 

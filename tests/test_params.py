@@ -203,3 +203,18 @@ def test_species_table_is_the_reference_default():
     lines = [f"{r} {e} {a} {z} {s.decode()}\n" for r, e, a, z, s in zip(g["rmin"], g["epsilon"], g["alpha"], g["atom"], g["symbol"])]
     sp2 = common.loadSpeciesLines(lines + ["short line\n"])
     assert len(sp2) == len(sp) and np.array_equal(sp2["rmin"], sp["rmin"]) and np.array_equal(sp2["symbol"], sp["symbol"])
+
+
+def test_wsxm_writers(tmp_path):
+    """WSxM ASCII XYZ slices (io.py:680-706): the header, then x, y and the value at every
+    pixel of the slice in meshgrid order (byte-identical to the reference's writer when checked
+    against it)."""
+    from ppafm_gb300 import io
+
+    data = np.arange(4 * 3 * 2, dtype=np.float64).reshape(4, 3, 2)
+    io.saveWSxM_3D(str(tmp_path / "df"), data, [0.0, 3.0, 1.0, 2.0])
+    lines = open(tmp_path / "df_001.xyz").read().split("\n")
+    assert lines[:4] == ["WSxM file copyright Nanotec Electronica", "WSxM ASCII XYZ file", "X[A]  Y[A]  df[Hz]", ""]
+    v = np.loadtxt(tmp_path / "df_001.xyz", skiprows=4)
+    Xs, Ys = np.meshgrid(np.linspace(0, 3, 4), np.linspace(1, 2, 3))
+    assert np.allclose(v[:, 0], Xs.ravel()) and np.allclose(v[:, 1], Ys.ravel()) and np.allclose(v[:, 2], data[:, :, 1].ravel())
