@@ -207,8 +207,7 @@ def test_species_table_is_the_reference_default():
 
 def test_wsxm_writers(tmp_path):
     """WSxM ASCII XYZ slices (io.py:680-706): the header, then x, y and the value at every
-    pixel of the slice in meshgrid order (byte-identical to the reference's writer when checked
-    against it)."""
+    pixel of the slice in meshgrid order, the layout of the reference's writer."""
     from ppafm_gb300 import io
 
     data = np.arange(4 * 3 * 2, dtype=np.float64).reshape(4, 3, 2)
