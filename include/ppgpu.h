@@ -245,6 +245,11 @@ int ppgpu_batch_info(void *handle, long long *out4);
 /* FIRE iterations of the last run (synchronises the stream). */
 int ppgpu_batch_iterations(void *handle, unsigned long long *out, void *stream);
 int ppgpu_batch_destroy(void *handle);
+/* No counterpart in the reference (failure detection).  Limit of a stroke's bounded wait for
+ * its system's force field (wait_s seconds, default 2) and, for tests, a system whose force
+ * field is treated as never published (held >= 0; -1 none): its strokes give up after the
+ * limit and ppgpu_device_status reports PPGPU_ERR_DEVICE_TIMEOUT.  Synchronous. */
+int ppgpu_batch_set_wait(void *handle, double wait_s, int held);
 /* Height-synchronous run with an optional warm-start network (ppgpu_mlp_*; NULL = plain FIRE
  * from the height above): for each height the network proposes every stroke's starting
  * displacement and FIRE starts from the proposal unless its force residual exceeds the plain
@@ -347,10 +352,19 @@ int ppgpu_grid_to_f64(double *F3, double *E, const float *FE, long long npts, in
  * allocate device memory at call time (an application whose allocator reserved the device
  * memory up front; a latency-sensitive loop that cannot take the device-wide
  * synchronisation of cudaMalloc/cudaFree): it allocates nothing and stages its scratch in a
- * fixed 5.5 MB array that every GPU loading the library holds until exit.  Limits: natoms <=
- * 32768 and n2 <= 262144 (larger requests return PPGPU_ERR_ARG).  The first call on a device
- * looks up the array's device address.  All calls share the array: calls that overlap on
- * the GPU race. */
+ * fixed 5.5 MB array.  Limits: natoms <= 32768 and n2 <= 262144 (larger requests return
+ * PPGPU_ERR_ARG).
+ * Loading: the array is part of the library's device code, which CUDA loads on a device at
+ * the first call there (lazy module loading, the default) -- that load takes device memory
+ * once, and the device then holds the array until the process exits.  Callers that reserve
+ * all device memory make one small call on each device first (or set
+ * CUDA_MODULE_LOADING=EAGER).  The first call on a device also looks up the array's device
+ * address (cudaGetSymbolAddress, once per device, cached for the process: the library does
+ * not survive cudaDeviceReset).
+ * All calls share the array and it keeps the last call's contents: calls that overlap on the
+ * GPU race.  The call returns once its work is queued on `stream`; a bounded device wait that
+ * gave up inside it is reported by ppgpu_device_status(stream), which also allocates
+ * nothing. */
 int ppgpu_lj_grid_f64_noalloc(double *gridF, double *gridE, const int *n, const double *cell, int natoms,
                               const double *Ratoms, const double *cLJs, void *stream);
 

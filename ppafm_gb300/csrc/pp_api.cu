@@ -58,6 +58,13 @@ int *device_error_word() {
     return g_err_words[dev];
 }
 
+int *device_error_word_if_allocated() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(g_err_mutex);
+    return g_err_words[dev];
+}
+
 // GridShape::setCell + Mat3::invert_T_to (Grid.h:29-36, Mat3.h:275-286).
 int make_geom(const int *n, const double *cell, GridGeom *g) {
     for (int k = 0; k < 3; k++) {
@@ -320,18 +327,26 @@ using namespace ppgpu;
 extern "C" const char *ppgpu_last_error(void) { return g_msg; }
 extern "C" int ppgpu_last_status(void) { return g_status; }
 
+// Reads (and clears) the error words that kernels set when a bounded wait gives up: the
+// library's per-device word and that of the no-allocation entry point's fixed array.  Words
+// that were never allocated or looked up were never written; nothing is allocated here.
 extern "C" int ppgpu_device_status(void *stream) {
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
-    int *w = device_error_word();
-    if (!w) return set_error(PPGPU_ERR_CUDA, "device error word unavailable");
-    int code = 0;
-    e = cudaMemcpy(&code, w, sizeof(int), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "read device error word");
-    if (code) {
-        cudaMemset(w, 0, sizeof(int));
-        return set_error(code, "a kernel gave up on a bounded device-side wait (code %d)", code);
+    int *words[2] = {device_error_word_if_allocated(), noalloc_error_word_if_loaded()};
+    int first = 0;
+    for (int *w : words) {
+        if (!w) continue;
+        int code = 0;
+        e = cudaMemcpy(&code, w, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "read device error word");
+        if (code) {
+            e = cudaMemset(w, 0, sizeof(int));
+            if (e != cudaSuccess) return cuda_fail(e, "clear device error word");
+            if (!first) first = code;
+        }
     }
+    if (first) return set_error(first, "a kernel gave up on a bounded device-side wait (code %d)", first);
     return set_ok();
 }
 

@@ -53,6 +53,7 @@ struct BatchJob {  // device copy, one per system
     long long nchunks;
     int nzc;
     int ff_blocks;
+    int publish_need;     // published blocks its strokes wait for: ff_blocks (more: never ready)
     long long ff_block0;  // first item of this system in the force-field list
     // relaxation
     dfl dic[3];              // diagonal grid metric
@@ -89,6 +90,7 @@ struct BatchPrm {
     float W[BATCH_MAX_TAPS];
     unsigned long long *iter_total;
     int *err;
+    unsigned long long wait_ns;  // limit of a stroke's wait for its force field
 };
 
 __device__ __forceinline__ int find_job_ff(const BatchPrm &B, long long item) {
@@ -272,7 +274,6 @@ __device__ void relax_phase(const BatchPrm &B) {
     long long pool_next = 0, pool_end = 0;  // warp-uniform
     bool drained = false;                   // warp-uniform
     unsigned long long mine = 0;
-    constexpr unsigned long long WAIT_NS = 2000000000ull;
     while (true) {
         unsigned need = __ballot_sync(FULL, !has);
         while (need && !drained) {
@@ -296,13 +297,13 @@ __device__ void relax_phase(const BatchPrm &B) {
         if (!__any_sync(FULL, has)) break;
         if (has) {
             if (!S.ready) {
-                if (ld_acquire(&B.ff_done[S.job]) >= B.jobs[S.job].ff_blocks) {
+                if (ld_acquire(&B.ff_done[S.job]) >= B.jobs[S.job].publish_need) {
                     S.ready = true;
                 } else {
                     const unsigned long long t = global_ns();
                     if (S.wait_t0 == 0) {
                         S.wait_t0 = t;
-                    } else if (t - S.wait_t0 > WAIT_NS || load_err(B.err) != 0) {
+                    } else if (t - S.wait_t0 > B.wait_ns || load_err(B.err) != 0) {
                         raise_device_error(B.err, PPGPU_ERR_DEVICE_TIMEOUT);
                         has = false;  // the stroke is abandoned; the error is reported to the host
                     }
@@ -975,6 +976,7 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
         b.nzc = (b.n2 + 7) / 8;  // P = 8 points per thread (P2 = 4)
         b.nchunks = (long long)b.n0 * b.n1 * b.nzc;
         b.ff_blocks = (int)((b.nchunks + BATCH_THREADS - 1) / BATCH_THREADS);
+        b.publish_need = b.ff_blocks;
         b.ff_block0 = ff0;
         ff0 += b.ff_blocks;
         for (int k = 0; k < 3; k++) b.dic[k] = df_from(g.dicell[4 * k]);
@@ -1058,6 +1060,7 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
     B.iter_total = (unsigned long long *)((char *)H->ctr_base + sizeof(BatchCtr));
     B.ff_done = (int *)((char *)H->ctr_base + sizeof(BatchCtr) + sizeof(unsigned long long));
     B.err = device_error_word();
+    B.wait_ns = 2000000000ull;
     H->prm = B;
     *handle = H;
     return set_ok();
@@ -1070,6 +1073,24 @@ extern "C" int ppgpu_batch_run(void *handle, void *stream) {
     PPGPU_CUDA(cudaMemsetAsync(H->ctr_base, 0, H->ctr_bytes, st), "batch counters");
     batch_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm);
     PPGPU_CHECK_LAUNCH("batch_kernel");
+    return set_ok();
+}
+
+/* Limit of a stroke's wait for its system's force field (seconds; default 2) and, for tests of
+ * failure detection, a system whose force field its strokes treat as never published (held >= 0;
+ * -1: none): they give up after the limit, the launch ends, and ppgpu_device_status reports
+ * PPGPU_ERR_DEVICE_TIMEOUT.  Synchronous (updates the device table); applies to launches and
+ * graphs made after the call. */
+extern "C" int ppgpu_batch_set_wait(void *handle, double wait_s, int held) {
+    BatchHandle *H = (BatchHandle *)handle;
+    if (!H) return set_error(PPGPU_ERR_ARG, "batch_set_wait: null handle");
+    if (!(wait_s > 0.0) || wait_s > 60.0) return set_error(PPGPU_ERR_ARG, "batch_set_wait: limit %g s outside (0, 60]", wait_s);
+    if (held < -1 || held >= H->njobs) return set_error(PPGPU_ERR_ARG, "batch_set_wait: system %d of %d", held, H->njobs);
+    H->prm.wait_ns = (unsigned long long)(wait_s * 1e9);
+    std::vector<BatchJob> J(H->njobs);
+    PPGPU_CUDA(cudaMemcpy(J.data(), H->prm.jobs, sizeof(BatchJob) * H->njobs, cudaMemcpyDeviceToHost), "batch table read");
+    for (int j = 0; j < H->njobs; j++) J[j].publish_need = J[j].ff_blocks + (j == held ? 1 : 0);
+    PPGPU_CUDA(cudaMemcpy((void *)H->prm.jobs, J.data(), sizeof(BatchJob) * H->njobs, cudaMemcpyHostToDevice), "batch table write");
     return set_ok();
 }
 

@@ -15,8 +15,13 @@ int set_error(int status, const char *fmt, ...);
 int set_ok();
 // Translates a CUDA error into PPGPU_ERR_CUDA with context.
 int cuda_fail(cudaError_t e, const char *what);
-// Per-device error word that kernels set when a bounded wait gives up.
+// Per-device error word that kernels set when a bounded wait gives up (allocated on first
+// use); the _if_allocated form returns it without allocating (nullptr before first use).
 int *device_error_word();
+int *device_error_word_if_allocated();
+// Error word of the no-allocation entry point's fixed array on the current device, or nullptr
+// while no call has looked the array up on it (pp_ff.cu); never allocates.
+int *noalloc_error_word_if_loaded();
 // Runs fn(arg) with the radial tip spline (n knots xs, (value, slope) pairs ydys; n 0: none)
 // in place of the current one, then restores it; returns fn's status (pp_relax.cu).
 int with_tip_spline(int n, const double *xs, const double *ydys, int (*fn)(void *), void *arg);

@@ -369,10 +369,15 @@ extern "C" int ppgpu_ff_grid(float *FE, const int *n, const double *cell, const 
 // the kernels' error word) lives in one fixed array below, so the call allocates nothing.
 //
 // Limits: at most NOALLOC_MAX_ATOMS atoms per call; the grid is processed in chunks of at
-// most NOALLOC_CHUNK_PTS points (one z column, n2, must fit in a chunk).  Every GPU that loads
-// the library holds the array (5.5 MB) until the process exits.  All calls share it and it
-// keeps the last call's contents: calls that overlap on the GPU (different streams, or
-// different host threads) race on it.
+// most NOALLOC_CHUNK_PTS points (one z column, n2, must fit in a chunk).  Every GPU on which
+// the library's device code is loaded holds the array (5.5 MB) until the process exits; with
+// CUDA's default lazy loading that happens at the first call on the device (or at any other
+// launch of the library there), and that load itself takes device memory -- callers that
+// reserve all device memory make one small call first, or set CUDA_MODULE_LOADING=EAGER.
+// All calls share the array and it keeps the last call's contents: calls that overlap on the
+// GPU (different streams, or different host threads) race on it.  The calls return as soon
+// as their work is queued; a bounded wait that gave up inside them is reported by
+// ppgpu_device_status, which reads this array's error word too.
 
 namespace ppgpu {
 
@@ -410,21 +415,33 @@ __global__ void pack_lj_records_kernel(float *rec, const double *R, const double
     o[11] = 0.f;
 }
 
+// Device address of the fixed array, per device.  In host code g_noalloc_scratch names a
+// host-side stand-in, not device memory, so the address is looked up with
+// cudaGetSymbolAddress once per device with that device current (the lookup loads the
+// library's device code on that device if it is not loaded yet; it allocates nothing
+// afterwards).  The cache is per process: the library does not survive cudaDeviceReset.
+static unsigned char *g_noalloc_addr[64] = {nullptr};
+static std::mutex g_noalloc_mu;
+
 static int noalloc_scratch_address(unsigned char **out) {
-    // cudaGetSymbolAddress once per device, with that device current (it allocates nothing).
-    static unsigned char *addr[64] = {nullptr};
-    static std::mutex mu;
     int dev = 0;
     PPGPU_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= 64) return set_error(PPGPU_ERR_NO_DEVICE, "device index %d out of range", dev);
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
         void *p = nullptr;
         PPGPU_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
-        addr[dev] = (unsigned char *)p;
+        g_noalloc_addr[dev] = (unsigned char *)p;
     }
-    *out = addr[dev];
+    *out = g_noalloc_addr[dev];
     return PPGPU_OK;
+}
+
+int *noalloc_error_word_if_loaded() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    return g_noalloc_addr[dev] ? (int *)(g_noalloc_addr[dev] + NOALLOC_REC_BYTES + NOALLOC_CHUNK_BYTES) : nullptr;
 }
 
 }  // namespace ppgpu
@@ -449,7 +466,8 @@ extern "C" int ppgpu_lj_grid_f64_noalloc(double *gridF, double *gridE, const int
     float *chunk = (float *)(base + NOALLOC_REC_BYTES);
     int *err = (int *)(base + NOALLOC_REC_BYTES + NOALLOC_CHUNK_BYTES);
     cudaStream_t cs = (cudaStream_t)stream;
-    PPGPU_CUDA(cudaMemsetAsync(err, 0, sizeof(int), cs), "clear error word");
+    // The error word is zero when the library's device code is loaded and is cleared only by
+    // ppgpu_device_status, which reports it: a timeout of one call is not lost by the next.
     if (natoms > 0) {
         pack_lj_records_kernel<<<(natoms + 127) / 128, 128, 0, cs>>>(rec, Ratoms, cLJs, natoms);
         PPGPU_CHECK_LAUNCH("pack_lj_records_kernel");

@@ -237,93 +237,93 @@ def loadGeometryIN(fname):
     return np.array(xyzs), np.array(Zs, dtype=np.int32), lv
 
 
-def loadGeometry(fname=None, format=None, parameters=None):
-    """(atoms [Zs, x, y, z, q] lists, grid size, lvec [4, 3]) of a geometry file (io.py:398-503):
-    xyz (with ASE lattice), xsf (PRIMCOORD), cube, POSCAR/CONTCAR or FHI-aims .in.  A missing lattice
-    comes from the parameters; a zero lattice vector becomes one that encloses the scan window
-    (probe offset included) with 3 A of padding and switches PBC off; a grid size that is not
-    positive becomes 10 points per A.  The parameters' grid (gridO/A/B/C, gridN) is set to the
-    result, as in the reference.  CUBE files give their atoms and cell; npy geometries are not
-    read here."""
-    import copy
+def _geometry_format(fname):
+    """The geometry format a file name implies, or None: POSCAR*/CONTCAR* by the base name, the
+    others by suffix (.xyz, .xsf, .cube, .npy, FHI-aims .in and .in.next_step)."""
+    base = fname.replace("\\", "/").rsplit("/", 1)[-1]
+    if base.startswith(("POSCAR", "CONTCAR")):
+        return "poscar"
+    low = base.lower()
+    if low.endswith((".in", ".in.next_step")):
+        return "in"
+    suffix = low.rsplit(".", 1)[-1] if "." in low else ""
+    return suffix if suffix in ("xyz", "xsf", "cube", "npy") else None
 
-    if fname is None:
-        raise ValueError("Please provide the name of the file with coordinates")
-    if parameters is None:
-        raise ValueError("Please provide the parameters dictionary here")
-    fname = str(fname)
-    if format is None or format == "":
-        low = fname.lower()
-        for ext, fmt in ((".xyz", "xyz"), (".cube", "cube"), (".xsf", "xsf"), (".npy", "npy")):
-            if low.endswith(ext):
-                format = fmt
-        if low.endswith(".in") or low.endswith(".in.next_step"):
-            format = "in"
-        base = fname.replace("\\", "/").split("/")[-1]
-        if base.startswith("POSCAR") or base.startswith("CONTCAR"):
-            format = "poscar"
-    else:
-        format = format.lower()
-    xyzs = Zs = qs = None
-    nDim = None
-    if format == "xyz":
+
+def _atom_lists(xyzs, Zs, qs):
+    """The [Zs, x, y, z, q] lists of the geometry readers (charges 0 when the file has none)."""
+    qs = np.zeros(len(Zs)) if qs is None else qs
+    return [list(Zs), list(xyzs[:, 0]), list(xyzs[:, 1]), list(xyzs[:, 2]), list(qs)]
+
+
+def _geometry_from_file(fname, fmt, parameters):
+    """(atom lists, grid size or None, lattice rows or None) of one file.  Files with a grid of
+    their own (xsf, cube) give its size; atom-only formats take the parameters' grid size."""
+    if fmt == "xsf":
+        return loadXSFGeom(fname)
+    if fmt == "cube":
+        return loadAtomsCUBE(fname), loadNCUBE(fname), loadCellCUBE(fname)
+    if fmt == "xyz":
         xyzs, Zs, qs, comment = loadXYZ(fname)
         lvec = parseLvecASE(comment)
-    elif format == "xsf":
-        atoms, nDim, lvec = loadXSFGeom(fname)
-    elif format == "poscar":
-        xyzs, Zs, lvec = loadPOSCAR(fname)
-    elif format == "in":
-        xyzs, Zs, lvec = loadGeometryIN(fname)
-    elif format == "cube":
-        atoms = loadAtomsCUBE(fname)
-        lvec = loadCellCUBE(fname)
-        nDim = loadNCUBE(fname)
-    elif format == "npy":
+    elif fmt == "poscar":
+        (xyzs, Zs, lvec), qs = loadPOSCAR(fname), None
+    elif fmt == "in":
+        (xyzs, Zs, lvec), qs = loadGeometryIN(fname), None
+    elif fmt == "npy":
         raise NotImplementedError("npy geometries are not read by this library")
-    elif format is None:
-        raise ValueError("ERROR!!! Input geometry format was neither specified nor could it be determined automatically.")
     else:
-        raise ValueError("ERROR!!! Unknown format %s of input geometry." % (format))
-    if xyzs is not None:
-        if qs is None:
-            qs = np.zeros(len(Zs))
-        atoms = [list(Zs), list(xyzs[:, 0]), list(xyzs[:, 1]), list(xyzs[:, 2]), list(qs)]
-        nDim = np.array(parameters.gridN)
+        raise ValueError(f"unknown geometry format {fmt!r} of {fname}")
+    return _atom_lists(xyzs, Zs, qs), np.array(parameters.gridN), lvec
+
+
+def _full_lattice(lvec, parameters):
+    """A [4, 3] lattice (origin + three vectors): rows the file lacks come from the
+    parameters' grid (gridO when the file gives no lattice at all)."""
+    defaults = [parameters.gridO, parameters.gridA, parameters.gridB, parameters.gridC]
+    rows = [] if lvec is None else [list(v) for v in lvec]
+    if not rows:
+        rows = [list(defaults[0])]
+    rows += [list(d) for d in defaults[len(rows) :]]
+    return np.array(rows, dtype=np.float64)
+
+
+def loadGeometry(fname=None, format=None, parameters=None):
+    """(atoms [Zs, x, y, z, q] lists, grid size, lvec [4, 3]) of a geometry file: xyz (with an
+    ASE lattice in the comment), xsf (PRIMCOORD), Gaussian cube, POSCAR/CONTCAR or FHI-aims
+    .in; the behaviour of ppafm/io.py:398-503.  Lattice vectors the file lacks come from the
+    parameters' grid.  A lattice vector that is zero is replaced by a box along its axis that
+    holds the probe's path over the scan window (scanMin..scanMax shifted by r0Probe, z
+    downwards) with 3 A to spare on each side, and periodic boundaries are switched off.  A
+    grid size that is not positive becomes the lattice vector's length over a 0.1 A step.  The
+    parameters' grid (gridO, gridA, gridB, gridC, gridN) is set to the result.  npy geometries
+    are not read here."""
+    if fname is None:
+        raise ValueError("loadGeometry needs the name of a geometry file")
+    if parameters is None:
+        raise ValueError("loadGeometry needs the simulation parameters")
+    fname = str(fname)
+    fmt = format.lower() if format else _geometry_format(fname)
+    if fmt is None:
+        raise ValueError(f"cannot tell the geometry format of {fname} from its name; pass format=")
+    atoms, nDim, lvec = _geometry_from_file(fname, fmt, parameters)
     nDim = np.array(nDim)
-    if lvec is None or len(lvec) == 0:
-        lvec = np.zeros((4, 3))
-        lvec[0, :] = copy.copy(parameters.gridO)
-        lvec[1, :] = copy.copy(parameters.gridA)
-        lvec[2, :] = copy.copy(parameters.gridB)
-        lvec[3, :] = copy.copy(parameters.gridC)
-    else:
-        lvec = [list(v) for v in lvec]
-        if len(lvec) == 1:
-            lvec.append(list(parameters.gridA))
-        if len(lvec) == 2:
-            lvec.append(list(parameters.gridB))
-        if len(lvec) == 3:
-            lvec.append(list(parameters.gridC))
-    lvec = np.array(lvec, dtype=np.float64)
-    probe_min = np.array(parameters.scanMin, dtype=np.float64)
-    probe_max = np.array(parameters.scanMax, dtype=np.float64)
-    r0 = parameters.r0Probe
-    probe_min += (r0[0], r0[1], -r0[2])
-    probe_max += (r0[0], r0[1], -r0[2])
-    pad, default_grid_step = 3.0, 0.1
-    for i in range(3):
-        if np.allclose(lvec[i + 1, :], 0):
+    lvec = _full_lattice(lvec, parameters)
+    r0 = np.array(parameters.r0Probe, dtype=np.float64) * (1.0, 1.0, -1.0)
+    path_lo = np.array(parameters.scanMin, dtype=np.float64) + r0
+    path_hi = np.array(parameters.scanMax, dtype=np.float64) + r0
+    pad, step = 3.0, 0.1  # A
+    for axis in range(3):
+        if np.allclose(lvec[axis + 1], 0):
             parameters.PBC = False
-            lvec[i + 1, i] = probe_max[i] - probe_min[i] + 2 * pad
-            lvec[0, i] = probe_min[i] - pad
-        if not nDim[i] > 0:
-            nDim[i] = round(np.linalg.norm(lvec[i + 1, :]) / default_grid_step)
-    for i in range(3):
-        parameters.gridO[i] = lvec[0][i]
-        parameters.gridA[i] = lvec[1][i]
-        parameters.gridB[i] = lvec[2][i]
-        parameters.gridC[i] = lvec[3][i]
+            lvec[axis + 1, axis] = path_hi[axis] - path_lo[axis] + 2 * pad
+            lvec[0, axis] = path_lo[axis] - pad
+        if not nDim[axis] > 0:
+            nDim[axis] = round(np.linalg.norm(lvec[axis + 1]) / step)
+    for name, row in zip(("gridO", "gridA", "gridB", "gridC"), lvec):
+        grid = getattr(parameters, name)
+        for k in range(3):
+            grid[k] = row[k]
     parameters.gridN = nDim
     return atoms, nDim, lvec
 

@@ -1,9 +1,10 @@
 """Generates the golden fixtures in tests/golden/ by running the reference ppafm package.
 
-Run where the reference checkout exists (it is read only):
+Run where the reference checkout exists (it is read only); its root is the first argument,
+else $PPAFM_REFERENCE, else /root/reference:
 
-    python tests/golden/make_golden.py [/root/reference]           # all fixtures
-    python tests/golden/make_golden.py /root/reference extras      # xsf/, tilt.npz, params/ only
+    python tests/golden/make_golden.py [REFERENCE_ROOT]           # all fixtures
+    python tests/golden/make_golden.py REFERENCE_ROOT extras      # xsf/, tilt.npz, params/ only
 
 The script copies the reference's ``ppafm`` package to a temporary directory, compiles
 its two C++ modules there from their own sources with g++ (ProbeParticle, GridUtils; the
@@ -38,7 +39,10 @@ def setup_reference(ref_root):
     return tmp
 
 
-def main(ref_root="/root/reference", only=None):
+DEFAULT_REFERENCE = os.environ.get("PPAFM_REFERENCE", "/root/reference")
+
+
+def main(ref_root=DEFAULT_REFERENCE, only=None):
     tmp = setup_reference(ref_root)
     if only == "extras":
         try:

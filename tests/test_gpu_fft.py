@@ -267,8 +267,10 @@ def overlap_case(oracle):
 @pytest.mark.parametrize("f64", [True, False])
 def test_density_overlap_pipeline_vs_oracle(gpulib, overlap_case, f64):
     """Pauli + Hartree force field, relaxed scan and Δf at half size (128^3 grid, 80x80x30
-    scan).  float64 transforms: positions within 1e-3 A like the point-charge pipeline.
-    float32 transforms (the default of the density-overlap workload): force field within
+    scan).
+    float64 transforms: the bar of the double-float relaxation path (every position within the
+    convergence ball, at most 1 in 10^4 past 1e-3 A, every Δf within 0.1 Hz).  float32
+    transforms (the default of the density-overlap workload): force field within
     1e-5 of its maximum; the ~1e-6 * max transform noise (~3e-5 eV/A against a 0.016 eV/A^2
     lateral spring) moves 0.2% of the positions past 1e-3 A, at most 0.028 A (stated bound:
     <= 0.5% past 1e-3 A, all within 0.04 A)."""
@@ -291,11 +293,12 @@ def test_density_overlap_pipeline_vs_oracle(gpulib, overlap_case, f64):
     dpos = np.linalg.norm(ppg - pp, axis=-1)
     if f64:
         flips = _check_positions(dpos)
+        assert np.abs(out["df"].cpu().numpy() - df).max() < 0.1
     else:
         flips, good = _split_flips(dpos)
         assert flips.mean() <= 0.005 and np.mean(good > POS_TOL) <= 0.005 and good.max() < 0.04, (flips.mean(), np.mean(good > POS_TOL), good.max())
-    ok = ~flips.any(axis=-1)
-    assert np.abs(out["df"].cpu().numpy() - df)[ok].max() < 0.1
+        ok = ~flips.any(axis=-1)
+        assert np.abs(out["df"].cpu().numpy() - df)[ok].max() < 0.1
     itg = out["iters"].cpu().numpy()
     assert abs(itg.mean() - it.mean()) < 0.05 * it.mean() + 0.5
     dfz = np.abs(out["fzs"].cpu().numpy() - fzs)[~flips].max()

@@ -44,10 +44,9 @@ def test_small_molecule_pipeline_vs_oracle(gpulib, oracle):
     dpos = np.linalg.norm(ppg - pp, axis=-1)
     from tests.test_gpu_relax import _check_positions
 
-    flips = _check_positions(dpos)
+    _check_positions(dpos)
     dfg = out["df"].cpu().numpy()
-    ok = ~flips.any(axis=-1)
-    assert np.abs(dfg - df)[ok].max() < 0.1
+    assert np.abs(dfg - df).max() < 0.1
     itg = out["iters"].cpu().numpy()
     assert abs(itg.mean() - it.mean()) < 0.05 * it.mean() + 0.5
     assert pl.iterations() == int(itg.sum()) or pl.iterations() >= int(itg.sum())

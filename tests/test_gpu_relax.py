@@ -1,13 +1,24 @@
 """GPU relaxation and Δf against the reference-generated fixtures and the oracle.
 
-Bars: relaxed probe positions within 1e-3 A of the reference for 99.9 % of pixel heights,
-Δf within 0.1 Hz.  The FIRE stopping rule |F| < 1e-4 eV/A leaves the converged position
-undetermined by up to |F|/k ~ 6e-3 A along the soft lateral spring (k = 0.25 N/m), and a
-few pixel heights are so sensitive that any change in the last bits of the force grid
-moves their stopping point within that ball; those may differ by up to 2e-2 A (twice the
-ball).  Larger differences are basin flips (different minima of a bistable pixel) and may
-affect at most 0.5 % of pixel heights.  Grid forces at the relaxed positions agree to
-1e-4 eV/A (the convergence force) except at flips."""
+Bars (the double-float relaxation path), written in ``_check_positions``:
+  * every Δf value within 0.1 Hz (checked by each test);
+  * no basin flips, and every relaxed probe position within the FIRE convergence ball of the
+    reference's: |F| < 1e-4 eV/A leaves the stopping point undetermined by up to
+    |F|/k_lat = 6.4e-3 A along the soft lateral spring (k_lat = 0.25 N/m);
+  * positions within 1e-3 A of the reference's for all but at most 1 in 10^4 pixel heights
+    (rounded up).
+The double-float interpolation, springs and force sum keep the GPU's trajectories on the
+reference's (measured max 1.6e-4 A on the relaxed-scan fixture).  What is left is the float32
+storage of the force grid (interleaved float4, ~6e-8 relative): near the end of a stroke the
+residual |F| ~ 1e-4 eV/A is a difference of forces ~1 eV/A, so that rounding can move the
+iteration at which |F| first drops below the criterion, and the stopping point moves inside
+the ball (measured: 7 of 192 000 pixel heights past 1e-3 A, at most 5.2e-3 A, on the FFT route
+with float64 transforms).  Two paths do not follow the reference's trajectories and are held
+to a stated looser bound in their own tests: the FFT route with float32 transforms (transform
+noise of ~1e-6 of the field's maximum) and the learned warm start (a different starting
+point inside the same ball); they use ``_split_flips``."""
+
+import math
 
 import numpy as np
 import pytest
@@ -16,7 +27,9 @@ pytestmark = pytest.mark.gpu
 
 POS_TOL = 1e-3
 DF_TOL = 0.1
-FLIP_FRAC = 0.005
+# |F_conv| / k_lat: sqrt(convF2) = 1e-4 eV/A over 0.25 N/m = 0.25/16.0217662 eV/A^2
+BALL = 1e-4 / (0.25 / 16.0217662)
+OUTLIER_FRAC = 1e-4
 
 
 def _relax_fixture(oracle, golden):
@@ -27,21 +40,48 @@ def _relax_fixture(oracle, golden):
     return g, FF, prm, xT, yT, zT
 
 
-BALL = 2e-2
-
-
 def _split_flips(dpos):
-    """Per pixel height: position error; flips = error above 0.05 A (a different minimum)."""
+    """Per pixel height: position error; flips = error above 0.05 A (a different minimum).
+    For the paths with a stated looser bound only."""
     flips = dpos > 0.05
     return flips, dpos[~flips]
 
 
 def _check_positions(dpos):
-    flips, good = _split_flips(dpos)
-    assert flips.mean() <= FLIP_FRAC, f"{flips.sum()} basin flips"
-    assert np.mean(good > POS_TOL) <= 1e-3, f"{np.sum(good > POS_TOL)} of {good.size} beyond {POS_TOL} A"
-    assert good.max() < BALL, good.max()
-    return flips
+    """The bar of the double-float path (module docstring).  Returns the mask of the pixel
+    heights past 1e-3 A (at most 1 in 10^4), which the callers' force comparisons skip;
+    Δf is compared everywhere."""
+    dpos = np.asarray(dpos)
+    n_out = int((dpos > POS_TOL).sum())
+    worst = float(dpos.max()) if dpos.size else 0.0
+    allowed = math.ceil(OUTLIER_FRAC * dpos.size)
+    assert worst < BALL, f"a pixel height {worst:.3g} A from the reference's: outside the convergence ball ({BALL:.3g} A)"
+    assert n_out <= allowed, f"{n_out} of {dpos.size} pixel heights beyond {POS_TOL} A (max {worst:.3g} A; at most {allowed} allowed)"
+    return dpos > POS_TOL
+
+
+END_TO_END_OUT_FRAC = 1e-2
+
+
+def _check_end_to_end(dpos, ddf):
+    """End to end: the GPU's float32 force field and its relaxation against the oracle's float64
+    force field and relaxation on the same atoms (dpos [..., heights], ddf [..., df values]).
+    The float32 grid's own error (stated per grid by the force-field tests) moves stopping points
+    inside the convergence ball more often than the grid's storage rounding alone, and at a
+    pixel whose two minima are a hair apart it can send the probe into the other one (a basin
+    flip; Δf of that pixel then differs).  Bar: basin flips (beyond the ball) at most 1 in 10^4
+    pixel heights (rounded up); every other height within the ball, at most 1 in 100 past
+    1e-3 A; Δf within 0.1 Hz at every pixel without a flip.  Returns (flipped heights, pixels
+    with a flip)."""
+    dpos = np.asarray(dpos)
+    flips = dpos > BALL
+    n_flip = int(flips.sum())
+    assert n_flip <= math.ceil(OUTLIER_FRAC * dpos.size), f"{n_flip} of {dpos.size} pixel heights in another basin"
+    rest = dpos[~flips]
+    assert np.mean(rest > POS_TOL) <= END_TO_END_OUT_FRAC, f"{int((rest > POS_TOL).sum())} of {rest.size} pixel heights beyond {POS_TOL} A"
+    pix_flip = flips.any(axis=-1)
+    assert np.abs(ddf)[~pix_flip].max() < DF_TOL
+    return flips, pix_flip
 
 
 def test_relax_scan_golden(gpulib, oracle, golden):
@@ -58,10 +98,9 @@ def test_relax_scan_golden(gpulib, oracle, golden):
     it = out["iters"].cpu().numpy()
     df = out["df"].cpu().numpy()
     dpos = np.linalg.norm(pp - g["PPpos"], axis=-1)
-    flips = _check_positions(dpos)
-    assert np.abs(fzs - g["fzs"])[~flips].max() < 1e-4
-    pix_ok = ~flips.any(axis=-1)
-    assert np.abs(df - g["df"])[pix_ok].max() < DF_TOL
+    outl = _check_positions(dpos)
+    assert np.abs(fzs - g["fzs"])[~outl].max() < 1e-4
+    assert np.abs(df - g["df"]).max() < DF_TOL
     # iteration counts of the sampled strokes: same FIRE, float32 vs float64 rounding
     for (ix, iy), s in zip(g["picks"], g["itsum"]):
         assert abs(int(it[ix, iy].sum()) - int(s)) <= 0.05 * s + 3
@@ -89,8 +128,8 @@ def test_dropin_relax_strokes_vs_oracle(gpulib, oracle, golden, probeStart, rela
         p2[2] = 0.1
     rs2, fs2, sums, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, p2, rT, probeStart=probeStart, relaxAlg=relaxAlg)
     dpos = np.linalg.norm(rs - rs2, axis=-1)
-    flips = _check_positions(dpos)
-    assert np.abs(fs - fs2)[~flips].max() < 1e-4
+    outl = _check_positions(dpos)
+    assert np.abs(fs - fs2)[~outl].max() < 1e-4
     assert core.last_iterations() > 0
     # one stroke: the iteration sum is returned
     s1 = core.relaxTipStroke(np.ascontiguousarray(rT[1, 1]), np.zeros_like(rT[1, 1]), np.zeros_like(rT[1, 1]), probeStart=probeStart, relaxAlg=relaxAlg)
@@ -239,8 +278,8 @@ def test_tilted_scan_relaxation(gpulib, oracle, golden):
     f_tilt, pp_tilt, _, lvs = HL.perform_relaxation(g["lvec"], FF, parameters=p, relax=relax)
     assert f_tilt.shape == f_plain.shape + (3,)
     dpos = np.linalg.norm(pp_tilt - g["PPpos"], axis=-1)
-    flips = _check_positions(dpos)
-    assert np.abs(f_tilt[..., 2] - f_plain)[~flips].max() < 1e-4
+    outl = _check_positions(dpos)
+    assert np.abs(f_tilt[..., 2] - f_plain)[~outl].max() < 1e-4
     # along z the tilted conversion is the plain one times the step length (the projection
     # on d is not normalised, common.py:443-445)
     df_t = common.Fz2df_tilt(f_tilt, [0.0, 0.0, 0.1], k0=1800.0, f0=30000.0, amplitude=1.0)
@@ -279,16 +318,16 @@ def test_tip_spline_strokes_and_scan_vs_oracle(gpulib, oracle, golden):
     finally:
         core.deleteFF_Fpointer()
     rs2, fs2, _, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, prm, rT, spline=(xs, ydys))
-    flips = _check_positions(np.linalg.norm(rs - rs2, axis=-1))
-    assert np.abs(fs - fs2)[~flips].max() < 1e-4
+    outl = _check_positions(np.linalg.norm(rs - rs2, axis=-1))
+    assert np.abs(fs - fs2)[~outl].max() < 1e-4
     rs3, _, _, _ = oracle.relax_strokes(g["n"], lv[1:], FFc, prm, rT)
     assert np.abs(rs3 - rs2).max() > 1e-3  # the spline changes the relaxed positions
     # the scan path (relax_scan inside perform_relaxation)
     p = dict(charge=0.0, klat=float(g["klat"]), krad=float(g["krad"]), r0Probe=list(g["r0Probe"]), scanMin=list(g["scanMin"]), scanMax=list(g["scanMax"]), scanStep=list(g["scanStep"]))
     fzs, PPpos, _, _ = HL.perform_relaxation(lv, FF, parameters=p, relax=dict(maxIters=300, convF2=1e-8, dt=0.5, damping=0.1), tip_spline=core.SplineParameters(xs, ydys))
     fz_o, pp_o, _ = oracle.relaxed_scan(g["n"], lv[1:], FF, prm, xT, yT, zT, lv[0], spline=(xs, ydys))
-    flips = _check_positions(np.linalg.norm(PPpos - pp_o, axis=-1))
-    assert np.abs(fzs - fz_o)[~flips].max() < 1e-4
+    outl = _check_positions(np.linalg.norm(PPpos - pp_o, axis=-1))
+    assert np.abs(fzs - fz_o)[~outl].max() < 1e-4
 
 
 def test_batch_refuses_tip_spline(gpulib):

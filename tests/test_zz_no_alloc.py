@@ -8,7 +8,8 @@ the C ABI with device buffers the test allocates beforehand, twice in a row on t
 grid (the second call accumulates a different atom set on top of the first, so stale
 scratch from the first call would show), and compares with the drop-in getLennardJonesFF
 (which allocates its own scratch) under the same tolerance as the other force-field tests.
-The file is named to be collected last.
+The second pair of calls must leave the device's free memory (cudaMemGetInfo) unchanged,
+and ppgpu_device_status must report no timeout.  The file is named to be collected last.
 """
 
 import ctypes
@@ -37,6 +38,8 @@ def _dropin(n, lvec, sets, with_E):
 
 
 def _noalloc(L, n, lvec, sets, with_E):
+    """Runs the calls on buffers allocated beforehand; returns (F, E, free bytes before the
+    calls, free bytes after them)."""
     import torch
 
     from ppafm_gb300 import _lib
@@ -47,11 +50,13 @@ def _noalloc(L, n, lvec, sets, with_E):
     E = torch.zeros(int(np.prod(nn)), dtype=torch.float64, device="cuda") if with_E else None
     dev = [(torch.as_tensor(np.ascontiguousarray(R)).cuda(), torch.as_tensor(np.ascontiguousarray(c)).cuda()) for R, c in sets]
     torch.cuda.synchronize()  # every buffer exists before the calls
+    free0 = torch.cuda.mem_get_info()[0]
     st = _lib.stream_handle()
     for (R, c), (Rd, cd) in zip(sets, dev):
         _lib.check(L.ppgpu_lj_grid_f64_noalloc(_lib.tptr(F), _lib.tptr(E), _lib.iptr(nn), _lib.dptr(cell), len(R), _lib.tptr(Rd), _lib.tptr(cd), st))
-    torch.cuda.synchronize()
-    return F.cpu().numpy().reshape(tuple(nn) + (3,)), (E.cpu().numpy().reshape(tuple(nn)) if with_E else None)
+    _lib.check(L.ppgpu_device_status(st))  # synchronises; no bounded wait gave up
+    free1 = torch.cuda.mem_get_info()[0]
+    return F.cpu().numpy().reshape(tuple(nn) + (3,)), (E.cpu().numpy().reshape(tuple(nn)) if with_E else None), free0, free1
 
 
 @pytest.mark.parametrize("shape", ["planes", "columns"])
@@ -70,13 +75,15 @@ def test_noalloc_matches_dropin_twice(gpulib, shape):
         c = np.column_stack([rng.uniform(10, 60, na), rng.uniform(1e4, 8e4, na)])
         sets.append((R, c))
     F0, E0 = _dropin(n, lvec, sets, True)
-    F1, E1 = _noalloc(gpulib, n, lvec, sets, True)
+    F1, E1, _, _ = _noalloc(gpulib, n, lvec, sets, True)
     ok = np.linalg.norm(F0, axis=-1) < 1e30
     assert rel_err(F1[ok], F0[ok], FLOOR) < TOL
     assert rel_err(E1[ok], E0[ok], FLOOR) < 1e-4
-    # repeat the pair of calls: the shared scratch keeps the last call's contents
-    F2, _ = _noalloc(gpulib, n, lvec, sets, False)
+    # repeat the pair of calls: the shared scratch keeps the last call's contents, and the
+    # calls (device code loaded by the first pair) take no device memory
+    F2, _, free0, free1 = _noalloc(gpulib, n, lvec, sets, False)
     assert rel_err(F2[ok], F0[ok], FLOOR) < TOL
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes across the calls"
 
 
 def test_noalloc_rejects_oversized_requests(gpulib):
