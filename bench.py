@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--relax-tps", type=int, default=0, help="lanes per stroke of the single-system relaxation (1, 2, 4, 8; 0 = library default)")
+    ap.add_argument("--no-extras", action="store_true", help="default workload: skip the 256-molecule batch (batched, per-molecule loop, learned warm start) added to the line")
     return ap.parse_args()
 
 
@@ -373,6 +374,8 @@ class BatchBench:
         torch.cuda.synchronize()
         it_plain, df_plain = its(), dfs()
         ms = {}
+        clocks = ClockSampler(torch.cuda.current_device())
+        clocks.start()
         for name, fn in (("learned", lambda: pl.run_layered(net)), ("layered_plain", lambda: pl.run_layered(None))):
             g = pl.capture(fn)
             g.replay()
@@ -387,10 +390,12 @@ class BatchBench:
             ms[name] = a.elapsed_time(b) / args.steps
             if name == "learned":
                 it_l, df_l = its(), dfs()
+        clk = clocks.stop()
         dd = np.concatenate([np.abs(x - y).ravel() for x, y in zip(df_l, df_plain)])
         net.close()
         pl.close()
         return {
+            "clocks": clk,
             "ms_per_step": ms["learned"],
             "value": self.units / (ms["learned"] * 1e-3),
             "speedup_vs_plain_gpu_loop": plain_loop_ms / ms["learned"],
@@ -401,6 +406,7 @@ class BatchBench:
         }
 
     def plain_ms(self, reps=3):
+        """The per-molecule loop (best of reps, CUDA events) and the clocks seen meanwhile."""
         pls = self.BT.plain_loop(self.systems, self.w, self.relax)
         torch = self.torch
         for p in pls:
@@ -409,6 +415,8 @@ class BatchBench:
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         best = float("inf")
+        clocks = ClockSampler(torch.cuda.current_device())
+        clocks.start()
         for _ in range(reps):
             a.record()
             for p in pls:
@@ -416,6 +424,7 @@ class BatchBench:
             b.record()
             b.synchronize()
             best = min(best, a.elapsed_time(b))
+        self.plain_clocks = clocks.stop()
         return best
 
 
@@ -515,7 +524,7 @@ def run_batch(args, rank, world, local):
             "l2": "inputs larger than L2 (force fields %.2f GB)" % (job.npts * 16 / 1e9),
             "parallelism": f"replicas x{world}",
         },
-        "plain_gpu_loop": {"ms_per_step": plain, "value": job.units / (plain * 1e-3), "speedup_of_batched": plain / (1e3 * t_step_max / K)},
+        "plain_gpu_loop": {"ms_per_step": plain, "value": job.units / (plain * 1e-3), "speedup_of_batched": plain / (1e3 * t_step_max / K), "clocks": job.plain_clocks},
         "learned_warm_start": learned,
         "fire_iters_per_pixel_z": iters / job.units,
         "e2e": {"value": job.units * world * K / t_e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -569,48 +578,61 @@ def run_ours(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
 
-    # ---------------- device-resident steps
-    # a force field that fits in L2 is flushed from it between timed steps (256 MB written)
+    # ---------------- device-resident steps, pipelined: step k+1's force field runs while step
+    # k's relaxation finishes (two force-field grids and output sets, HighLevel.StepPipeline).
+    # A force field that fits in L2 is flushed from it before every timed step's force field
+    # (256 MB written on the force-field stream).
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if npts * 16 < 129e6 else None
+    sp = HL.StepPipeline(pl)
+
+    def device_step(timing=None):
+        if flush is not None:
+            with torch.cuda.stream(sp.s_ff):
+                flush.zero_()
+        return sp.step(timing=timing)
+
     for _ in range(args.warmup):
-        pl.run()
+        device_step()
+    sp.wait_idle()
     torch.cuda.synchronize()
     pl.counter.zero_()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    timing = []
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
     clocks.start()
     t0 = time.perf_counter()
-    for e0, e1, e2 in ev:
-        if flush is not None:
-            flush.zero_()
-        e0.record(st)
-        pl.build_ff()
-        e1.record(st)
-        pl.relax()
-        e2.record(st)
+    ev_a = torch.cuda.Event(enable_timing=True)
+    ev_b = torch.cuda.Event(enable_timing=True)
+    ev_a.record(st)
+    sp.start_after(ev_a)
+    for _ in range(args.steps):
+        device_step(timing)
+    sp.wait_idle(st)
+    ev_b.record(st)
     torch.cuda.synchronize()
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    t_ff = [a.elapsed_time(b) * 1e-3 for a, b, _ in ev]
-    t_rx = [b.elapsed_time(c) * 1e-3 for _, b, c in ev]
-    t_step = sum(a.elapsed_time(c) * 1e-3 for a, _, c in ev)
+    t_ff = [e[0].elapsed_time(e[1]) * 1e-3 for e in timing]
+    t_rx = [e[2].elapsed_time(e[3]) * 1e-3 for e in timing]
+    t_step = ev_a.elapsed_time(ev_b) * 1e-3
     iters_total = int(pl.counter.item())
     _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
 
     # ---------------- end to end through the host API.  Every step copies its own inputs in
-    # and its outputs out, through pinned slot k % 2.  The copies run on two more streams: the
-    # inputs of step k go in once step k-1's force field has read its inputs (during step
-    # k-1's relaxation), the outputs of step k come out while step k+1's force field runs
-    # (step k+1's relaxation waits for them); the host prepares step k while the GPU works and
-    # waits only for step k-2's outputs before reusing their slot.
-    pin_out = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in pl.out.items()} for _ in range(2)]
+    # and its outputs out, through pinned slot k % 2, on two more streams: the inputs of step k
+    # go in once step k-1's force field has read its inputs, the outputs of step k come out
+    # once its relaxation is done (step k+2's relaxation, which writes the same device output
+    # set, waits for that copy); the host prepares step k while the GPU works and waits only
+    # for step k-2's outputs before reusing their pinned slot.  Force fields and relaxations
+    # are pipelined as above.
+    out0 = sp.outs[0]
+    pin_out = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in out0.items()} for _ in range(2)]
     cs = torch.cuda.Stream()  # host -> device
     ds = torch.cuda.Stream()  # device -> host
     done = [None, None]
-    last = {"ff": None, "d2h": None}
+    last = {"ff": None}
     h2d = [0]
     kstep = [0]
 
@@ -625,24 +647,18 @@ def run_ours(args, rank, world, local):
             job.e2e_h2d(slot)
             inputs_in = torch.cuda.Event()
             inputs_in.record(cs)
-        st.wait_event(inputs_in)
         if flush is not None:
-            flush.zero_()
-        pl.build_ff()
-        last["ff"] = torch.cuda.Event()
-        last["ff"].record(st)
-        if last["d2h"] is not None:
-            st.wait_event(last["d2h"])
-        pl.relax()
-        relaxed = torch.cuda.Event()
-        relaxed.record(st)
+            with torch.cuda.stream(sp.s_ff):
+                flush.zero_()
+        j, out, ff_done, rx_done = sp.step(after=inputs_in)
+        last["ff"] = ff_done
         with torch.cuda.stream(ds):
-            ds.wait_event(relaxed)
-            for k, v in pl.out.items():
+            ds.wait_event(rx_done)
+            for k, v in out.items():
                 pin_out[slot][k].copy_(v, non_blocking=True)
             done[slot] = torch.cuda.Event()
             done[slot].record(ds)
-        last["d2h"] = done[slot]
+        sp.release(j, done[slot])
         kstep[0] += 1
 
     for _ in range(max(1, args.warmup)):
@@ -652,8 +668,12 @@ def run_ours(args, rank, world, local):
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
     a.record(st)
+    sp.start_after(a)
+    cs.wait_event(a)
+    ds.wait_event(a)
     for _ in range(args.steps):
         e2e_step()
+    sp.wait_idle(st)
     st.wait_stream(ds)  # the last outputs are on the host before the interval ends
     b.record(st)
     b.synchronize()
@@ -698,7 +718,7 @@ def run_ours(args, rank, world, local):
             from oracle import cpu_baseline
 
             s = cpu_baseline.sample_pipeline(w, budget_s=args.cpu_budget)
-            cpu = {"value": s["pixel_z_per_s"], "unit": UNIT, "cores": s["cores"], "kind": s["kind"], "sample": s["sample"], "seconds_full_job": s["seconds_full_job"]}
+            cpu = {"value": s["pixel_z_per_s"], "unit": UNIT, "cores": s["cores"], "cpu_model": s.get("cpu_model"), "kind": s["kind"], "sample": s["sample"], "seconds_full_job": s["seconds_full_job"]}
             if "ff_pairs_per_s" in s:
                 cpu["ff_grid_pt_atoms_per_s"] = s["ff_pairs_per_s"]
         except Exception as e:  # the baseline is reported, never fatal
@@ -713,8 +733,9 @@ def run_ours(args, rank, world, local):
             "fire": relax,
             "probe": {"klat": w["klat"], "krad": w["krad"], "r0": list(w["r0Probe"]), "Q": w["charge"]},
             "df": {"f0": w["f0Cantilever"], "k": w["kCantilever"], "A": w["Amplitude"]},
-            "l2": ("inputs larger than L2 (force field %.2f GB)" if npts * 16 >= 129e6 else "force field %.2f GB fits in L2: 256 MB written between steps to flush it") % (npts * 16 / 1e9),
+            "l2": ("inputs larger than L2 (force field %.2f GB)" if npts * 16 >= 129e6 else "force field %.2f GB fits in L2: 256 MB written before every step's force field to flush it") % (npts * 16 / 1e9),
             "relax_lanes_per_stroke": args.relax_tps or 1,
+            "steps": "pipelined: step k+1's force field runs while step k's relaxation finishes (two force-field grids and output sets, relaxations on a higher-priority stream); stage_ms are each kernel's own event-timed duration on its stream",
             "parallelism": f"replicas x{world}",
         }
     )
@@ -814,9 +835,30 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "grid": list(w["gridN"]), "scan": [len(xT), len(yT), len(zT)], "parallelism": "host cores"},
         "ff_grid_pt_atoms_per_s": info["ff_pairs_per_s"],
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": info["sample"], "seconds_full_job": info["seconds_full_job"]},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "cpu_model": info.get("cpu_model"), "kind": info["kind"], "sample": info["sample"], "seconds_full_job": info["seconds_full_job"]},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def extra_batch(args, rank, world, local):
+    """The 256-molecule batch measured in the default run (its own line's main figures): the
+    batched persistent launch, the plain per-molecule loop and the learned warm start, each
+    timed with CUDA events and with the clocks sampled meanwhile."""
+    import copy
+
+    a = copy.copy(args)
+    a.workload = "molecule_batch"
+    a.steps = min(args.steps, 5)
+    a.warmup = max(3, min(args.warmup, 3))
+    a.cpu_budget = args.cpu_budget / 2
+    line = run_batch(a, rank, world, local)
+    if line is None:
+        return None
+    keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "e2e", "fire_iters_per_pixel_z", "plain_gpu_loop", "learned_warm_start", "clocks", "cpu_baseline", "gpu_launches")
+    out = {k: line[k] for k in keep if k in line}
+    out["config"] = line["config"]
+    out["roofline"] = {k: line["roofline"][k] for k in ("kernel", "achieved", "peak", "unit", "frac")}
+    return out
 
 
 def main():
@@ -828,6 +870,8 @@ def main():
         line = run_batch(args, rank, world, local)
     else:
         line = run_ours(args, rank, world, local)
+        if line is not None and args.workload == "slab_molecule" and world == 1 and not args.no_extras:
+            line["extra_workloads"] = {"molecule_batch": extra_batch(args, rank, world, local)}
     if line is not None:
         print(json.dumps(line), flush=True)
 

@@ -440,7 +440,7 @@ void oc_relax_strokes(const int n[3], const double cell[9], const double *gridF,
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-#pragma omp parallel for schedule(dynamic, 4)
+#pragma omp parallel for schedule(static)
     for (int s = 0; s < nstroke; s++) {
         long long off = (long long)s * nstep * 3;
         int sum = oc_relax_stroke(&C, probeStart, relaxAlg, nstep, rTips + off, rs + off, fs + off,

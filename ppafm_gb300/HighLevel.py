@@ -359,6 +359,98 @@ def _scan_coords(self, stream=None):
     return self._coords[1]
 
 
+def _relax(self, stream=None, ff=None, out=None):
+    """The relaxed scan + Δf on ``ff`` (default: the pipeline's grid) into the output set
+    ``out`` (a dict filled on first use; default: the pipeline's own, ``self.out``)."""
+    ff = self.ff if ff is None else ff
+    own = out is None
+    res = relax_scan(ff, self.prm, *self._scan_coords(stream), pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out if own else out, stream=stream)
+    if own:
+        self.out = res
+    return res
+
+
+class StepPipeline:
+    """Back-to-back scans of one pipeline (``Pipeline`` or ``DensityOverlapPipeline``), each
+    step a full force field + relaxed scan + Δf of the pipeline's current inputs, with step
+    k+1's force field computed while step k's relaxation runs.
+
+    The relaxation of a scan is latency-bound: its time is set by its longest strokes, and for
+    most of it few SMs are busy.  So the steps alternate between ``nbuf`` force-field grids and
+    output sets; the force fields run in order on one stream and the relaxations in order on
+    another, of higher priority, so a relaxation's blocks are placed first and the force field
+    of the next step fills the SMs around them.  Step k's force field waits for the relaxation
+    that last read its grid (and for ``after``, e.g. the copy of the step's inputs); step k's
+    relaxation waits for its force field and for ``release``d events on its output set (e.g.
+    the copy of that set's previous outputs to the host).  Results are those of ``run()``."""
+
+    def __init__(self, pl, nbuf=2):
+        if nbuf < 1:
+            raise ValueError("nbuf >= 1")
+        self.pl = pl
+        self.nbuf = nbuf
+        self.ffs = [pl.ff] + [DeviceFF(pl.gridN, pl.lvec) for _ in range(nbuf - 1)]
+        self.outs = [{} for _ in range(nbuf)]
+        self.s_ff = torch.cuda.Stream()
+        _, high = torch.cuda.Stream.priority_range()
+        self.s_rx = torch.cuda.Stream(priority=high)
+        self._grid_free = [None] * nbuf  # relaxation that last read grid j
+        self._out_free = [None] * nbuf  # consumer of output set j (released)
+        self.k = 0
+
+    def step(self, after=None, timing=None):
+        """Queues one step into slot k % nbuf; returns (slot, outputs, force-field done event,
+        relaxation done event).  timing: a list that gets (ff start, ff end, relax start,
+        relax end) timing events of this step."""
+        j = self.k % self.nbuf
+        sf, sr = self.s_ff, self.s_rx
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if timing is not None else None
+        with torch.cuda.stream(sf):
+            if self._grid_free[j] is not None:
+                sf.wait_event(self._grid_free[j])
+            if after is not None:
+                sf.wait_event(after)
+            if ev:
+                ev[0].record(sf)
+            self.pl.build_ff(stream=sf, ff=self.ffs[j])
+            ff_done = torch.cuda.Event()
+            ff_done.record(sf)
+            if ev:
+                ev[1].record(sf)
+        with torch.cuda.stream(sr):
+            sr.wait_event(ff_done)
+            if self._out_free[j] is not None:
+                sr.wait_event(self._out_free[j])
+            if ev:
+                ev[2].record(sr)
+            out = self.pl.relax(stream=sr, ff=self.ffs[j], out=self.outs[j])
+            rx_done = torch.cuda.Event()
+            rx_done.record(sr)
+            if ev:
+                ev[3].record(sr)
+        self._grid_free[j] = rx_done
+        self._out_free[j] = None
+        if ev:
+            timing.append(ev)
+        self.k += 1
+        return j, out, ff_done, rx_done
+
+    def release(self, j, event):
+        """Output set j is written again only after ``event``."""
+        self._out_free[j] = event
+
+    def wait_idle(self, stream=None):
+        """``stream`` (default: the current one) waits for every queued step."""
+        s = stream if stream is not None else torch.cuda.current_stream()
+        s.wait_stream(self.s_ff)
+        s.wait_stream(self.s_rx)
+
+    def start_after(self, event):
+        """The next steps start only after ``event`` (e.g. the start of a timed interval)."""
+        self.s_ff.wait_event(event)
+        self.s_rx.wait_event(event)
+
+
 class Pipeline:
     """The reference CPU pipeline (computeLJ + computeELFF_pointCharge with the default
     clamp, perform_relaxation, Fz2df) as device-resident stages.  Build once per system,
@@ -397,24 +489,24 @@ class Pipeline:
         if self.tip != "s" and self.Q != 0.0:
             self.atoms_el, _, self.nch_el = pack_atoms(self.Rs0, None, self.kqq, stream=stream)
 
-    def build_ff(self, stream=None):
+    def build_ff(self, stream=None, ff=None):
+        """The force field into ``ff`` (default: the pipeline's own grid)."""
+        ff = self.ff if ff is None else ff
         if self.Q == 0.0:
-            self.ff.compute(self.atoms, self.natoms, 0, FF_LJ, stream=stream).clamp(Fmax_DEFAULT, stream=stream)
+            ff.compute(self.atoms, self.natoms, 0, FF_LJ, stream=stream).clamp(Fmax_DEFAULT, stream=stream)
         elif self.tip == "s":
-            self.ff.compute(self.atoms, self.natoms, self.ncharged, FF_LJC, Q=self.Q, Fmax=Fmax_DEFAULT, stream=stream)
+            ff.compute(self.atoms, self.natoms, self.ncharged, FF_LJC, Q=self.Q, Fmax=Fmax_DEFAULT, stream=stream)
         else:
-            self.ff.compute(self.atoms, self.natoms, 0, FF_LJ, stream=stream).clamp(Fmax_DEFAULT, stream=stream)
+            ff.compute(self.atoms, self.natoms, 0, FF_LJ, stream=stream).clamp(Fmax_DEFAULT, stream=stream)
             if self.ff_el is None:
                 self.ff_el = DeviceFF(self.gridN, self.lvec)
             self.ff_el.compute(self.atoms_el, self.natoms, self.nch_el, FF_COULOMB, kind=TIP_KINDS[self.tip], stream=stream).clamp(Fmax_DEFAULT, stream=stream)
-            self.ff.axpby(1.0, self.ff_el, self.Q, stream=stream)
-        return self.ff
+            ff.axpby(1.0, self.ff_el, self.Q, stream=stream)
+        return ff
 
     _scan_coords = _scan_coords
+    relax = _relax
 
-    def relax(self, stream=None):
-        self.out = relax_scan(self.ff, self.prm, *self._scan_coords(stream), pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
-        return self.out
 
     def run(self, stream=None):
         self.build_ff(stream)
@@ -501,24 +593,23 @@ class DensityOverlapPipeline:
         for dst, src in ((self.rho_s, rho_s), (self.rho_q, rho_q), (self.rho_t, rho_t)):
             dst.copy_(torch.as_tensor(np.asarray(src, dtype=np.float32) if not torch.is_tensor(src) else src))
 
-    def build_ff(self, stream=None):
+    def build_ff(self, stream=None, ff=None):
+        """The force field into ``ff`` (default: the pipeline's own grid)."""
+        ff = self.ff if ff is None else ff
         g = self.fft
         with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
             self._ws.copy_(self.rho_s)
             self._wt.copy_(self.rho_t)
         g.density_power(self._ws, self.B, self.fix_negative, stream=stream)
         g.density_power(self._wt, self.B, self.fix_negative, stream=stream)
-        g.potential2forces(self._ws, self._wt, self.lvec, FE=self.ff.FE, scale=self.A, with_E=True, stream=stream)
+        g.potential2forces(self._ws, self._wt, self.lvec, FE=ff.FE, scale=self.A, with_E=True, stream=stream)
         if self.Q != 0.0:
             g.poisson(self.rho_q, self.lvec, out=self.V, stream=stream)
-            g.potential2forces(self.V, self.rho_t, self.lvec, FE=self.ff.FE, scale=self.Q / self.Ne, with_E=True, accumulate=True, stream=stream)
-        return self.ff
+            g.potential2forces(self.V, self.rho_t, self.lvec, FE=ff.FE, scale=self.Q / self.Ne, with_E=True, accumulate=True, stream=stream)
+        return ff
 
     _scan_coords = _scan_coords
-
-    def relax(self, stream=None):
-        self.out = relax_scan(self.ff, self.prm, *self._scan_coords(stream), pos_offset=self.lvec[0], df_weights=self.W, want_ppos=self.want_ppos, want_iters=self.want_iters, counter=self.counter, out=self.out, stream=stream)
-        return self.out
+    relax = _relax
 
     def run(self, stream=None):
         self.build_ff(stream)

@@ -90,6 +90,7 @@ SIGNATURES = {
     "ppgpu_batch_iterations": ([c_void_p, POINTER(c_ulonglong), c_void_p], c_int),
     "ppgpu_batch_destroy": ([c_void_p], c_int),
     "ppgpu_batch_set_wait": ([c_void_p, c_double, c_int], c_int),
+    "ppgpu_set_ff_block": ([c_int], c_int),
     "ppgpu_batch_run_layered": ([c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p], c_int),
     "ppgpu_batch_layer_info": ([c_void_p, POINTER(c_longlong)], c_int),
     "ppgpu_tc_selftest": ([c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p], c_int),

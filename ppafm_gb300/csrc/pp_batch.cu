@@ -50,6 +50,7 @@ struct BatchJob {  // device copy, one per system
     int natoms, ncharged;
     int n0, n1, n2;
     double dA[3], dB[3], dC[3];
+    float off[3][FF_MAX_P];  // float(dC[c] * i) (FFParams::off)
     long long nchunks;
     int nzc;
     int ff_blocks;
@@ -134,6 +135,10 @@ __device__ __forceinline__ FFParams ff_params_of(const BatchJob &J, const BatchP
         p.dB[k] = J.dB[k];
         p.dC[k] = J.dC[k];
     }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int i = 0; i < FF_MAX_P; i++) p.off[c][i] = J.off[c][i];
     p.eps = 1.0e-8f;
     p.eps64 = (double)1.0e-8f;
     p.Q = B.Q;
@@ -973,6 +978,8 @@ extern "C" int ppgpu_batch_create(const ppgpu_batch_job *jobs, int njobs, const 
             b.dB[k] = g.dcell[3 + k];
             b.dC[k] = g.dcell[6 + k];
         }
+        for (int c = 0; c < 3; c++)
+            for (int i = 0; i < FF_MAX_P; i++) b.off[c][i] = (float)(b.dC[c] * i);
         b.nzc = (b.n2 + 7) / 8;  // P = 8 points per thread (P2 = 4)
         b.nchunks = (long long)b.n0 * b.n1 * b.nzc;
         b.ff_blocks = (int)((b.nchunks + BATCH_THREADS - 1) / BATCH_THREADS);

@@ -36,12 +36,12 @@
 
 namespace ppgpu {
 
-template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT>
-__global__ void __launch_bounds__(FF_THREADS) ff_kernel(const FFParams prm) {
+template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) ff_kernel(const FFParams prm) {
     __shared__ __align__(128) FFShared sh;
     ff_shared_init(sh);
     uint32_t T = 0;
-    ff_block<MODE, WITH_E, ORTHO, P2, SPLIT>(prm, (long long)blockIdx.x, sh, T);
+    ff_block<MODE, WITH_E, ORTHO, P2, SPLIT, NT>(prm, (long long)blockIdx.x, sh, T);
 }
 
 // ------------------------------------------------------------- float64 kernel
@@ -203,17 +203,34 @@ static int ff64_dispatch(const FFParams &prm, int mode, int kind, cudaStream_t s
 
 // ------------------------------------------------------------------------ host
 
+// Threads per CTA of the single-grid kernel (ppgpu_set_ff_block): 0 = by atom count.  Every
+// CTA waits for its first atom tile and sets up its points before summing, so with few atoms
+// the larger CTA (256 threads, 2048 points) amortises that better; with many atoms that cost
+// vanishes and the smaller CTA (128 threads) packs more evenly, also beside the blocks of a
+// relaxation running on another stream.
+static int g_ff_block = 0;
+constexpr int FF_SMALL_SYSTEM_ATOMS = 4096;
+
+template <int MODE, bool WITH_E, int P2, bool SPLIT, int NT>
+static void launch_ff_nt(const FFParams &prm, bool ortho, long long nblk, cudaStream_t st) {
+    if (ortho)
+        ff_kernel<MODE, WITH_E, true, P2, SPLIT, NT><<<(unsigned)nblk, NT, 0, st>>>(prm);
+    else
+        ff_kernel<MODE, WITH_E, false, P2, SPLIT, NT><<<(unsigned)nblk, NT, 0, st>>>(prm);
+}
+
 template <int MODE, bool WITH_E, int P2, bool SPLIT>
 static int launch_ff(FFParams &prm, bool ortho, cudaStream_t st) {
     prm.nzc = (prm.ns[2] + 2 * P2 - 1) / (2 * P2);
     prm.nchunks = (long long)prm.ns[0] * prm.ns[1] * prm.nzc;
-    const long long nblk = (prm.nchunks + FF_THREADS - 1) / FF_THREADS;
+    const int nt = g_ff_block ? g_ff_block : (prm.natoms <= FF_SMALL_SYSTEM_ATOMS ? 256 : 128);
+    const long long nblk = (prm.nchunks + nt - 1) / nt;
     if (nblk <= 0) return set_ok();
     if (nblk > 0x7fffffffLL) return set_error(PPGPU_ERR_ARG, "ff grid too large (%lld blocks)", nblk);
-    if (ortho)
-        ff_kernel<MODE, WITH_E, true, P2, SPLIT><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+    if (nt == 256)
+        launch_ff_nt<MODE, WITH_E, P2, SPLIT, 256>(prm, ortho, nblk, st);
     else
-        ff_kernel<MODE, WITH_E, false, P2, SPLIT><<<(unsigned)nblk, FF_THREADS, 0, st>>>(prm);
+        launch_ff_nt<MODE, WITH_E, P2, SPLIT, 128>(prm, ortho, nblk, st);
     PPGPU_CHECK_LAUNCH("ff_kernel launch");
     return set_ok();
 }
@@ -315,6 +332,7 @@ extern "C" int ppgpu_ff_subgrid(float *FE, const int *n, const double *cell, con
         prm.dB[k] = g.dcell[3 + k];
         prm.dC[k] = g.dcell[6 + k];
     }
+    ff_set_offsets(prm);
     // Forces.h:12 (R2SAFE = 1e-8 for the CPU core) and FF.cl:1 (1e-6 for the OpenCL grid).
     prm.eps = (mode == PPGPU_FF_QZS) ? 1e-6f : 1.0e-8f;
     prm.eps64 = (mode == PPGPU_FF_QZS) ? (double)1e-6f : (double)1.0e-8f;
@@ -348,6 +366,13 @@ extern "C" int ppgpu_ff_subgrid(float *FE, const int *n, const double *cell, con
     }
     if (flags & PPGPU_FF_F64) return ff64_dispatch(prm, mode, coul_kind, (cudaStream_t)stream);
     return ff_dispatch(prm, mode, coul_kind, with_e, ortho, (cudaStream_t)stream);
+}
+
+extern "C" int ppgpu_set_ff_block(int threads) {
+    if (threads != 0 && threads != 128 && threads != 256)
+        return set_error(PPGPU_ERR_ARG, "set_ff_block: %d not in {0 (by atom count), 128, 256}", threads);
+    g_ff_block = threads;
+    return set_ok();
 }
 
 extern "C" int ppgpu_ff_grid(float *FE, const int *n, const double *cell, const float *atoms, int natoms,
@@ -482,6 +507,7 @@ extern "C" int ppgpu_lj_grid_f64_noalloc(double *gridF, double *gridE, const int
         prm.dB[k] = g.dcell[3 + k];
         prm.dC[k] = g.dcell[6 + k];
     }
+    ff_set_offsets(prm);
     prm.eps = 1.0e-8f;
     prm.eps64 = (double)1.0e-8f;
     prm.err = err;

@@ -10,11 +10,13 @@
 
 namespace ppgpu {
 
-constexpr int FF_THREADS = 256;
+constexpr int FF_THREADS = 256;   // CTA of the persistent batched kernel (the single-grid kernel
+                                  // picks 128 or 256 per call, pp_ff.cu)
 constexpr int FF_TILE = 256;       // atoms per shared-memory stage
 constexpr int FF_REC = 3;          // float4 per atom record
 constexpr float R2CAP = 1e-4f;     // slow-path floor of r^2 (A^2)
 constexpr int SPLIT_MAX_CHARGED = 1024;  // LJC: charged atoms summed single-level up to this
+constexpr int FF_MAX_P = 8;               // points per thread (z run), at most
 
 enum { M_LJ = 0, M_COUL = 1, M_LJC = 2, M_QZS = 3 };
 
@@ -35,7 +37,14 @@ struct FFParams {
     long long nchunks;
     int nzc;
     int *err;
+    float off[3][FF_MAX_P];  // float(dC[c] * i): offsets of a thread's points from its first one
 };
+
+// Fills prm.off from prm.dC (host).
+inline void ff_set_offsets(FFParams &prm) {
+    for (int c = 0; c < 3; c++)
+        for (int i = 0; i < FF_MAX_P; i++) prm.off[c][i] = (float)(prm.dC[c] * i);
+}
 
 // ------------------------------------------------------------------ TMA helpers
 
@@ -191,6 +200,27 @@ __device__ __forceinline__ void lj_ir2(float2 ir2, float2 dx, float2 dy, float2 
     if (WITH_E) a.e[p] = fma2(fma2(c12, ir6, c6n), ir6, a.e[p]);  // c12 ir12 - c6 ir6
 }
 
+// LJ + Coulomb of one charged atom on pair p from ir = 1/r: ir^3 is formed once and serves
+// both, ir^6 = (ir^3)^2 for the LJ powers and kqq ir^3 for the Coulomb factor (the energy,
+// when wanted, adds kqq ir): 7 multiplies/FMAs before the six accumulations.
+template <bool WITH_E, int P2>
+__device__ __forceinline__ void ljc_ir(float2 ir, float2 dx, float2 dy, float2 dz, float2 c6n6, float2 c12x12,
+                                       float2 c6n, float2 c12, float2 kqq, Acc<P2> &a, Acc<P2> &u, int p) {
+    const float2 ir2 = mul2(ir, ir);
+    const float2 ir3 = mul2(ir, ir2);
+    const float2 ir6 = mul2(ir3, ir3);
+    const float2 fr = mul2(fma2(c12x12, ir6, c6n6), mul2(ir6, ir2));  // (12 c12 ir6 - 6 c6) ir8
+    a.x[p] = fma2(fr, dx, a.x[p]);
+    a.y[p] = fma2(fr, dy, a.y[p]);
+    a.z[p] = fma2(fr, dz, a.z[p]);
+    if (WITH_E) a.e[p] = fma2(fma2(c12, ir6, c6n), ir6, a.e[p]);
+    const float2 fq = mul2(kqq, ir3);
+    u.x[p] = fma2(fq, dx, u.x[p]);
+    u.y[p] = fma2(fq, dy, u.y[p]);
+    u.z[p] = fma2(fq, dz, u.z[p]);
+    if (WITH_E) u.e[p] = fma2(kqq, ir, u.e[p]);
+}
+
 // Coulomb (Forces.h:237-244) of one atom on pair p, from ir = 1/r.
 template <bool WITH_E, int P2>
 __device__ __forceinline__ void coul_ir(float2 ir, float2 ir2, float2 dx, float2 dy, float2 dz, float2 kqq,
@@ -338,7 +368,7 @@ __device__ float4 point_slow(const FFParams &prm, double px, double py, double p
 // LJ partial and total sums (used when the charged atoms are at most SPLIT_MAX_CHARGED
 // and the output is not accumulated).
 //
-// ff_block computes the points of block `blk` (FF_THREADS chunks of P points) of the grid
+// ff_block computes the points of block `blk` (NT chunks of P points; NT = the CTA's threads) of the grid
 // described by prm.  The shared stages and their mbarriers belong to the calling kernel and
 // are initialised once per kernel; T counts the atom tiles this CTA has consumed so far
 // (stage = T & 1, mbarrier phase parity = (T >> 1) & 1), so a persistent CTA can run many
@@ -359,7 +389,7 @@ __device__ __forceinline__ void ff_shared_init(FFShared &sh) {
     __syncthreads();
 }
 
-template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT>
+template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT, int NT = FF_THREADS>
 __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFShared &sh, uint32_t &T) {
     constexpr int P = 2 * P2;
     auto &s_at = sh.at;
@@ -368,7 +398,7 @@ __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFS
     const uint32_t T0 = T;
 
     const int tid = threadIdx.x;
-    const long long chunk = blk * FF_THREADS + tid;
+    const long long chunk = blk * NT + tid;
     const bool valid = chunk < prm.nchunks;
 
     // ---- this thread's points: column (ga, gb), z points gc0 .. gc0+P-1
@@ -392,9 +422,9 @@ __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFS
         q.lz = __double2float_rn(pd[2] - (double)hz);
 #pragma unroll
         for (int p = 0; p < P2; p++) {
-            q.ox[p] = make_float2(__double2float_rn(prm.dC[0] * (2 * p)), __double2float_rn(prm.dC[0] * (2 * p + 1)));
-            q.oy[p] = make_float2(__double2float_rn(prm.dC[1] * (2 * p)), __double2float_rn(prm.dC[1] * (2 * p + 1)));
-            q.oz[p] = make_float2(__double2float_rn(prm.dC[2] * (2 * p)), __double2float_rn(prm.dC[2] * (2 * p + 1)));
+            q.ox[p] = make_float2(prm.off[0][2 * p], prm.off[0][2 * p + 1]);
+            q.oy[p] = make_float2(prm.off[1][2 * p], prm.off[1][2 * p + 1]);
+            q.oz[p] = make_float2(prm.off[2][2 * p], prm.off[2][2 * p + 1]);
         }
     }
 
@@ -481,10 +511,7 @@ __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFS
             for (int p = 0; p < P2; p++) {
                 float2 dx, dy, dz, r2;
                 pair_geo<ORTHO, P2>(q, g, p, eps, dx, dy, dz, r2);
-                const float2 ir = rsqrt2(r2);
-                const float2 ir2 = mul2(ir, ir);
-                lj_ir2<WITH_E, P2>(ir2, dx, dy, dz, c6n6, c12x12, c6n, c12, a, p);
-                coul_ir<WITH_E, P2>(ir, ir2, dx, dy, dz, kqq, u, p);
+                ljc_ir<WITH_E, P2>(rsqrt2(r2), dx, dy, dz, c6n6, c12x12, c6n, c12, kqq, a, u, p);
             }
         }
     };

@@ -125,7 +125,7 @@ def test_batch_output_sets(gpulib):
 
 def test_batch_system_vs_oracle(gpulib, oracle):
     from ppafm_gb300.batch import BatchPipeline
-    from tests.conftest import rel_err
+    from tests.conftest import check_ff, grid_coords
     from tests.test_gpu_pipeline import _oracle_pipeline
     from tests.test_gpu_relax import _check_positions
 
@@ -136,7 +136,10 @@ def test_batch_system_vs_oracle(gpulib, oracle):
     FF, fzs, pp, df, it = _oracle_pipeline(oracle, w, relax)
     s = bp.systems[1]
     Fg = s["FE"].view(tuple(s["n"]) + (4,))[..., :3].cpu().numpy()
-    assert rel_err(Fg, FF, 1e-2) < 1e-5
+    from ppafm_gb300 import HighLevel as HL
+
+    Rs0, cLJs, kqq = HL.prepare_atoms(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w)
+    check_ff("batched system LJ+Coulomb force field", Fg.astype(np.float64), FF, grid_coords(s["n"], w["lvec"]), Rs0, cLJs, kqq, params["charge"])
     out = bp.outputs(1)
     _check_positions(np.linalg.norm(out["ppos"].cpu().numpy() - pp, axis=-1))
     assert np.abs(out["df"].cpu().numpy() - df).max() < 0.1

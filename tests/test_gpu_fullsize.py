@@ -3,7 +3,7 @@ molecule workload (the headline: 800x800x500 grid, 18 540 atoms with images, 512
 scan) by sampling, each against the oracle (the float64 restatement of the reference core,
 bit-identical to it).
 
-Force grids (``_check_ff``): every point within 1e-5 relative of the oracle
+Force grids (``tests.conftest.check_ff``): every point within 1e-5 relative of the oracle
 (|dF| <= 1e-5 * max(|F|, 1e-2 eV/A)), except where that is finer than float32 can resolve:
 a float32 evaluation of a sum of pair terms carries an error of a few ulps of the terms'
 magnitudes, sum_i |F_i|, so where the terms cancel (|F| << sum_i |F_i|: between atoms, and
@@ -33,47 +33,17 @@ import time
 import numpy as np
 import pytest
 
-from tests.conftest import rel_err
+from tests.conftest import check_ff, rel_err
 from tests.test_gpu_relax import _check_end_to_end, _check_positions
 
 pytestmark = pytest.mark.gpu
 
-FF_TOL = 1e-5
 FLOOR = 1e-2
-SUM_ULPS = 2.0**-20  # 16 float32 ulps (u = 2^-24)
-SUM_CLAUSE_FRAC = 1e-3
 DF_TOL = 0.1
 
 
-def _term_magnitudes(pts, Rs0, cLJs, kqq, Q):
-    """sum_i |F_LJ,i(p)| + |Q| sum_i |F_el,i(p)| at points p (grid-origin frame), float64."""
-    out = np.zeros(len(pts))
-    for k, p in enumerate(pts):
-        d = p[None, :] - Rs0
-        r2 = np.einsum("ij,ij->i", d, d) + 1e-8
-        ir2 = 1.0 / r2
-        ir6 = ir2**3
-        flj = np.abs((12.0 * cLJs[:, 1] * ir6 - 6.0 * cLJs[:, 0]) * ir6 * ir2) * np.sqrt(r2)
-        out[k] = flj.sum() + abs(Q) * (np.abs(kqq) * ir2).sum()
-    return out
-
-
 def _check_ff(name, got, ref, coords, pl):
-    """Applies the force-grid bar to grids [..., 3]; coords(idx) gives the grid-origin-frame
-    positions of index tuples.  Prints the float32 error."""
-    d = np.linalg.norm(got - ref, axis=-1)
-    m = np.linalg.norm(ref, axis=-1)
-    err = d / np.maximum(m, FLOOR)
-    over = np.argwhere(err > FF_TOL)
-    worst_sum = 0.0
-    if len(over):
-        assert len(over) <= SUM_CLAUSE_FRAC * err.size, f"{name}: {len(over)} of {err.size} points beyond {FF_TOL} relative"
-        S = _term_magnitudes(coords(over), pl.Rs0, pl.cLJs, pl.kqq, pl.Q)
-        ratio = d[tuple(over.T)] / (SUM_ULPS * S)
-        worst_sum = float(ratio.max())
-        assert worst_sum <= 1.0, f"{name}: a point beyond both 1e-5 relative and the float32 summation bound ({worst_sum:.2f} of it)"
-    print(f"{name}: float32 max rel err {err.max():.2e}; {len(over)} of {err.size} points past 1e-5 (within {worst_sum:.2f} of the float32 summation bound)")
-    return err.max()
+    return check_ff(name, got, ref, coords, pl.Rs0, pl.cLJs, pl.kqq, pl.Q)
 
 
 def _relax_params(w):

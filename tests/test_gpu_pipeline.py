@@ -37,9 +37,9 @@ def test_small_molecule_pipeline_vs_oracle(gpulib, oracle):
     pl = HL.Pipeline(w["Zs"], w["Rs"], w["Qs"], w["lvec"], w["gridN"], w, relax=relax, want_iters=True)
     out = pl.run()
     Fg, _ = pl.ff.to_host()
-    from tests.conftest import rel_err
+    from tests.conftest import check_ff, grid_coords
 
-    assert rel_err(Fg, FF, 1e-2) < 1e-5
+    check_ff("small molecule (scaled) LJ+Coulomb force field", Fg, FF, grid_coords(w["gridN"], w["lvec"]), pl.Rs0, pl.cLJs, pl.kqq, pl.Q)
     ppg = out["ppos"].cpu().numpy()
     dpos = np.linalg.norm(ppg - pp, axis=-1)
     from tests.test_gpu_relax import _check_positions
@@ -168,3 +168,47 @@ def test_afmulator_hartree_point_charge_tip_vs_oracle(gpulib, oracle, matching):
     # the tip charges matter: without them the image differs
     afm0 = AFMulator(**kw, Qs=[0, 0, 0, 0])
     assert np.abs(afm0.eval(xyzs, Zs, HartreePotential(pot, lvp)) - X).max() > 0.1
+
+
+def test_step_pipeline_matches_run(gpulib):
+    """HighLevel.StepPipeline (step k+1's force field on its own stream while step k relaxes,
+    two grids and output sets) gives run()'s results bit for bit, with the inputs alternating
+    between two molecules: each step's atoms go in on a third stream after the previous
+    force field has read the atom buffer, and the outputs of each step are checked."""
+    import torch
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import workloads
+
+    w = workloads.small_molecule(seed=2, scale=0.3)
+    relax = dict(maxIters=w["maxIters"], convF2=w["convF2"], dt=w["dt"], damping=w["damping"])
+    w2 = dict(w, Rs=w["Rs"] + np.array([0.37, -0.21, 0.05]))
+    ref, recs = [], []
+    for ww in (w, w2):
+        pl = HL.Pipeline(ww["Zs"], ww["Rs"], ww["Qs"], ww["lvec"], ww["gridN"], ww, relax=relax, want_iters=True)
+        ref.append({k: v.clone() for k, v in pl.run().items()})
+        recs.append(pl.atoms.clone())
+    assert not torch.equal(ref[0]["ppos"], ref[1]["ppos"])
+    sp = HL.StepPipeline(pl)  # pl holds w2's atoms; every step below loads its own
+    cs = torch.cuda.Stream()
+    last_ff, steps = None, []
+    for k in range(6):
+        with torch.cuda.stream(cs):
+            if last_ff is not None:
+                cs.wait_event(last_ff)
+            pl.atoms.copy_(recs[k % 2], non_blocking=True)
+            loaded = torch.cuda.Event()
+            loaded.record(cs)
+        j, out, last_ff, rx = sp.step(after=loaded)
+        snap = torch.cuda.Stream()
+        with torch.cuda.stream(snap):  # keep a copy of this step's outputs before set j is reused
+            snap.wait_event(rx)
+            steps.append({key: v.clone() for key, v in out.items()})
+            copied = torch.cuda.Event()
+            copied.record(snap)
+        sp.release(j, copied)
+    sp.wait_idle()
+    torch.cuda.synchronize()
+    for k, got in enumerate(steps):
+        for key, v in ref[k % 2].items():
+            assert torch.equal(got[key], v), (k, key)
