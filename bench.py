@@ -175,8 +175,12 @@ class PointChargeJob:
         self.nch = self.pl.ncharged
         self.ff_name = "ff_kernel<LJC> (force field)" if self.pl.Q != 0.0 else "ff_kernel<LJ> (force field)"
         self.launches_per_step = 2
-        self.rec_pinned = [torch.empty(self.pl.atoms.shape, dtype=self.pl.atoms.dtype, pin_memory=True) for _ in range(2)]
+        self.pinned_slots(2)
         self.host_in = {k: np.asarray(w[k]).copy() for k in ("Zs", "Rs", "Qs")}
+
+    def pinned_slots(self, n):
+        """n pinned host buffers for the atom records of steps in flight."""
+        self.rec_pinned = [self.torch.empty(self.pl.atoms.shape, dtype=self.pl.atoms.dtype, pin_memory=True) for _ in range(n)]
 
     def e2e_host(self, slot=0):
         """Host prep of one step (PBC images, LJ mixing, packing into pinned slot `slot`);
@@ -222,6 +226,9 @@ class OverlapJob:
         self.host = [torch.empty(self.pl.gridN, dtype=torch.float32, pin_memory=True) for _ in range(3)]
         for h, d in zip(self.host, (self.pl.rho_s, self.pl.rho_q, self.pl.rho_t)):
             h.copy_(d)
+
+    def pinned_slots(self, n):
+        """The density grids stay in one pinned set: every step copies the same host arrays."""
 
     def e2e_host(self, slot=0):
         """Nothing to prepare: the density grids are pinned host arrays; returns their bytes."""
@@ -583,7 +590,8 @@ def run_ours(args, rank, world, local):
     # A force field that fits in L2 is flushed from it before every timed step's force field
     # (256 MB written on the force-field stream).
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if npts * 16 < 129e6 else None
-    sp = HL.StepPipeline(pl)
+    NSLOT = 3  # grids, device output sets and pinned host slots in flight
+    sp = HL.StepPipeline(pl, nbuf=NSLOT)
 
     def device_step(timing=None):
         if flush is not None:
@@ -621,23 +629,24 @@ def run_ours(args, rank, world, local):
     _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
 
     # ---------------- end to end through the host API.  Every step copies its own inputs in
-    # and its outputs out, through pinned slot k % 2, on two more streams: the inputs of step k
-    # go in once step k-1's force field has read its inputs, the outputs of step k come out
-    # once its relaxation is done (step k+2's relaxation, which writes the same device output
-    # set, waits for that copy); the host prepares step k while the GPU works and waits only
-    # for step k-2's outputs before reusing their pinned slot.  Force fields and relaxations
-    # are pipelined as above.
+    # and its outputs out, through pinned slot k % NSLOT, on two more streams: the inputs of step
+    # k go in once step k-1's force field has read its inputs, the outputs of step k come out
+    # once its relaxation is done (step k+NSLOT's relaxation, which writes the same device
+    # output set, waits for that copy); the host prepares step k while the GPU works and waits
+    # only for step k-NSLOT's outputs before reusing their pinned slot.  Force fields and
+    # relaxations are pipelined as above.
     out0 = sp.outs[0]
-    pin_out = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in out0.items()} for _ in range(2)]
+    pin_out = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in out0.items()} for _ in range(NSLOT)]
+    job.pinned_slots(NSLOT)
     cs = torch.cuda.Stream()  # host -> device
     ds = torch.cuda.Stream()  # device -> host
-    done = [None, None]
+    done = [None] * NSLOT
     last = {"ff": None}
     h2d = [0]
     kstep = [0]
 
     def e2e_step():
-        slot = kstep[0] % 2
+        slot = kstep[0] % NSLOT
         if done[slot] is not None:
             done[slot].synchronize()
         h2d[0] = job.e2e_host(slot)
@@ -735,7 +744,7 @@ def run_ours(args, rank, world, local):
             "df": {"f0": w["f0Cantilever"], "k": w["kCantilever"], "A": w["Amplitude"]},
             "l2": ("inputs larger than L2 (force field %.2f GB)" if npts * 16 >= 129e6 else "force field %.2f GB fits in L2: 256 MB written before every step's force field to flush it") % (npts * 16 / 1e9),
             "relax_lanes_per_stroke": args.relax_tps or 1,
-            "steps": "pipelined: step k+1's force field runs while step k's relaxation finishes (two force-field grids and output sets, relaxations on a higher-priority stream); stage_ms are each kernel's own event-timed duration on its stream",
+            "steps": "pipelined: step k+1's force field runs while step k's relaxation finishes (three force-field grids and output sets in flight, relaxations on a higher-priority stream); stage_ms are each kernel's own event-timed duration on its stream",
             "parallelism": f"replicas x{world}",
         }
     )

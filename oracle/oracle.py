@@ -757,15 +757,15 @@ class AFMulator:
         self.dfWeight = get_simple_df_weight(df_steps, dz=self.dz).astype(np.float32)
         self.dfWeight *= eVA_Nm * f0Cantilever / kCantilever
 
-    def eval(self, xyzs, Zs, qs, sample_lvec=None, nthreads=0, return_all=False, pot=None, rho=None, sigma=0.71, rot=np.eye(3)):
+    def eval(self, xyzs, Zs, qs, sample_lvec=None, nthreads=0, return_all=False, pot=None, rho=None, sigma=0.71, rot=np.eye(3), REAs=None):
         """pot = (array [n0,n1,n2], lvec [4,3]) selects the Hartree route with the multipole tip
         density rho (dict), or with the point-charge tip when rho is None; otherwise point
-        charges qs."""
+        charges qs.  REAs: per-atom (R, E, alpha) pair parameters (default: from FFparams)."""
         if pot is not None:
             sample_lvec = np.asarray(pot[1])[1:] if sample_lvec is None else sample_lvec
             qs = np.zeros(len(Zs))
         npbc = self.npbc if sample_lvec is not None else (0, 0, 0)
-        REAs = getAtomsREA(self.iZPP, Zs, self.FFparams)
+        REAs = getAtomsREA(self.iZPP, Zs, self.FFparams) if REAs is None else np.asarray(REAs, np.float64)
         cLJs = REA2LJ(REAs)
         xyzs = np.asarray(xyzs, np.float64)
         qs = np.asarray(qs, np.float64)
