@@ -37,6 +37,7 @@ METRIC = "relaxed pixel-z points/s & FF grid-pt·atoms/s; FIRE iters/pixel at 1e
 UNIT = "pixel-z/s"
 FLOPS_LJ_PAIR = 26  # float32 flops per atom-point pair, FMA = 2 (LJ only)
 FLOPS_LJC_PAIR = 30  # LJ + Coulomb sharing r^2
+FLOPS_TIP_CHARGE_PAIR = 20  # one AFMulator tip charge on one atom (FF.cl evalLJC_QZs_noPos)
 
 
 def parse():
@@ -44,7 +45,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap", "molecule_batch"])
+    ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap", "molecule_batch", "afmulator"])
     ap.add_argument("--nmol", type=int, default=256)
     ap.add_argument("--no-learned", action="store_true", help="molecule_batch: skip the learned warm start")
     ap.add_argument("--tuning", default=None, help="molecule_batch launch shape 'ctas_per_sm,tile_w,tile_h,chunk' (default: autotuned)")
@@ -784,6 +785,8 @@ def run_ours(args, rank, world, local):
 def run_reference(args, rank, world):
     if rank != 0:
         return None
+    if args.workload == "afmulator":
+        return {"impl": "reference", "unavailable": "the reference's AFMulator runs on OpenCL, which has no runtime here; the afmulator line's cpu_baseline times the C restatement of its kernels instead"}
     from oracle import cpu_baseline
 
     if args.workload == "molecule_batch":
@@ -849,6 +852,145 @@ def run_reference(args, rank, world):
     }
 
 
+def run_afmulator(args, rank, world, local):
+    """The AFMulator's point-charge route the way the ML generators drive it: for each molecule
+    of a seeded set (the first args.nmol // 4 molecules of the batch workload), the scan window
+    follows the molecule, its force field (LJ + four tip charges) is made on a grid around the
+    window and the tilted-stroke relaxation + z convolution writes its image into one device
+    buffer; the images go to the host once per step (GeneratorAFMtrainer, sim_type LJ+PC).
+    A step is one batch.  The inputs are host molecules by design (the generator packs every
+    molecule's atoms), so the step is end to end; value and e2e are that one measurement.  The
+    two kernels' durations come from a second pass that brackets each image's launches with
+    CUDA events."""
+    import torch
+
+    from ppafm_gb300 import _lib, workloads
+    from ppafm_gb300.AFMulator import AFMulator
+    from ppafm_gb300.ml.Generator import GeneratorAFMtrainer
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    nmol = max(1, args.nmol // 4)
+    mols = workloads.molecule_batch(seed=args.seed + rank, nmol=nmol, scale=args.scale)
+    samples = [{"xyzs": np.asarray(m["Rs"], np.float64), "Zs": np.asarray(m["Zs"]), "qs": np.asarray(m["Qs"], np.float64)} for m in mols]
+    kw = dict(pixPerAngstrome=10, scan_dim=(128, 128, 30), scan_window=((0.0, 0.0, 7.0), (16.0, 16.0, 10.0)), df_steps=10)
+    afm = AFMulator(**kw)
+    seen = []
+    record = [False]
+
+    class Trainer(GeneratorAFMtrainer):
+        def on_afm_start(self):
+            if record[0]:
+                d = self.sample_dict
+                seen.append((self.scan_window, d["xyzs"], d["Zs"], d["qs"], d["REAs"]))
+
+    tr = Trainer(afm, [], samples, sim_type="LJ+PC", batch_size=nmol, iZPPs=[8], Qs=[[-10, 20, -10, 0]], QZs=[[0.1, 0, -0.1, 0]])
+    for _ in range(args.warmup):
+        for _ in tr:
+            pass
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    clocks = ClockSampler(local)
+    clocks.start()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    a.record(st)
+    for _ in range(args.steps):
+        for _ in tr:
+            pass
+    b.record(st)
+    b.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    t_step = a.elapsed_time(b) * 1e-3 / args.steps
+    nx, ny, nz = kw["scan_dim"]
+    units = nmol * nx * ny * nz
+    # kernel pass: each image's force field and relaxation bracketed by events
+    record[0] = True
+    for _ in tr:
+        pass
+    torch.cuda.synchronize()
+    out = torch.empty((nx, ny, nz - kw["df_steps"] + 1), dtype=torch.float32, device="cuda")
+
+    def images(timing=None):
+        for sw, xyzs, Zs, qs, REAs in seen:
+            afm.setScanWindow(sw, kw["scan_dim"], df_steps=kw["df_steps"])
+            afm.setLvec()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if timing is not None else None
+            if e:
+                e[0].record(st)
+            afm.prepareFF(xyzs, Zs, qs, REAs=REAs)
+            if e:
+                e[1].record(st)
+            afm.evalAFM(out=out)
+            if e:
+                e[2].record(st)
+                timing.append(e)
+
+    ev = []
+    images(ev)
+    torch.cuda.synchronize()
+    t_ff = float(np.mean([e[0].elapsed_time(e[1]) for e in ev])) * 1e-3
+    t_rx = float(np.mean([e[1].elapsed_time(e[2]) for e in ev])) * 1e-3
+    afm.counter.zero_()
+    images()
+    iters = int(afm.counter.item())
+    _lib.check(L.ppgpu_device_status(_lib.stream_handle()))
+    npts = int(np.prod(afm.nDim))
+    # the dominant kernel is the force field (ff_kernel<QZS>, FP32-FMA bound).  Work per
+    # atom-point pair in FF.cl's form (FMA = 2): LJ 26 flops, each nonzero tip charge 20
+    # (offset 1, r^2 5, R2SAFE 1, 1/r^2 1, energy 2, force factor 1, charge weight 3,
+    # accumulation 6): 86 for the three-charge tip
+    nq = int(np.count_nonzero(afm.Qs))
+    flops = float(np.mean([npts * len(z) for _, _, z, _, _ in seen])) * (FLOPS_LJ_PAIR + FLOPS_TIP_CHARGE_PAIR * nq)
+    peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
+    achieved = flops / t_ff / 1e12
+    roof = {"bound": "fp32", "kernel": "ff_kernel<QZS> (LJ + point-charge tip force field)", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "peak_source": "FFMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP32 figure)", "flops_per_launch": flops, "flops_per_pair": FLOPS_LJ_PAIR + FLOPS_TIP_CHARGE_PAIR * nq, "traffic": read_profile_traffic("ff_kernel", "afmulator")}
+    if rank != 0:
+        return None
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            from oracle import oracle as O
+            from ppafm_gb300 import species
+
+            FFp = np.array([(r[0], r[1], r[2]) for r in species.loadSpecies()])
+            nthreads = os.cpu_count() or 1
+            picks = seen[: max(1, min(4, len(seen)))]
+            t0c = time.perf_counter()
+            for sw, xyzs, Zs, qs, REAs in picks:
+                O.AFMulator(FFp, **{**kw, "scan_window": sw}).eval(xyzs, Zs, qs, REAs=REAs, nthreads=nthreads)
+            tc = (time.perf_counter() - t0c) / len(picks)
+            cpu = {"value": nx * ny * nz / tc, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": f"{len(picks)} of {len(seen)} molecules through the oracle's float32 C restatement of the OpenCL kernels (evalLJC_QZs_noPos, relaxStrokesTilted, convolveZ), OpenMP over grid points and pixels; the reference's own path is OpenCL, which does not run here"}
+        except Exception as exc:  # the baseline is reported, never fatal
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {exc}"}
+    return {
+        "metric": METRIC,
+        "value": units / t_step,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "afmulator", "molecules": nmol, "scan": list(kw["scan_dim"]), "force_field_grid": [int(x) for x in afm.nDim], "route": "LJ + point-charge tip (Qs -10, 20, -10 e at QZ 0.1, 0, -0.1 A)", "df_steps": kw["df_steps"], "l2": "every image has its own force field (%.0f MB) and scan window" % (npts * 16 / 1e6), "parallelism": f"replicas x{world}"},
+        "images_per_s": nmol / t_step,
+        "stage_ms": {"force_field": 1e3 * t_ff, "relax_and_df": 1e3 * t_rx},
+        "fire_iters_per_pixel_z": iters / units,
+        "e2e": {"value": units / t_step, "unit": UNIT, "h2d_bytes_per_step": int(sum(len(s["Zs"]) * 48 for s in samples)), "d2h_bytes_per_step": int(nmol * nx * ny * (nz - kw["df_steps"] + 1) * 4)},
+        "gpu_launches": 2 * nmol * args.steps,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+
+
 def extra_batch(args, rank, world, local):
     """The 256-molecule batch measured in the default run (its own line's main figures): the
     batched persistent launch, the plain per-molecule loop and the learned warm start, each
@@ -877,6 +1019,8 @@ def main():
         line = run_reference(args, rank, world)
     elif args.workload == "molecule_batch":
         line = run_batch(args, rank, world, local)
+    elif args.workload == "afmulator":
+        line = run_afmulator(args, rank, world, local)
     else:
         line = run_ours(args, rank, world, local)
         if line is not None and args.workload == "slab_molecule" and world == 1 and not args.no_extras:
