@@ -587,18 +587,18 @@ def run_ours(args, rank, world, local):
             torch.distributed.barrier()
 
     # ---------------- device-resident steps, pipelined: step k+1's force field runs while step
-    # k's relaxation finishes (two force-field grids and output sets, HighLevel.StepPipeline).
-    # A force field that fits in L2 is flushed from it before every timed step's force field
-    # (256 MB written on the force-field stream).
+    # k's relaxation finishes (force-field grids and output sets in flight,
+    # HighLevel.StepPipeline).  A force field that fits in L2 is flushed from it before every
+    # timed step's relaxation: 256 MB written on the relaxation stream once the step's force
+    # field is done, so the relaxation reads its grid from DRAM, not from the L2 lines its
+    # producer left.
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if npts * 16 < 129e6 else None
     NSLOT = 3  # grids, device output sets and pinned host slots in flight
     sp = HL.StepPipeline(pl, nbuf=NSLOT)
+    flush_l2 = (lambda: flush.zero_()) if flush is not None else None
 
     def device_step(timing=None):
-        if flush is not None:
-            with torch.cuda.stream(sp.s_ff):
-                flush.zero_()
-        return sp.step(timing=timing)
+        return sp.step(timing=timing, before_relax=flush_l2)
 
     for _ in range(args.warmup):
         device_step()
@@ -657,10 +657,7 @@ def run_ours(args, rank, world, local):
             job.e2e_h2d(slot)
             inputs_in = torch.cuda.Event()
             inputs_in.record(cs)
-        if flush is not None:
-            with torch.cuda.stream(sp.s_ff):
-                flush.zero_()
-        j, out, ff_done, rx_done = sp.step(after=inputs_in)
+        j, out, ff_done, rx_done = sp.step(after=inputs_in, before_relax=flush_l2)
         last["ff"] = ff_done
         with torch.cuda.stream(ds):
             ds.wait_event(rx_done)
@@ -743,7 +740,7 @@ def run_ours(args, rank, world, local):
             "fire": relax,
             "probe": {"klat": w["klat"], "krad": w["krad"], "r0": list(w["r0Probe"]), "Q": w["charge"]},
             "df": {"f0": w["f0Cantilever"], "k": w["kCantilever"], "A": w["Amplitude"]},
-            "l2": ("inputs larger than L2 (force field %.2f GB)" if npts * 16 >= 129e6 else "force field %.2f GB fits in L2: 256 MB written before every step's force field to flush it") % (npts * 16 / 1e9),
+            "l2": ("inputs larger than L2 (force field %.2f GB)" if npts * 16 >= 129e6 else "force field %.2f GB fits in L2: 256 MB written before every step's relaxation (after its force field) to flush it") % (npts * 16 / 1e9),
             "relax_lanes_per_stroke": args.relax_tps or 1,
             "steps": "pipelined: step k+1's force field runs while step k's relaxation finishes (three force-field grids and output sets in flight, relaxations on a higher-priority stream); stage_ms are each kernel's own event-timed duration on its stream",
             "parallelism": f"replicas x{world}",
@@ -962,7 +959,9 @@ def run_afmulator(args, rank, world, local):
             for sw, xyzs, Zs, qs, REAs in picks:
                 O.AFMulator(FFp, **{**kw, "scan_window": sw}).eval(xyzs, Zs, qs, REAs=REAs, nthreads=nthreads)
             tc = (time.perf_counter() - t0c) / len(picks)
-            cpu = {"value": nx * ny * nz / tc, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": f"{len(picks)} of {len(seen)} molecules through the oracle's float32 C restatement of the OpenCL kernels (evalLJC_QZs_noPos, relaxStrokesTilted, convolveZ), OpenMP over grid points and pixels; the reference's own path is OpenCL, which does not run here"}
+            from oracle.cpu_baseline import cpu_model
+
+            cpu = {"value": nx * ny * nz / tc, "unit": UNIT, "cores": nthreads, "cpu_model": cpu_model(), "kind": "port", "sample": f"{len(picks)} of {len(seen)} molecules through the oracle's float32 C restatement of the OpenCL kernels (evalLJC_QZs_noPos, relaxStrokesTilted, convolveZ), OpenMP over grid points and pixels; the reference's own path is OpenCL, which does not run here"}
         except Exception as exc:  # the baseline is reported, never fatal
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {exc}"}
     return {

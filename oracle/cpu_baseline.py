@@ -177,7 +177,7 @@ def sample_overlap(w, budget_s=20.0, nthreads=0, use_reference=True, seed=0):
         seconds_full_job=full,
         total_s=total,
         pixel_z_per_s=P * Z / total,
-        sample=f"force field: full {dims[0]}x{dims[1]}x{dims[2]} grid with numpy float64 FFTs (single-threaded like the reference's numpy); relax: {nblocks} blocks of 4x4 pixels x {Z} heights with the {'reference' if ref is not None else 'restated'} FIRE on {nthreads} threads; extrapolated per pixel-height",
+        sample=f"force field: full {dims[0]}x{dims[1]}x{dims[2]} grid with numpy float64 FFTs (single-threaded like the reference's numpy); relax: {nblocks} blocks of 8x8 pixels x {Z} heights with the {'reference' if ref is not None else 'restated'} FIRE on {nthreads} threads; extrapolated per pixel-height",
     )
 
 

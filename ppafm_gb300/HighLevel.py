@@ -398,10 +398,11 @@ class StepPipeline:
         self._out_free = [None] * nbuf  # consumer of output set j (released)
         self.k = 0
 
-    def step(self, after=None, timing=None):
+    def step(self, after=None, timing=None, before_relax=None):
         """Queues one step into slot k % nbuf; returns (slot, outputs, force-field done event,
         relaxation done event).  timing: a list that gets (ff start, ff end, relax start,
-        relax end) timing events of this step."""
+        relax end) timing events of this step.  before_relax: a callable queued on the
+        relaxation stream once the step's force field is done, before its relaxation."""
         j = self.k % self.nbuf
         sf, sr = self.s_ff, self.s_rx
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if timing is not None else None
@@ -421,6 +422,8 @@ class StepPipeline:
             sr.wait_event(ff_done)
             if self._out_free[j] is not None:
                 sr.wait_event(self._out_free[j])
+            if before_relax is not None:
+                before_relax()
             if ev:
                 ev[2].record(sr)
             out = self.pl.relax(stream=sr, ff=self.ffs[j], out=self.outs[j])
