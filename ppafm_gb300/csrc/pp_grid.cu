@@ -6,6 +6,7 @@
 //   conversions between the reference's float64 [n,3] (+[n]) grids and float4 grids.
 // All are HBM-streaming kernels: grid-stride loops over 16-byte elements, sized to a
 // multiple of the SM count.
+#include <algorithm>
 #include <cstring>
 
 #include "pp_common.cuh"
@@ -40,6 +41,59 @@ __global__ void fz2df_kernel(const float *__restrict__ F, long long ncol, int nz
             for (int i = 0; i < nw; i++) acc = fmaf(f[j + i], W.w[nw - 1 - i], acc);
             o[j] = acc * scale;
         }
+    }
+}
+
+// The same convolution with the columns staged in shared memory: a warp takes 32
+// consecutive columns, whose samples are one contiguous run of 32*nz floats (and whose outputs
+// one run of 32*nout), loads the run with coalesced float4 reads, convolves each column from
+// shared memory in the order of fz2df_kernel (bit for bit its result), and stores the outputs
+// coalesced.  Columns of at most FZ2DF_TILE_NZ samples; F and out 16-byte aligned.
+constexpr int FZ2DF_TILE_NZ = 64;
+constexpr int FZ2DF_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * FZ2DF_WARPS) fz2df_tiled_kernel(const float *__restrict__ F, long long ncol,
+                                                                       int nz, int nw, DfW W, float scale,
+                                                                       float *__restrict__ out) {
+    extern __shared__ __align__(16) float fz_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nout = nz - nw + 1;
+    float *sin = fz_smem + (size_t)warp * 32 * (nz + nout);
+    float *sout = sin + 32 * nz;
+    const long long ntile = (ncol + 31) / 32;
+    for (long long t = (long long)blockIdx.x * FZ2DF_WARPS + warp; t < ntile; t += (long long)gridDim.x * FZ2DF_WARPS) {
+        const long long c0 = t * 32;
+        const int ncl = (int)min(32LL, ncol - c0);
+        const float *src = F + c0 * nz;
+        const int nin = ncl * nz;
+        if (ncl == 32 && (nz & 3) == 0) {  // whole tile: float4 (32*nz floats from a 16-byte boundary)
+            const float4 *s4 = reinterpret_cast<const float4 *>(src);
+            float4 *d4 = reinterpret_cast<float4 *>(sin);
+            for (int i = lane; i < nin / 4; i += 32) d4[i] = __ldcs(s4 + i);
+        } else {
+            for (int i = lane; i < nin; i += 32) sin[i] = __ldcs(src + i);
+        }
+        __syncwarp();
+        if (lane < ncl) {
+            const float *f = sin + lane * nz;
+            float *o = sout + lane * nout;
+            for (int j = 0; j < nout; j++) {
+                float acc = 0.f;
+                for (int i = 0; i < nw; i++) acc = fmaf(f[j + i], W.w[nw - 1 - i], acc);
+                o[j] = acc * scale;
+            }
+        }
+        __syncwarp();
+        float *dst = out + c0 * nout;
+        const int nres = ncl * nout;
+        if (ncl == 32 && (nout & 3) == 0) {
+            const float4 *s4 = reinterpret_cast<const float4 *>(sout);
+            float4 *d4 = reinterpret_cast<float4 *>(dst);
+            for (int i = lane; i < nres / 4; i += 32) __stcs(d4 + i, s4[i]);
+        } else {
+            for (int i = lane; i < nres; i += 32) __stcs(dst + i, sout[i]);
+        }
+        __syncwarp();
     }
 }
 
@@ -391,6 +445,23 @@ extern "C" int ppgpu_fz2df(const float *F, long long ncol, int nz, int nw, const
     DfW w;
     memset(&w, 0, sizeof(w));
     for (int i = 0; i < nw; i++) w.w[i] = (float)W[i];
+    const bool aligned = (((uintptr_t)F | (uintptr_t)out) & 15u) == 0;
+    if (nz <= FZ2DF_TILE_NZ && aligned) {
+        const int nout = nz - nw + 1;
+        const size_t smem = (size_t)FZ2DF_WARPS * 32 * (nz + nout) * sizeof(float);
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long ntile = (ncol + 31) / 32;
+        const long long want = (ntile + FZ2DF_WARPS - 1) / FZ2DF_WARPS;
+        const unsigned nblk = (unsigned)std::max(1LL, std::min(want, (long long)sms * 8));
+        PPGPU_CUDA(cudaFuncSetAttribute(fz2df_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        FZ2DF_WARPS * 32 * 2 * FZ2DF_TILE_NZ * (int)sizeof(float)),
+                   "fz2df shared memory");
+        fz2df_tiled_kernel<<<nblk, 32 * FZ2DF_WARPS, smem, (cudaStream_t)stream>>>(F, ncol, nz, nw, w, (float)scale, out);
+        PPGPU_CHECK_LAUNCH("fz2df_tiled_kernel");
+        return set_ok();
+    }
     fz2df_kernel<<<stream_blocks(ncol), GRID_THREADS, 0, (cudaStream_t)stream>>>(F, ncol, nz, nw, w, (float)scale, out);
     PPGPU_CHECK_LAUNCH("fz2df_kernel");
     return set_ok();

@@ -182,6 +182,34 @@ def test_fz2df_gpu_golden(gpulib, golden):
         common.Fz2df(g["Fz"][..., :5], dz=0.1, k0=1800.0, f0=30000.0, amplitude=1.0)
 
 
+@pytest.mark.parametrize("shape", [(512, 512, 40), (1000, 31), (37, 30), (300, 100)])
+def test_fz2df_device_sizes(gpulib, oracle, shape):
+    """ppgpu_fz2df on device arrays: the shared-memory kernel (columns of at most 64 samples, whole
+    and ragged 32-column tiles, nz not a multiple of 4) is bit for bit the column-per-thread
+    kernel (which a misaligned input takes), and both agree with the float64 oracle; columns of
+    more than 64 samples take the column-per-thread kernel."""
+    import torch
+
+    from ppafm_gb300 import common
+
+    rng = np.random.default_rng(7)
+    Fh = rng.standard_normal(shape).astype(np.float32)
+    F = torch.from_numpy(Fh).cuda()
+    kw = dict(dz=0.1, k0=1800.0, f0=30300.0, amplitude=1.0)
+    got = common.Fz2df(F, **kw)
+    n = Fh.size
+    buf = torch.empty(n + 1, dtype=torch.float32, device="cuda")
+    mis = buf[1:].view(shape)  # 4 bytes past a 16-byte boundary
+    mis.copy_(F)
+    assert mis.data_ptr() % 16 != 0
+    ref_kernel = common.Fz2df(mis, **kw)
+    assert torch.equal(got, ref_kernel)
+    want = oracle.Fz2df(Fh.astype(np.float64), **kw)
+    W = common.get_df_weight(1.0, dz=0.1) * 16.0217656 * 30300.0 / 1800.0
+    bound = 1e-6 * np.abs(W).sum() * np.abs(Fh).max()  # float32 rounding of an nw-term sum
+    assert np.abs(got.cpu().numpy() - want).max() <= bound
+
+
 @pytest.mark.parametrize("tps", [2, 4, 8])
 def test_lanes_per_stroke_bit_identical(gpulib, oracle, golden, tps):
     """Splitting each stroke's gathers over 2, 4 or 8 lanes gives the one-lane results bit for
