@@ -144,6 +144,7 @@ __device__ __forceinline__ FFParams ff_params_of(const BatchJob &J, const BatchP
     p.Q = B.Q;
     p.Fmax = B.Fmax;
     p.nq = 0;
+    p.nqa = 0;
     p.Qsum = 0.f;
     p.accumulate = 0;
     p.nchunks = J.nchunks;
@@ -321,10 +322,10 @@ __device__ void relax_phase(const BatchPrm &B) {
     add_iterations(B.iter_total, mine);
 }
 
-__global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const BatchPrm B) {
-    __shared__ __align__(128) FFShared sh;
+// Phase 1: force-field items from the global counter until none is left; each finished block
+// is published to its system's strokes (release).
+__device__ __forceinline__ void ff_phase(const BatchPrm &B, FFShared &sh) {
     __shared__ long long s_item;
-    ff_shared_init(sh);
     uint32_t T = 0;
     while (true) {
         if (threadIdx.x == 0) s_item = atomicAdd(&B.ctr->ff_next, 1);
@@ -341,7 +342,21 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const BatchPrm 
         if (threadIdx.x == 0) red_release_add(&B.ff_done[j], 1);
         if (!ok) break;
     }
+}
+
+__global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const BatchPrm B) {
+    __shared__ __align__(128) FFShared sh;
+    ff_shared_init(sh);
+    ff_phase(B, sh);
     relax_phase(B);
+}
+
+// The force fields alone (the height-synchronous mode computes them before its heights): the
+// same phase 1 without the relaxation's code, so its register budget is the force field's own.
+__global__ void __maxnreg__(112) batch_ff_kernel(const BatchPrm B) {
+    __shared__ __align__(128) FFShared sh;
+    ff_shared_init(sh);
+    ff_phase(B, sh);
 }
 
 // ------------------------------------------------------------ height-synchronous mode
@@ -1182,11 +1197,9 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     }
     PPGPU_CUDA(cudaMemsetAsync(H->ctr_base, 0, H->ctr_bytes, st), "batch counters");
     PPGPU_CUDA(cudaMemsetAsync(H->pools, 0, b_ctr, st), "batch layer counters");
-    // force fields only (an empty stroke pool ends the relaxation phase at once)
-    BatchPrm Bff = H->prm;
-    Bff.nstrokes = 0;
-    batch_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(Bff);
-    PPGPU_CHECK_LAUNCH("batch_kernel (force fields)");
+    // force fields only
+    batch_ff_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm);
+    PPGPU_CHECK_LAUNCH("batch_ff_kernel");
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->dev);
     if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM), "infer smem");

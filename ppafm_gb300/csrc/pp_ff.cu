@@ -107,10 +107,10 @@ __global__ void __launch_bounds__(FF_THREADS) ff_f64_kernel(const FFParams prm) 
             }
             if (MODE == M_LJC && charged) Ge += coul64(dx, dy, dz, kqqa, G[0], G[1], G[2]);
             if (MODE == M_QZS && charged) {
-                for (int k = 0; k < prm.nq; k++) {
-                    const double dq = dz + (double)prm.QZs[k];
+                for (int k = 0; k < prm.nqa; k++) {
+                    const double dq = dz + (double)prm.QZa[k];
                     const double ir2 = 1.0 / (((dx * dx + dy * dy) + dq * dq) + prm.eps64);
-                    const double eq = kqqa * sqrt(ir2) * (double)prm.Qs[k];
+                    const double eq = kqqa * sqrt(ir2) * (double)prm.Qa[k];
                     const double fq = eq * ir2;
                     F[0] += dx * fq;
                     F[1] += dy * fq;
@@ -339,17 +339,25 @@ extern "C" int ppgpu_ff_subgrid(float *FE, const int *n, const double *cell, con
     prm.Q = (float)Q;
     prm.Fmax = (float)Fmax;
     prm.nq = 0;
+    prm.nqa = 0;
     prm.Qsum = 0.f;
     if (mode == PPGPU_FF_QZS) {
-        // Coulomb constant of FF.cl:2, folded into the tip charges; zero charges dropped.
+        // Coulomb constant of FF.cl:2, folded into the tip charges; zero charges dropped.  The
+        // kernel sums Qsum C(dz) + sum_k Q_k [C(dz + QZ_k) - C(dz)]: a charge at QZ = 0 only
+        // enters Qsum (its difference term is exactly zero, so it is not listed).
         for (int q = 0; q < 4; q++) {
             if (Qs[q] != 0.0) {
                 const float qz = (float)QZs[q];
-                prm.Qs[prm.nq] = (float)Qs[q] * 14.399644f;
+                const float qk = (float)Qs[q] * 14.399644f;
+                prm.Qsum += qk;
+                prm.Qa[prm.nqa] = qk;
+                prm.QZa[prm.nqa] = qz;
+                prm.nqa++;
+                if (qz == 0.f) continue;
+                prm.Qs[prm.nq] = qk;
                 prm.QZs[prm.nq] = qz;
                 prm.QZn2[prm.nq] = -2.f * qz;
                 prm.QZnsq[prm.nq] = -qz * qz;
-                prm.Qsum += prm.Qs[prm.nq];
                 prm.nq++;
             }
         }

@@ -29,10 +29,13 @@ struct FFParams {
     float eps;
     double eps64;
     float Q, Fmax;
-    float Qs[4], QZs[4];  // tip charges (times k_e) and their z offsets, zero charges dropped
+    float Qs[4], QZs[4];  // tip charges (times k_e) and their z offsets: the charges off the
+                          // central point (QZ != 0), whose differences the fast kernel sums
     float QZn2[4], QZnsq[4];  // -2 QZ and -QZ^2
-    float Qsum;
+    float Qsum;               // all tip charges (times k_e)
     int nq;
+    float Qa[4], QZa[4];  // every nonzero tip charge and offset (the plain sums: float64, slow path)
+    int nqa;
     int accumulate;
     long long nchunks;
     int nzc;
@@ -347,11 +350,11 @@ __device__ float4 point_slow(const FFParams &prm, double px, double py, double p
             a[3] += eq;
         }
         if (MODE == M_QZS && charged) {
-            for (int k = 0; k < prm.nq; k++) {
-                const float dq = dz + prm.QZs[k];
+            for (int k = 0; k < prm.nqa; k++) {
+                const float dq = dz + prm.QZa[k];
                 const float rq = fmaxf(fmaf(dq, dq, dxy2), R2CAP);
                 const float ir = rsqrtf(rq);
-                const float eq = r2r.z * ir * prm.Qs[k], fq = eq * ir * ir;
+                const float eq = r2r.z * ir * prm.Qa[k], fq = eq * ir * ir;
                 t[0] = fmaf(fq, dx, t[0]);
                 t[1] = fmaf(fq, dy, t[1]);
                 t[2] = fmaf(fq, dq, t[2]);
