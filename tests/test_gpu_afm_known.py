@@ -197,3 +197,90 @@ def test_qzs_single_atom_against_energy_gradient(gpulib):
     assert err[ok].max() < 5e-5, err[ok].max()
     Eerr = np.abs(g[..., 3] - U(P)) / np.maximum(np.abs(U(P)), 1e-2)
     assert Eerr[ok].max() < 1e-4, Eerr[ok].max()
+
+
+@pytest.mark.parametrize("tip", ["s", "pz"])
+def test_hartree_tip_density_plane_waves(gpulib, tip):
+    """The Hartree route with a tip density, no atoms: the potential V = cos(Gx x + Gz z) +
+    0.5 sin(Gy y) on the force-field grid cross-correlated with a Gaussian tip density of width
+    s (calc_force_hartree, field.py:1446-1504).  An s density of charge c multiplies each wave
+    by c exp(-s^2 |G|^2 / 2); a pz density c (z / s) g(r) turns cos(G.r) into
+    -c s Gz exp(-s^2 |G|^2 / 2) sin(G.r) (the sign fixes correlation against convolution).
+    F = -grad E by periodic centred differences: a wave A cos(phase) gives A sin(phase)
+    sin(G_k h) / h along axis k."""
+    from ppafm_gb300.AFMulator import AFMulator, HartreePotential
+
+    n = (16, 16, 20)
+    lv = np.array([[0.0, 0, 0], [8.0, 0, 0], [0, 8.0, 0], [0, 0, 10.0]])
+    h, s = 0.5, 0.7
+    x, y, z = [np.arange(k) * h for k in n]
+    Gx, Gy, Gz = 2 * np.pi / 8, 2 * 2 * np.pi / 8, 2 * 2 * np.pi / 10
+    ph = Gx * x[:, None, None] + Gz * z[None, None, :] + 0 * y[None, :, None]
+    wy = y[None, :, None] + 0 * ph
+    V = (np.cos(ph) + 0.5 * np.sin(Gy * wy)).astype(np.float32)
+    c = -0.3 if tip == "s" else 0.2
+    afm = AFMulator(pixPerAngstrome=2, lvec=lv, rho={tip: c}, sigma=s, npbc=(0, 0, 0))
+    assert tuple(afm.nDim) == n
+    afm.prepareFF(np.zeros((0, 3)), np.zeros(0, dtype=np.int32), HartreePotential(V, lv), rot_center=np.zeros(3), REAs=np.zeros((0, 4)))
+    FE = afm.downloadFF().astype(np.float64)
+    A = np.exp(-(s * s) * (Gx**2 + Gz**2) / 2)
+    B = 0.5 * np.exp(-(s * s) * Gy**2 / 2)
+    if tip == "s":
+        E = c * (A * np.cos(ph) + B * np.sin(Gy * wy))
+        F = [c * A * np.sin(ph) * np.sin(Gx * h) / h, -c * B * np.cos(Gy * wy) * np.sin(Gy * h) / h, c * A * np.sin(ph) * np.sin(Gz * h) / h]
+    else:  # only the wave with a z component survives an odd-in-z density
+        a = -c * s * Gz * A
+        E = a * np.sin(ph)
+        F = [-a * np.cos(ph) * np.sin(Gx * h) / h, 0 * ph, -a * np.cos(ph) * np.sin(Gz * h) / h]
+    for k, ref in enumerate(F + [E]):
+        assert np.abs(FE[..., k] - ref).max() < 5e-6, (k, np.abs(FE[..., k] - ref).max())
+
+
+def test_hartree_point_charge_tip_known_answers(gpulib):
+    """The Hartree route with the point-charge tip, no atoms (field.py:1168-1317): the
+    potential's field sampled at the tip charges Qs placed QZs above each force-field node.
+    Potential on the force-field grid itself: periodic centred differences of a plane wave.
+    Potential on a larger grid of its own: a linear potential, whose field the differences at
+    +-0.05 A of the interpolated potential give exactly; the energy samples V at the charges,
+    periodic over the force-field cell."""
+    from ppafm_gb300.AFMulator import AFMulator, HartreePotential
+
+    n = (16, 12, 20)
+    lv = np.array([[0.0, 0, 0], [8.0, 0, 0], [0, 6.0, 0], [0, 0, 10.0]])
+    h = 0.5
+    kx, kz = 2 * np.pi / 8.0, 2 * 2 * np.pi / 10.0
+    x, y, z = [np.arange(k) * h for k in n]
+    one = np.ones(n)
+    V = (np.sin(kx * x)[:, None, None] + 0.5 * np.cos(kz * z)[None, None, :]) * one
+    Qs, QZs = [1.0, -2.0, 0.0, 0.0], [0.0, 1.0, 0.0, 0.0]
+    none = (np.zeros((0, 3)), np.zeros(0, dtype=np.int32))
+    kw = dict(rot_center=np.zeros(3), REAs=np.zeros((0, 4)))
+    afm = AFMulator(pixPerAngstrome=2, lvec=lv, Qs=Qs, QZs=QZs, npbc=(0, 0, 0))
+    assert tuple(afm.nDim) == n
+    afm.prepareFF(*none, HartreePotential(V.astype(np.float32), lv), **kw)
+    FE = afm.downloadFF().astype(np.float64)
+
+    def field(zs):  # (Ex, Ez, V) of the wave at heights zs by centred differences
+        ex = -np.cos(kx * x)[:, None, None] * np.sin(kx * h) / h * one
+        ez = 0.5 * np.sin(kz * zs)[None, None, :] * np.sin(kz * h) / h * one
+        return ex, ez, (np.sin(kx * x)[:, None, None] + 0.5 * np.cos(kz * zs)[None, None, :]) * one
+
+    e0, e1 = field(z), field(z + 1.0)  # QZ = 1 A is two steps, periodic in the cell
+    assert np.abs(FE[..., 0] - (e0[0] - 2 * e1[0])).max() < 1e-5
+    assert np.abs(FE[..., 1]).max() < 1e-5
+    assert np.abs(FE[..., 2] - (e0[1] - 2 * e1[1])).max() < 1e-5
+    assert np.abs(FE[..., 3] - (e0[2] - 2 * e1[2])).max() < 1e-5
+    a, b, cz = 0.3, -0.2, 0.5
+    lvp = np.array([[-1.0, -1.0, -2.0], [12.0, 0, 0], [0, 10.0, 0], [0, 0, 16.0]])
+    npot = (24, 20, 32)
+    gp = [lvp[0][k] + np.arange(npot[k]) * 0.5 for k in range(3)]
+    Vp = (a * gp[0][:, None, None] + b * gp[1][None, :, None] + cz * gp[2][None, None, :]).astype(np.float32)
+    afm.prepareFF(*none, HartreePotential(Vp, lvp), **kw)
+    FE = afm.downloadFF().astype(np.float64)
+    for k, f in enumerate((a, b, cz)):  # F = sum_k Q_k (-grad V) = (1 - 2)(-a, -b, -c)
+        assert np.abs(FE[..., k] - f).max() < 2e-3, (k, np.abs(FE[..., k] - f).max())
+
+    def Vff(zs):
+        return a * x[:, None, None] + b * y[None, :, None] + cz * zs[None, None, :]
+
+    assert np.abs(FE[..., 3] - (Vff(z) - 2 * Vff((z + 1.0) % 10.0))).max() < 1e-4

@@ -353,3 +353,19 @@ def test_interp_tip_at_gaussian(oracle):
     x = np.arange(72)
     x = np.where(x > 36, x - 72, x) * (12 / 72)
     assert (out[np.abs(x) > 5.0 + 1e-6] == 0).all()
+
+
+def test_hartree_pz_tip_density_sign(oracle):
+    """An odd tip density fixes correlation against convolution: V = cos(G z) with a pz
+    density c (z / s) g(r) gives E = -c s G exp(-s^2 G^2 / 2) sin(G z) (a convolution would give
+    the opposite sign)."""
+    n = (8, 8, 20)
+    lv = np.array([[0.0, 0, 0], [4.0, 0, 0], [0, 4.0, 0], [0, 0, 10.0]])
+    h, s, c = 0.5, 0.7, 0.2
+    z = np.arange(n[2]) * h
+    G = 2 * 2 * np.pi / 10.0
+    pot = np.broadcast_to(np.cos(G * z)[None, None, :], n).astype(np.float32)
+    FE = oracle.hartree_ff(n, lv, pot, lv, {"pz": c}, s, np.zeros((0, 3)), np.zeros((0, 2)), np.eye(3), np.zeros(3)).transpose(2, 1, 0, 3)
+    a = -c * s * G * np.exp(-(s * G) ** 2 / 2)
+    assert np.allclose(FE[2, 3, :, 3], a * np.sin(G * z), atol=1e-6)
+    assert np.allclose(FE[2, 3, :, 2], -a * np.cos(G * z) * np.sin(G * h) / h, atol=1e-6)
