@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--relax-tps", type=int, default=0, help="lanes per stroke of the single-system relaxation (1, 2, 4, 8; 0 = library default)")
-    ap.add_argument("--no-extras", action="store_true", help="default workload: skip the 256-molecule batch (batched, per-molecule loop, learned warm start) added to the line")
+    ap.add_argument("--no-extras", action="store_true", help="default workload: skip the other workloads added to the line (the 256-molecule batch with its per-molecule loop and learned warm start, the small molecule, the density-overlap route, the AFMulator)")
     return ap.parse_args()
 
 
@@ -1011,6 +1011,31 @@ def extra_batch(args, rank, world, local):
     return out
 
 
+# Timed steps of the single-system extras: enough for the timed region to span many clock samples
+# (a step of these workloads takes 2-4 ms; an AFMulator step is one batch of 64 images).
+EXTRA_STEPS = {"small_molecule": 400, "density_overlap": 300, "afmulator": 5}
+
+
+def extra_single(args, rank, world, local, workload):
+    """A single-system workload measured in the default run with its own CUDA-event timing,
+    clock samples, roofline and a shorter CPU-baseline sample: the small molecule (config 0),
+    the density-overlap FFT route (config 3) and the AFMulator."""
+    import copy
+
+    a = copy.copy(args)
+    a.workload = workload
+    a.steps = EXTRA_STEPS[workload]
+    a.warmup = 3
+    a.cpu_budget = args.cpu_budget / 4
+    line = (run_afmulator if workload == "afmulator" else run_ours)(a, rank, world, local)
+    if line is None:
+        return None
+    keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "e2e", "stage_ms", "images_per_s", "fire_iters_per_pixel_z", "clocks", "cpu_baseline", "gpu_launches", "config")
+    out = {k: line[k] for k in keep if k in line}
+    out["roofline"] = {k: line["roofline"][k] for k in ("kernel", "bound", "achieved", "peak", "unit", "frac", "traffic") if k in line["roofline"]}
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -1023,7 +1048,10 @@ def main():
     else:
         line = run_ours(args, rank, world, local)
         if line is not None and args.workload == "slab_molecule" and world == 1 and not args.no_extras:
-            line["extra_workloads"] = {"molecule_batch": extra_batch(args, rank, world, local)}
+            extras = {"molecule_batch": extra_batch(args, rank, world, local)}
+            for wl in ("small_molecule", "density_overlap", "afmulator"):
+                extras[wl] = extra_single(args, rank, world, local, wl)
+            line["extra_workloads"] = extras
     if line is not None:
         print(json.dumps(line), flush=True)
 
