@@ -348,7 +348,7 @@ class BatchBench:
         """The current stream waits for the output copies still in flight."""
         self.torch.cuda.current_stream().wait_stream(self.d2h_stream)
 
-    def learned(self, args, plain_loop_ms, steps=120000, lr=1e-3):
+    def learned(self, args, plain_loop_ms, steps=480000, lr=1e-3):
         """Config-4 line: train the warm-start network on plain-FIRE pairs of a held-out batch
         (every 4th stroke of 256 other molecules: ~21M pairs; Adam, batch 8192, cosine-decayed
         learning rate, z error weighted 10x), then

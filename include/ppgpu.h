@@ -167,8 +167,7 @@ int ppgpu_set_tip_spline(int n, const double *xs, const double *ydys);
  * 0 restores the default, 1.  ppgpu_get_relax_tps returns the value used for nstroke strokes. */
 int ppgpu_set_relax_tps(int tps);
 /* No counterpart in the reference (a launch-shape knob).  Threads per CTA of the single-grid
- * force-field kernel: 128 or 256, 0 = by atom count (256 up to 4096 atoms, where the per-CTA
- * set-up weighs more; 128 above). */
+ * force-field kernel: 128 or 256, 0 = the default (128). */
 int ppgpu_set_ff_block(int threads);
 int ppgpu_get_relax_tps(long long nstroke, int *out);
 

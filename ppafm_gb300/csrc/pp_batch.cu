@@ -322,24 +322,31 @@ __device__ void relax_phase(const BatchPrm &B) {
     add_iterations(B.iter_total, mine);
 }
 
-// Phase 1: force-field items from the global counter until none is left; each finished block
-// is published to its system's strokes (release).
+// Phase 1: force-field items from the global counter until none is left.  An item is
+// BATCH_THREADS chunks of a system's grid; a CTA of NT threads takes it in BATCH_THREADS / NT
+// parts.  PUBLISH: each finished item is published to its system's strokes (release).
+template <int NT, bool PUBLISH>
 __device__ __forceinline__ void ff_phase(const BatchPrm &B, FFShared &sh) {
-    __shared__ long long s_item;
+    constexpr int PARTS = BATCH_THREADS / NT;
+    static_assert(PARTS * NT == BATCH_THREADS && (PUBLISH ? PARTS == 1 : true), "whole items when published");
+    __shared__ long long s_part;
     uint32_t T = 0;
     while (true) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&B.ctr->ff_next, 1);
+        if (threadIdx.x == 0) s_part = atomicAdd(&B.ctr->ff_next, 1);
         __syncthreads();
-        const long long item = s_item;
+        const long long part = s_part;
         __syncthreads();
-        if (item >= B.nff_items) break;
+        if (part >= B.nff_items * PARTS) break;
+        const long long item = part / PARTS;
         const int j = find_job_ff(B, item);
         const BatchJob &J = B.jobs[j];
         const FFParams prm = ff_params_of(J, B);
-        const bool ok = ff_block<M_LJC, false, true, 4, true>(prm, item - J.ff_block0, sh, T);
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) red_release_add(&B.ff_done[j], 1);
+        const bool ok = ff_block<M_LJC, false, true, 4, true, NT>(prm, (item - J.ff_block0) * PARTS + part % PARTS, sh, T);
+        if constexpr (PUBLISH) {
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) red_release_add(&B.ff_done[j], 1);
+        }
         if (!ok) break;
     }
 }
@@ -347,16 +354,20 @@ __device__ __forceinline__ void ff_phase(const BatchPrm &B, FFShared &sh) {
 __global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const BatchPrm B) {
     __shared__ __align__(128) FFShared sh;
     ff_shared_init(sh);
-    ff_phase(B, sh);
+    ff_phase<BATCH_THREADS, true>(B, sh);
     relax_phase(B);
 }
 
-// The force fields alone (the height-synchronous mode computes them before its heights): the
-// same phase 1 without the relaxation's code, so its register budget is the force field's own.
-__global__ void __maxnreg__(112) batch_ff_kernel(const BatchPrm B) {
+// The force fields alone (the height-synchronous mode computes them before its heights, so
+// nothing waits on a published item): the same phase 1 without the relaxation's code, in CTAs
+// of BATCH_FF_THREADS threads, BATCH_FF_CTAS_PER_SM of them per SM at up to 128 registers
+// (more warps per SM than the 256-thread CTAs that share their registers with the relaxation).
+constexpr int BATCH_FF_THREADS = 128;
+constexpr int BATCH_FF_CTAS_PER_SM = 4;
+__global__ void __launch_bounds__(BATCH_FF_THREADS, BATCH_FF_CTAS_PER_SM) batch_ff_kernel(const BatchPrm B) {
     __shared__ __align__(128) FFShared sh;
     ff_shared_init(sh);
-    ff_phase(B, sh);
+    ff_phase<BATCH_FF_THREADS, false>(B, sh);
 }
 
 // ------------------------------------------------------------ height-synchronous mode
@@ -1198,10 +1209,10 @@ extern "C" int ppgpu_batch_run_layered(void *handle, void *mlp, int rec_stride, 
     PPGPU_CUDA(cudaMemsetAsync(H->ctr_base, 0, H->ctr_bytes, st), "batch counters");
     PPGPU_CUDA(cudaMemsetAsync(H->pools, 0, b_ctr, st), "batch layer counters");
     // force fields only
-    batch_ff_kernel<<<H->ctas, BATCH_THREADS, 0, st>>>(H->prm);
-    PPGPU_CHECK_LAUNCH("batch_ff_kernel");
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->dev);
+    batch_ff_kernel<<<sms * BATCH_FF_CTAS_PER_SM, BATCH_FF_THREADS, 0, st>>>(H->prm);
+    PPGPU_CHECK_LAUNCH("batch_ff_kernel");
     if (mlp) PPGPU_CUDA(cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM), "infer smem");
     const bool propose = mlp || rec_stride > 0;
     for (int iz = 0; iz < nz; iz++) {
