@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--workload", default="slab_molecule", choices=["slab_molecule", "small_molecule", "density_overlap", "molecule_batch", "afmulator"])
     ap.add_argument("--nmol", type=int, default=256)
     ap.add_argument("--no-learned", action="store_true", help="molecule_batch: skip the learned warm start")
+    ap.add_argument("--train-steps", type=int, default=480000, help="molecule_batch: Adam steps of the warm-start network (outside the timed region)")
     ap.add_argument("--tuning", default=None, help="molecule_batch launch shape 'ctas_per_sm,tile_w,tile_h,chunk' (default: autotuned)")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -504,7 +505,7 @@ def run_batch(args, rank, world, local):
     plain = job.plain_ms()
     learned = None
     if not args.no_learned:
-        learned = job.learned(args, plain)
+        learned = job.learned(args, plain, steps=args.train_steps)
     peak = ffma_peak_tflops(torch, L, _lib.check, _lib.tptr, _lib.stream_handle)
     flops = job.pairs * FLOPS_LJC_PAIR
     line = {
