@@ -196,12 +196,26 @@ def _relax_and_collect(ff, prm, lvec, xTips, yTips, zTips, lvecScan, tilted, bPP
 # ----------------------------------------------------------------- atom input
 
 
+_SPECIES = None
+
+
+def _default_species():
+    """The built-in species table and its symbol index, made once (read only here)."""
+    global _SPECIES
+    if _SPECIES is None:
+        table = PPU.loadSpecies()
+        _SPECIES = (table, PPU.getFFdict(table))
+    return _SPECIES
+
+
 def prepare_atoms(Zs, Rs, Qs, lvec, parameters, FFparams=None):
     """parseAtoms + getAtomsLJ + origin shift (common.py:828-868, HighLevel.py:269-277):
     returns (Rs0 relative to the grid origin, cLJs, kQQs) after in-plane PBC replication."""
     lvec = np.asarray(lvec, dtype=np.float64)
-    FFparams = PPU.loadSpecies() if FFparams is None else FFparams
-    elem_dict = PPU.getFFdict(FFparams)
+    if FFparams is None:
+        FFparams, elem_dict = _default_species()
+    else:
+        elem_dict = PPU.getFFdict(FFparams)
     iZs = np.asarray(Zs, dtype=np.int32)
     Rs = np.asarray(Rs, dtype=np.float64)
     Qs = np.asarray(Qs, dtype=np.float64)

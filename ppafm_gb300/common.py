@@ -313,10 +313,15 @@ def PBCAtoms(Zs, Rs, Qs, avec, bvec, na=None, nb=None, parameters=None):
         na = parameters.nPBC[0] if parameters is not None else 1
     if nb is None:
         nb = parameters.nPBC[1] if parameters is not None else 1
-    Rs = np.asarray(Rs, dtype=np.float64)
-    shifts = [(i, j) for i in range(-na, na + 1) for j in range(-nb, nb + 1)]
-    Rs_ = np.concatenate([np.column_stack([Rs[:, 0] + i * avec[0] + j * bvec[0], Rs[:, 1] + i * avec[1] + j * bvec[1], Rs[:, 2]]) for i, j in shifts])
-    return np.tile(np.asarray(Zs), len(shifts)), Rs_, np.tile(np.asarray(Qs, dtype=np.float64), len(shifts))
+    Rs = np.asarray(Rs, dtype=np.float64).reshape(-1, 3)
+    i, j = np.meshgrid(np.arange(-na, na + 1), np.arange(-nb, nb + 1), indexing="ij")
+    i, j = i.reshape(-1, 1).astype(np.float64), j.reshape(-1, 1).astype(np.float64)
+    nimg = i.shape[0]
+    Rs_ = np.empty((nimg, Rs.shape[0], 3))
+    for k in range(2):  # x + i a_k + j b_k, added in that order for every image
+        Rs_[..., k] = (Rs[None, :, k] + i * avec[k]) + j * bvec[k]
+    Rs_[..., 2] = Rs[None, :, 2]
+    return np.tile(np.asarray(Zs), nimg), Rs_.reshape(-1, 3), np.tile(np.asarray(Qs, dtype=np.float64), nimg)
 
 
 def parseAtoms(atoms, elem_dict, PBC=True, autogeom=False, lvec=None, parameters=None):
