@@ -263,6 +263,63 @@ def test_lanes_per_stroke_bit_identical(gpulib, oracle, golden, tps):
         _lib.check(L.ppgpu_set_relax_tps(3))
 
 
+@pytest.mark.parametrize("cell", ["orthogonal", "skewed"])
+@pytest.mark.parametrize("tip", ["straight", "offset"])
+def test_lanes_per_stroke_bit_identical_cells_and_tips(gpulib, oracle, golden, cell, tip):
+    """One lane per stroke against two lanes per stroke on an axis-aligned and a skewed cell
+    (general grid coordinates), with a straight tip (rPP0 = 0, no z lateral spring) and an
+    offset tip (rPP0 and a z lateral spring nonzero): identical bits for the scan and the stroke
+    entry points."""
+    import torch
+
+    from ppafm_gb300 import HighLevel as HL
+    from ppafm_gb300 import _lib, core, device
+
+    g, FF, prm, xT, yT, zT = _relax_fixture(oracle, golden)
+    lv = np.array(g["lvec"], dtype=np.float64)
+    if cell == "skewed":
+        lv[2] = [1.5, 9.8, 0.0]
+        lv[3] = [0.7, -0.4, 10.0]
+    prm = np.array(prm, dtype=np.float64)
+    rPP0, kS = np.zeros(3), np.array([0.25, 0.25, 0.0]) / -16.0217662
+    if tip == "offset":
+        rPP0 = np.array([0.12, -0.07, 0.05])
+        kS = np.array([0.25, 0.2, 0.3]) / -16.0217662
+        prm[9:12] = rPP0
+        prm[12:15] = kS
+    ff = device.DeviceFF(g["n"], lv).from_host_f64(FF.reshape(-1, 3))
+
+    def run():
+        out = device.relax_scan(ff, prm, xT - lv[0, 0], yT - lv[0, 1], zT[::-1] - lv[0, 2], pos_offset=lv[0], want_iters=True)
+        torch.cuda.synchronize()
+        return {k: v.clone() for k, v in out.items()}
+
+    HL.setFF(np.ascontiguousarray(FF), lvec=lv)
+    core.setRelax(300, 1e-8, 0.5, 0.1)
+    core.setFIRE(1.1, 0.5, 0.99)
+    core.setTip(lRadial=4.0, kRadial=20.0 / -16.0217662, rPP0=rPP0, kSpring=kS)
+    rT = oracle.scan_tips(xT[::3], yT[::3], zT, lv[0])
+
+    def strokes():
+        rs, fs = np.zeros_like(rT), np.zeros_like(rT)
+        core.relaxTipStrokes_omp(rT, rs, fs, probeStart=1, relaxAlg=1)
+        return rs, fs
+
+    L = _lib.lib()
+    try:
+        _lib.check(L.ppgpu_set_relax_tps(1))
+        ref, ref_s = run(), strokes()
+        _lib.check(L.ppgpu_set_relax_tps(2))
+        got, got_s = run(), strokes()
+    finally:
+        _lib.check(L.ppgpu_set_relax_tps(0))
+        core.deleteFF_Fpointer()
+    assert ref["iters"].float().mean() > 1.0
+    for k in ref:
+        assert ref[k].equal(got[k]), k
+    assert np.array_equal(ref_s[0], got_s[0]) and np.array_equal(ref_s[1], got_s[1])
+
+
 @pytest.mark.parametrize("fmt", ["xsf", "npy"])
 def test_outfz_file_handoff(gpulib, golden, tmp_path, fmt):
     """Relaxed-scan Fz through the OutFz file and back to Δf (the CLI stages' hand-off):
