@@ -341,7 +341,9 @@ __device__ __forceinline__ void ff_phase(const BatchPrm &B, FFShared &sh) {
         const int j = find_job_ff(B, item);
         const BatchJob &J = B.jobs[j];
         const FFParams prm = ff_params_of(J, B);
-        const bool ok = ff_block<M_LJC, false, true, 4, true, NT>(prm, (item - J.ff_block0) * PARTS + part % PARTS, sh, T);
+        const long long blk = (item - J.ff_block0) * PARTS + part % PARTS;
+        const bool ok = (J.ncharged == J.natoms) ? ff_block<M_LJC, false, true, 4, true, NT, true>(prm, blk, sh, T)
+                                                 : ff_block<M_LJC, false, true, 4, true, NT>(prm, blk, sh, T);
         if constexpr (PUBLISH) {
             __threadfence();
             __syncthreads();

@@ -36,12 +36,12 @@
 
 namespace ppgpu {
 
-template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT, int NT>
+template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT, int NT, bool ALLQ = false>
 __global__ void __launch_bounds__(NT, 512 / NT) ff_kernel(const FFParams prm) {
     __shared__ __align__(128) FFShared sh;
     ff_shared_init(sh);
     uint32_t T = 0;
-    ff_block<MODE, WITH_E, ORTHO, P2, SPLIT, NT>(prm, (long long)blockIdx.x, sh, T);
+    ff_block<MODE, WITH_E, ORTHO, P2, SPLIT, NT, ALLQ>(prm, (long long)blockIdx.x, sh, T);
 }
 
 // ------------------------------------------------------------- float64 kernel
@@ -214,6 +214,15 @@ constexpr int FF_DEFAULT_THREADS = 128;
 
 template <int MODE, bool WITH_E, int P2, bool SPLIT, int NT>
 static void launch_ff_nt(const FFParams &prm, bool ortho, long long nblk, cudaStream_t st) {
+    if constexpr (MODE == M_LJC && SPLIT) {
+        if (prm.ncharged == prm.natoms) {  // every atom charged: no neutral phase
+            if (ortho)
+                ff_kernel<MODE, WITH_E, true, P2, SPLIT, NT, true><<<(unsigned)nblk, NT, 0, st>>>(prm);
+            else
+                ff_kernel<MODE, WITH_E, false, P2, SPLIT, NT, true><<<(unsigned)nblk, NT, 0, st>>>(prm);
+            return;
+        }
+    }
     if (ortho)
         ff_kernel<MODE, WITH_E, true, P2, SPLIT, NT><<<(unsigned)nblk, NT, 0, st>>>(prm);
     else

@@ -277,10 +277,13 @@ __device__ __forceinline__ void qzs_tip(const FFParams &prm, float q, float2 r2,
     }
 }
 
-// Overflow-safe |F| <= Fmax clamp preserving direction (io.py:766-778).
+// Overflow-safe |F| <= Fmax clamp preserving direction (io.py:766-778).  A vector whose
+// largest component m is below 0.57 Fmax is left as it is without the division and root:
+// |F| <= sqrt(3) m < 0.9873 Fmax, so the full test below would not clamp it either (its
+// rounded root exceeds sqrt(3) m by a few ulps at most).
 __device__ __forceinline__ void clamp_vec(float &x, float &y, float &z, float Fmax) {
     const float m = fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z)));
-    if (!(m > 0.f)) return;
+    if (!(m > 0.f) || m < 0.57f * Fmax) return;
     const float s = 1.f / m;
     const float sx = x * s, sy = y * s, sz = z * s;
     const float fr = m * sqrtf(sx * sx + sy * sy + sz * sz);
@@ -392,8 +395,11 @@ __device__ __forceinline__ void ff_shared_init(FFShared &sh) {
     __syncthreads();
 }
 
-template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT, int NT = FF_THREADS>
+// ALLQ (SPLIT only): every atom is charged, so there is no neutral phase and the electrostatic
+// sums stay in registers instead of waiting in the output slots.
+template <int MODE, bool WITH_E, bool ORTHO, int P2, bool SPLIT, int NT = FF_THREADS, bool ALLQ = false>
 __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFShared &sh, uint32_t &T) {
+    static_assert(!ALLQ || (MODE == M_LJC && SPLIT), "ALLQ is a form of the split LJ + Coulomb block");
     constexpr int P = 2 * P2;
     auto &s_at = sh.at;
     uint64_t *s_bar = sh.bar;
@@ -532,7 +538,7 @@ __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFS
             release(t);
         }
         // park the electrostatic sums in this thread's output slots
-        if (valid) {
+        if (!ALLQ && valid) {
             const long long colbase = ((long long)la * prm.ns[1] + lb) * prm.ns[2];
 #pragma unroll
             for (int p = 0; p < P2; p++) {
@@ -547,7 +553,7 @@ __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFS
                 }
             }
         }
-        for (; t < ntiles; t++) {  // neutral atoms: two-level
+        for (; !ALLQ && t < ntiles; t++) {  // neutral atoms: two-level
             if (!acquire(t)) return false;
             const int nj = min(FF_TILE, nat - t * FF_TILE);
             run_lj(&s_at[stage(t)][0], 0, nj, acc);
@@ -609,7 +615,12 @@ __device__ __forceinline__ bool ff_block(const FFParams &prm, long long blk, FFS
             if (lz >= prm.ns[2]) continue;
             float ux = 0.f, uy = 0.f, uz = 0.f, ue = 0.f;
             if constexpr (MODE == M_LJC) {
-                if constexpr (SPLIT) {
+                if constexpr (SPLIT && ALLQ) {
+                    ux = h ? el.x[p].y : el.x[p].x;
+                    uy = h ? el.y[p].y : el.y[p].x;
+                    uz = h ? el.z[p].y : el.z[p].x;
+                    ue = h ? el.e[p].y : el.e[p].x;
+                } else if constexpr (SPLIT) {
                     const float4 v = prm.FE[colbase + lz];
                     ux = v.x;
                     uy = v.y;
