@@ -859,7 +859,8 @@ def run_afmulator(args, rank, world, local):
     A step is one batch.  The inputs are host molecules by design (the generator packs every
     molecule's atoms), so the step is end to end; value and e2e are that one measurement.  The
     two kernels' durations come from a second pass that brackets each image's launches with
-    CUDA events."""
+    CUDA events.  The generator runs the AFMulator in its overlap mode (each image's force field
+    beside the previous image's relaxation)."""
     import torch
 
     from ppafm_gb300 import _lib, workloads
@@ -904,10 +905,12 @@ def run_afmulator(args, rank, world, local):
     t_step = a.elapsed_time(b) * 1e-3 / args.steps
     nx, ny, nz = kw["scan_dim"]
     units = nmol * nx * ny * nz
-    # kernel pass: each image's force field and relaxation bracketed by events
+    # kernel pass: each image's force field and relaxation bracketed by events (in the
+    # AFMulator's plain mode: one stream, so the events bracket the two kernels)
     record[0] = True
     for _ in tr:
         pass
+    afm.set_overlap(False)
     torch.cuda.synchronize()
     out = torch.empty((nx, ny, nz - kw["df_steps"] + 1), dtype=torch.float32, device="cuda")
 

@@ -78,6 +78,7 @@ class AFMulator:
         self._rho_spectrum_of = None
         self._efield = None
         self._fft = None
+        self._streams = None  # overlap mode (set_overlap): force-field and relaxation streams
         self.setScanWindow(scan_window, scan_dim, df_steps)
         self.setLvec(lvec, pixPerAngstrome)
         self.setQs(Qs, QZs)
@@ -242,8 +243,59 @@ class AFMulator:
 
     # --------------------------------------------------------------- imaging
 
+    # ------------------------------------------------------------------ overlap mode
+
+    def set_overlap(self, on=True):
+        """Overlap mode, for callers that queue many images (the ML generators): each image's
+        force field goes to one of two device grids on a force-field stream, and its relaxation
+        runs on a stream of higher priority after it, so that image k+1's force field runs
+        beside image k's relaxation.  The results are those of the plain mode; what evalAFM
+        writes into ``out`` is ready on the current stream after ``join()`` (evalAFM without
+        ``out`` joins by itself).  Off: joins and returns to the current stream."""
+        if not on:
+            self.join()
+            self._streams = None
+            return
+        if self._streams is None:
+            _, high = torch.cuda.Stream.priority_range()
+            self._streams = (torch.cuda.Stream(), torch.cuda.Stream(priority=high))
+            self._slots = [None, None]  # the two force-field grids
+            self._ff_done = [None, None]  # force field of slot k written
+            self._rx_done = [None, None]  # relaxation that last read slot k finished
+            self._slot = 1
+
+    def join(self):
+        """The current stream waits for the force fields and relaxations queued in overlap mode."""
+        if self._streams is not None:
+            cur = torch.cuda.current_stream()
+            cur.wait_stream(self._streams[0])
+            cur.wait_stream(self._streams[1])
+
     def prepareFF(self, xyzs, Zs, qs, rho_sample=None, sample_lvec=None, rot=np.eye(3), rot_center=None, REAs=None, stream=None):
         """Point-charge force field on the device (AFMulator.py:321-429, field.py:1608-1713)."""
+        if self._streams is None or stream is not None:
+            return self._prepare_ff(xyzs, Zs, qs, rho_sample, sample_lvec, rot, rot_center, REAs, stream)
+        s_ff = self._streams[0]
+        self._slot ^= 1
+        k = self._slot
+        s_ff.wait_stream(torch.cuda.current_stream())
+        if self._rx_done[k] is not None:
+            s_ff.wait_event(self._rx_done[k])  # the relaxation that read this grid has finished
+        g = self._slots[k]
+        with torch.cuda.stream(s_ff):
+            if g is None or not np.array_equal(g.n, self.nDim) or not np.array_equal(g.cell, self.lvec[1:4]):
+                g = DeviceFF(self.nDim, self.lvec)
+                self._slots[k] = g
+            else:
+                g.lvec = self.lvec.copy()
+                g.origin = self.lvec[0].copy()
+            self._ff = g
+            out = self._prepare_ff(xyzs, Zs, qs, rho_sample, sample_lvec, rot, rot_center, REAs, s_ff)
+            self._ff_done[k] = torch.cuda.Event()
+            self._ff_done[k].record(s_ff)
+        return out
+
+    def _prepare_ff(self, xyzs, Zs, qs, rho_sample, sample_lvec, rot, rot_center, REAs, stream):
         if rho_sample is not None:
             raise NotImplementedError("FDBM (rho_sample) is not supported")
         pot = None
@@ -305,7 +357,36 @@ class AFMulator:
     def evalAFM(self, X=None, stream=None, keep_device=False, want_paths=False, want_iters=False, out=None):
         """Relaxation + z convolution of the prepared force field (AFMulator.py:447-479).
         out: a contiguous float32 device tensor [nx, ny, nz - df_steps + 1] that receives the
-        image (returned as is, nothing is copied to the host)."""
+        image (returned as is, nothing is copied to the host; in overlap mode ready on the
+        current stream after join())."""
+        if self._streams is None or stream is not None:
+            return self._eval_afm(X, stream, keep_device, want_paths, want_iters, out)
+        s_rx = self._streams[1]
+        k = self._slot
+        s_rx.wait_stream(torch.cuda.current_stream())
+        if self._ff_done[k] is not None:
+            s_rx.wait_event(self._ff_done[k])
+        with torch.cuda.stream(s_rx):
+            res = self._eval_afm(X, s_rx, True if out is None else keep_device, want_paths, want_iters, out)
+            self._rx_done[k] = torch.cuda.Event()
+            self._rx_done[k].record(s_rx)
+        if out is not None:
+            return res
+        self.join()
+        return self._host_image(res, X, keep_device)
+
+    def _host_image(self, Xd, X, keep_device):
+        if keep_device:
+            return Xd
+        Xh = Xd.cpu().numpy()
+        if X is None:
+            return Xh.copy()
+        if X.shape != Xd.shape:
+            raise ValueError(f"Expected an array of shape {tuple(Xd.shape)} for storing AFM image, but got an array of shape {X.shape} instead.")
+        X[:, :, :] = Xh
+        return X
+
+    def _eval_afm(self, X, stream, keep_device, want_paths, want_iters, out):
         ff = self._ff
         nx, ny, nz = self.scan_dim
         npix = nx * ny
@@ -342,16 +423,7 @@ class AFMulator:
         check(lib().ppgpu_relax_afm(tptr(ff.FE), iptr(ff.n), dptr(invCell), dptr(prm), npix, tptr(self._points), nz, tptr(o["FEs"]), tptr(o.get("paths")), tptr(o.get("iters")), nw, dptr(W), tptr(Xt), tptr(self.counter), stream_handle(stream)))
         if out is not None:
             return out
-        Xd = o["X"].view(nx, ny, nout)
-        if keep_device:
-            return Xd
-        Xh = Xd.cpu().numpy()
-        if X is None:
-            return Xh.copy()
-        if X.shape != (nx, ny, nout):
-            raise ValueError(f"Expected an array of shape {(nx, ny, nout)} for storing AFM image, but got an array of shape {X.shape} instead.")
-        X[:, :, :] = Xh
-        return X
+        return self._host_image(o["X"].view(nx, ny, nout), X, keep_device)
 
     def eval(self, xyzs, Zs, qs, rho_sample=None, sample_lvec=None, rot=np.eye(3), rot_center=None, REAs=None, X=None, plot_to_dir=None):
         """Prepare and evaluate the AFM image stack (AFMulator.py:142-173).  plot_to_dir: the
@@ -379,6 +451,7 @@ class AFMulator:
 
     def downloadFF(self):
         """The force field as [nx, ny, nz, 4] float32 (Fx, Fy, Fz, E)."""
+        self.join()
         return self._ff.grid4.cpu().numpy()
 
     def plot_images(self, X, outdir="afm_images", prefix="df", **plot_kwargs):

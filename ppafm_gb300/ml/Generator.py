@@ -7,9 +7,10 @@ blocking ``afmulator(...)`` call that ends with a device-to-host copy.  Here an 
 queued on the CUDA stream -- force field, relaxation and Δf written into its slot of one
 device buffer per batch (``_ImageBatch``) -- and the whole batch goes to the host in one
 copy.  The host prepares the next molecule (placement, pair parameters, atom records) while
-the GPU works on the previous ones.  The only synchronisation per image left is the one a
-user asks for by overriding ``InverseAFMtrainer.on_afm_end``, which sees the image as a host
-array in ``self.Xs``.
+the GPU works on the previous ones, and the AFMulator runs in its overlap mode, so each
+image's force field runs beside the previous image's relaxation.  The only synchronisation
+per image left is the one a user asks for by overriding ``InverseAFMtrainer.on_afm_end``,
+which sees the image as a host array in ``self.Xs``.
 
 Behaviour kept from the reference (by the same public names, arguments, callbacks and
 attributes): molecules read from xyz files or taken from a sample iterator; the molecule
@@ -102,6 +103,9 @@ class _TrainerBase:
     its randomisation, the callbacks, and the per-image call into the AFMulator."""
 
     def _init_common(self, afmulator, aux_maps, batch_size, distAbove, iZPPs):
+        # images queued back to back: each image's force field runs beside the previous
+        # image's relaxation (AFMulator.set_overlap); the host copies join the streams first
+        afmulator.set_overlap(True)
         self.afmulator = afmulator
         self.aux_maps = aux_maps
         self.batch_size = batch_size
@@ -259,12 +263,15 @@ class InverseAFMtrainer(_TrainerBase):
                 afm.prepareFF(self.xyzs, self.Zs, self.qs, REAs=self.REAs)
                 image = batch.slot(t, s)
                 afm.evalAFM(out=image)
+                if host_each:
+                    afm.join()
                 self.Xs = image.cpu().numpy() if host_each else image
                 self.on_afm_end()
             xyzqs = np.column_stack([self.xyzs, self.qs])
             for store, aux_map in zip(aux, self.aux_maps):
                 store.append(aux_map(xyzqs, self.Zs))
             self.counter += 1
+        afm.join()
         host = batch.to_host()  # [tips, n, ...]: one copy per batch
         self.last_timing["batch"] = time.perf_counter() - t0
         return list(host), [np.stack(store) for store in aux], mols
@@ -440,6 +447,7 @@ class GeneratorAFMtrainer(_TrainerBase):
             aux.append([aux_map(xyzqs, Zs, pot, rot) for aux_map in self.aux_maps])
         if not mols:
             raise StopIteration
+        self.afmulator.join()
         Xs = batch.to_host(len(mols))  # one copy per batch
         self.last_timing["batch"] = time.perf_counter() - t0
         return Xs, np.array(aux), mols, np.array(windows)
