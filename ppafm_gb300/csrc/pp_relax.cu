@@ -256,8 +256,10 @@ struct AfmPrm {
 
 __device__ __forceinline__ float dot3(float3 a, const float *b) { return a.x * b[0] + a.y * b[1] + a.z * b[2]; }
 
-__global__ void __launch_bounds__(RELAX_THREADS) relax_afm_kernel(const AfmPrm P) {
-    const int p = blockIdx.x * RELAX_THREADS + threadIdx.x;
+constexpr int AFM_RELAX_THREADS = 64;  // small blocks spread the strokes evenly over the SMs
+
+__global__ void __launch_bounds__(AFM_RELAX_THREADS) relax_afm_kernel(const AfmPrm P) {
+    const int p = blockIdx.x * AFM_RELAX_THREADS + threadIdx.x;
     bool active = p < P.npix && P.nz > 0;
     const float3 dTip = make_float3(P.tC[0] * P.zstep_w, P.tC[1] * P.zstep_w, P.tC[2] * P.zstep_w);
     // dpos0 rotated to the lab frame (rotMatT)
@@ -567,8 +569,8 @@ extern "C" int ppgpu_relax_afm(const float *FE, const int *n, const double *inv_
     P.nw = X ? nw : 0;
     for (int i = 0; i < P.nw; i++) P.W[i] = (float)weights[i];
     P.iter_total = iter_total;
-    const unsigned nblk = (unsigned)((npix + RELAX_THREADS - 1) / RELAX_THREADS);
-    relax_afm_kernel<<<nblk, RELAX_THREADS, 0, (cudaStream_t)stream>>>(P);
+    const unsigned nblk = (unsigned)((npix + AFM_RELAX_THREADS - 1) / AFM_RELAX_THREADS);
+    relax_afm_kernel<<<nblk, AFM_RELAX_THREADS, 0, (cudaStream_t)stream>>>(P);
     PPGPU_CHECK_LAUNCH("relax_afm_kernel");
     return set_ok();
 }
