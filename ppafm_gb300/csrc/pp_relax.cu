@@ -256,7 +256,7 @@ struct AfmPrm {
 
 __device__ __forceinline__ float dot3(float3 a, const float *b) { return a.x * b[0] + a.y * b[1] + a.z * b[2]; }
 
-constexpr int AFM_RELAX_THREADS = 64;  // small blocks spread the strokes evenly over the SMs
+constexpr int AFM_RELAX_THREADS = 128;  // as the single-grid kernel: packs beside the next image's force field
 
 __global__ void __launch_bounds__(AFM_RELAX_THREADS) relax_afm_kernel(const AfmPrm P) {
     const int p = blockIdx.x * AFM_RELAX_THREADS + threadIdx.x;
