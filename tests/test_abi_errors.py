@@ -1,8 +1,8 @@
-"""The device API's argument checks through the C ABI, on the CPU: each call below is
-rejected (or, for empty work, accepted) before the library touches a GPU, with
-PPGPU_ERR_ARG (1) and a message naming the problem in ppgpu_last_error -- the error
-behaviour a caller binding include/ppgpu.h relies on.  Pointers that the checks do not
-dereference are placeholders."""
+"""The C ABI's error behaviour, on the CPU: each call below is rejected (or, for empty work,
+accepted) before the library touches a GPU -- the device API with PPGPU_ERR_ARG (1), the
+drop-in symbols called before the state they need with PPGPU_ERR_STATE (3) -- and a message
+naming the problem in ppgpu_last_error: what a caller binding include/ppgpu.h relies on.
+Pointers that the checks do not dereference are placeholders."""
 
 import ctypes
 
@@ -108,3 +108,55 @@ def test_no_allocation_entry_point_limits(L):
     assert "chunk" in _msg(L)
     assert L.ppgpu_lj_grid_f64_noalloc(None, None, _ip(n), _dp(CELL), 4, FAKE, FAKE, None) == PPGPU_OK
     assert L.ppgpu_last_status() == PPGPU_OK
+
+
+DROPIN_SCRIPT = r"""
+import ctypes, numpy as np, sys
+sys.path.insert(0, sys.argv[1])
+from ppafm_gb300 import _lib, core
+L = _lib.load()
+ip = lambda a: np.ascontiguousarray(a, dtype=np.int32).ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+dp = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+rT = np.zeros((2, 2, 3, 3)); rs = np.zeros_like(rT); fs = np.zeros_like(rT)
+out = []
+# before setGridN / setGridCell: the relaxation and the force fields report a state error
+L.relaxTipStrokes_omp(2, 2, 1, 1, 3, dp(rT), dp(rs), dp(fs), None)
+out.append((L.ppgpu_last_status(), L.ppgpu_last_error().decode()))
+L.getLennardJonesFF(1, dp(np.zeros(3)), dp(np.ones(2)))
+out.append((L.ppgpu_last_status(), L.ppgpu_last_error().decode()))
+core.setGridN([8, 8, 8]); core.setGridCell(np.eye(3) * 8.0)
+# grid set, no force-field pointer: the relaxation still refuses; a force field with nothing to
+# store does nothing (the reference computes and stores nothing either)
+L.relaxTipStrokes_omp(2, 2, 1, 1, 3, dp(rT), dp(rs), dp(fs), None)
+out.append((L.ppgpu_last_status(), L.ppgpu_last_error().decode()))
+L.getLennardJonesFF(1, dp(np.zeros(3)), dp(np.ones(2)))
+out.append((L.ppgpu_last_status(), ""))
+# the Python wrappers turn the status into an exception
+try:
+    core.relaxTipStrokes_omp(rT, rs, fs)
+    out.append("no exception")
+except _lib.PPGPUError as e:
+    out.append("raised: " + str(e))
+print(repr(out))
+"""
+
+
+def test_dropin_state_errors():
+    """The drop-in symbols are void like the reference's; called before the state they need
+    (grid shape and cell, the borrowed force-field pointer) they do nothing and report
+    PPGPU_ERR_STATE (3) through ppgpu_last_status, which the Python wrappers raise.  Run in a
+    fresh process: the drop-in state is process-global."""
+    import ast
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", DROPIN_SCRIPT, root], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = ast.literal_eval(r.stdout.strip().splitlines()[-1])
+    assert out[0][0] == 3 and "setGridN/setGridCell" in out[0][1]
+    assert out[1][0] == 3 and "setGridN/setGridCell" in out[1][1]
+    assert out[2][0] == 3 and "setFF_Fpointer" in out[2][1]
+    assert out[3][0] == PPGPU_OK
+    assert out[4].startswith("raised:") and "setFF_Fpointer" in out[4]
